@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 wavefront aligner (one JSON line on rank 0).
+
+Workload (default): 1,000,000 synthetic gap-affine (4,6,2) pairs per GPU,
+|P| ~ U[500,1500], divergence ~ U[0,15%], full CIGAR, end-to-end, memory
+mode high -- the batched configuration the headline metric is quoted on.
+One step = one batched alignment of all pairs of this rank.
+
+value   pairs/s with inputs resident in HBM (kernels only, CUDA events on the
+        launching stream); inputs (~2 GB) exceed the 126 MB L2 between steps
+e2e     pairs/s through the public host API wavefront_align_batch(): per step
+        the H2D copy of the inputs from pinned memory and the D2H copy of the
+        results (scores, status, CIGAR operations) are inside the timed region
+--impl reference   the CPU implementation of the path on the host cores
+        (oracle/_ref when the reference was built here, else the C restatement
+        in oracle/), on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "wfa2-lib_gb300"))
+
+METRIC = "pairs/s bit-exact score+CIGAR, batched vs per-pair on 1 GB300; p50/p99 latency"
+INT_OPS_PER_CELL = 20      # gap-affine int32 ops per WFA cell
+INT_OPS_PER_EXT_WORD = 8   # per additional 32-base extend word
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pairs", type=int, default=1_000_000, help="pairs per GPU")
+    ap.add_argument("--workload", type=int, default=1)
+    ap.add_argument("--score-only", action="store_true")
+    ap.add_argument("--per-pair-sample", type=int, default=2000)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0,
+                    help="target wall time of the bounded CPU-baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gen_pinned(W, torch, workload, n, first):
+    """Seeded pairs in pinned host memory."""
+    def alloc(nbytes):
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+    p = W.generate(workload, n, first=first, alloc=alloc)
+
+    def pin(a):
+        t = torch.empty(a.shape, dtype={np.int64: torch.int64, np.int32: torch.int32}[a.dtype.type],
+                        pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+    return W.Pairs(p.seqs, pin(p.p_off), pin(p.p_len), pin(p.t_off), pin(p.t_len))
+
+
+def cpu_sample(O, W, workload, score_only, target_s, first, kind):
+    """Times the CPU path on a bounded sample; returns (pairs/s, sample n, threads, res)."""
+    threads = os.cpu_count() or 1
+    pen = O.Penalties()
+    n = 1000
+    while True:
+        p = W.generate(workload, n, first=first)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        t0 = time.perf_counter()
+        r = O.align(b, pen, score_only=score_only, kind=kind, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s * 0.5 or n >= 200_000:
+            return n / dt, n, threads, r, p, dt
+        n = min(200_000, int(n * max(2.0, target_s / max(dt, 1e-3))))
+
+
+def run_reference(args, rank):
+    """--impl reference: the CPU implementation on the host cores."""
+    if rank != 0:
+        return
+    import wfa2gpu as W
+    from oracle import oracle as O
+    W.build() if not os.path.exists(W.GEN_PATH) else None
+    O.build(ref=False)
+    kind = "reference" if O.have_reference() else "port"
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(O, W, args.workload, args.score_only, 1.0, 0, kind)
+    for _ in range(args.steps):
+        v, n, threads, _, _, dt = cpu_sample(O, W, args.workload, args.score_only,
+                                             args.cpu_seconds / max(args.steps, 1), 0, kind)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * n / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": kind,
+                         "sample": f"{n} pairs of the workload per step"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    names = {0: "100bp x 5 edits", 1: "500-1500bp, 0-15% divergence, 10% geometric indels",
+             2: "1-10kbp log-uniform, 5%, 20% long indels", 4: "lognormal 2kbp median, 1-20%"}
+    return {"workload": f"batched gap-affine(0,4,6,2) end-to-end "
+                        f"{'score-only' if args.score_only else 'full CIGAR'}, memory high, "
+                        f"{args.pairs} pairs/GPU of workload {args.workload} "
+                        f"({names.get(args.workload, '')})",
+            "pairs_per_gpu": args.pairs, "seq": "uint8 ASCII ACGT",
+            "l2": "inputs (~2 GB/GPU) larger than L2; no flush needed",
+            "parallelism": f"replicas x{args.gpus} (pairs sharded, no collective)"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    import wfa2gpu as W
+    from oracle import oracle as O
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if rank == 0 or not os.path.exists(W.LIB_PATH):
+        W.build() if not os.path.exists(W.LIB_PATH) else None
+    if dist:
+        dist.barrier()
+
+    # ------------------------------------------------------------ data
+    n = args.pairs
+    first = rank * n
+    p = gen_pinned(W, torch, args.workload, n, first)
+    max_len = p.max_len
+    cigar = not args.score_only
+    cap = p.p_len.astype(np.int64) + p.t_len.astype(np.int64)
+    ops_off = np.zeros(n + 1, np.int64)
+    np.cumsum(cap, out=ops_off[1:])
+
+    dev = torch.device("cuda", local)
+    seq_bytes = int(p.t_off[-1] + p.t_len[-1])
+    d_seqs = torch.from_numpy(p.seqs).to(dev)
+    d_poff = torch.from_numpy(p.p_off).to(dev)
+    d_plen = torch.from_numpy(p.p_len).to(dev)
+    d_toff = torch.from_numpy(p.t_off).to(dev)
+    d_tlen = torch.from_numpy(p.t_len).to(dev)
+    d_scores = torch.empty(n, dtype=torch.int32, device=dev)
+    d_status = torch.empty(n, dtype=torch.int32, device=dev)
+    d_ops = torch.empty(int(ops_off[-1]) + 16 if cigar else 16, dtype=torch.uint8, device=dev)
+    d_opsoff = torch.from_numpy(ops_off).to(dev)
+    d_opslen = torch.empty(n, dtype=torch.int32, device=dev)
+
+    cfg = W.Config(score_only=args.score_only)
+    al = W.Aligner(cfg)
+    stream = torch.cuda.current_stream(dev)
+
+    def step_device():
+        rc = al.align_batch_device(
+            n, d_seqs.data_ptr(), d_poff.data_ptr(), d_plen.data_ptr(), d_toff.data_ptr(),
+            d_tlen.data_ptr(), max_len, d_scores.data_ptr(), d_status.data_ptr(),
+            d_ops.data_ptr() if cigar else 0, d_opsoff.data_ptr() if cigar else 0,
+            d_opslen.data_ptr() if cigar else 0, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"wavefront_align_batch_device failed: {rc}")
+
+    for _ in range(max(args.warmup, 3)):
+        step_device()
+    torch.cuda.synchronize()
+    status = d_status.cpu().numpy()
+    if not (status == 0).all():
+        raise RuntimeError(f"{int((status != 0).sum())} pairs did not complete")
+
+    # ------------------------------------------------------------ timed (device-resident)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = al.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = al.launches - l0
+    clk = clocks.stop()
+    dev_s = ev0.elapsed_time(ev1) / 1000.0
+    if dist:
+        t = torch.tensor([dev_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * n * args.steps / dev_s
+
+    # ------------------------------------------------------------ e2e (host API)
+    e2e = None
+    if not args.no_e2e:
+        h_scores = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+        h_status = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+        h_ops = torch.empty(int(ops_off[-1]) + 16 if cigar else 16, dtype=torch.uint8,
+                            pin_memory=True).numpy()
+        h_opslen = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+        h_opsoff = torch.empty(n + 1, dtype=torch.int64, pin_memory=True).numpy()
+        h_opsoff[...] = ops_off
+
+        def step_host():
+            rc = al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len,
+                                ops_off=h_opsoff if cigar else None, scores=h_scores,
+                                status=h_status, ops=h_ops if cigar else None,
+                                ops_len=h_opslen if cigar else None)[0]
+            if rc != 0:
+                raise RuntimeError(f"wavefront_align_batch failed: {rc}")
+        step_host()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step_host()
+        e2e_s = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        h2d = seq_bytes + n * (8 + 4 + 8 + 4) + (n * 8 if cigar else 0)
+        d2h = n * 8 + ((n * 4 + int(ops_off[-1])) if cigar else 0)
+        e2e = {"value": world * n * args.steps / e2e_s, "unit": "pairs/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        # every result of the e2e path equals the device-resident path
+        assert np.array_equal(h_scores, d_scores.cpu().numpy())
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ------------------------------------------------------------ rank-0 extras
+    # per-pair drop-in: wavefront_align() once per pair from C
+    bl = C.CDLL(os.path.join(W.PKG_DIR, "lib", "libwfa2bench.so"))
+    bl.wf2g_bench_per_pair.restype = C.c_double
+    P = C.c_void_p
+    bl.wf2g_bench_per_pair.argtypes = [P, C.c_int, P, P, P, P, P, P, P, P]
+    k = min(args.per_pair_sample, n)
+    ps, pst, pl = (np.zeros(k, np.int32) for _ in range(3))
+
+    def ptr(a):
+        return C.c_void_p(a.ctypes.data)
+    pa = W.Aligner(cfg)
+    bl.wf2g_bench_per_pair(C.cast(pa._h, P), 50, ptr(p.seqs), ptr(p.p_off), ptr(p.p_len),
+                           ptr(p.t_off), ptr(p.t_len), ptr(ps), ptr(pst), ptr(pl))
+    per_pair_s = bl.wf2g_bench_per_pair(C.cast(pa._h, P), k, ptr(p.seqs), ptr(p.p_off),
+                                        ptr(p.p_len), ptr(p.t_off), ptr(p.t_len), ptr(ps),
+                                        ptr(pst), ptr(pl))
+    pa.close()
+    per_pair = k / per_pair_s
+    assert np.array_equal(ps, d_scores[:k].cpu().numpy())
+
+    # CPU baseline (bounded sample) and work units (WFA cells, extend chars)
+    cpu_v, cpu_n, cpu_threads, r, sp, _ = cpu_sample(O, W, args.workload, args.score_only,
+                                                     args.cpu_seconds, 0, "port")
+    # the bounded sample doubles as a parity spot-check of the timed results
+    if rank == 0 and first == 0:
+        m = min(cpu_n, n)
+        assert np.array_equal(r.score[:m], d_scores[:m].cpu().numpy())
+    cells_pp = float(r.cells.mean())
+    ext_words_pp = float(np.ceil(r.ext / 32.0).mean())
+    ops_pp = INT_OPS_PER_CELL * cells_pp + INT_OPS_PER_EXT_WORD * ext_words_pp
+    step_s = dev_s / args.steps
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    num_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak_tops = num_sms * 128 * sm_mhz * 1e6 / 1e12
+    achieved_tops = n * ops_pp / step_s / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    alg_bytes = seq_bytes + n * 4 + (int(np.sum(pl)) * n / k if cigar else 0)
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * step_s,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded SplitMix64 generator)", "config": workload_config(args),
+        "roofline": {"bound": "int32", "achieved": achieved_tops, "peak": peak_tops,
+                     "unit": "Tops/s", "frac": achieved_tops / peak_tops, "traffic": None,
+                     "units_per_launch": {"wfa_cells": n * cells_pp,
+                                          "ops_per_cell": INT_OPS_PER_CELL,
+                                          "ext_words": n * ext_words_pp},
+                     "peak_basis": f"{num_sms} SMs x 128 int32 lanes x {sm_mhz:.0f} MHz "
+                                   "(median SM clock sampled during the run)",
+                     "hbm": {"achieved_gbs": alg_bytes / step_s / 1e9, "peak_gbs": hbm_peak,
+                             "frac": alg_bytes / step_s / 1e9 / hbm_peak,
+                             "peak_basis": "MEASURED_PEAKS.json hbm_gbs (of measured)"}},
+        "cpu_baseline": {"value": cpu_v, "unit": "pairs/s", "cores": cpu_threads, "kind": "port",
+                         "sample": f"first {cpu_n} pairs of the workload, all host threads"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "per_pair_dropin": {"value": per_pair, "unit": "pairs/s",
+                            "sample": f"{k} wavefront_align() calls"},
+        "batched_over_per_pair": value / world / per_pair,
+        "cells_per_s": world * n * cells_pp * args.steps / dev_s,
+        "dp_cell_updates_per_s": float(np.sum(p.p_len.astype(np.float64) * p.t_len)) * world *
+        args.steps / dev_s,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,252 @@
+"""ctypes front-end for the CPU checker.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline / --impl reference legs of bench.py.  Two back-ends share one
+calling convention:
+
+* ``port``      -- oracle/_build/libwfa_oracle.so, the C restatement of the
+                   reference algorithm (wfa_oracle.c); builds on any host.
+* ``reference`` -- oracle/_ref/libwfa_ref.so, the unmodified reference library
+                   compiled from its sources (only where they are present).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "libwfa_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libwfa_ref.so")
+
+GAP_AFFINE = 3
+GAP_AFFINE_2P = 4
+MEM_HIGH, MEM_MED, MEM_LOW, MEM_ULTRALOW = 0, 1, 2, 3
+
+
+@dataclass
+class Penalties:
+    """Penalties as the reference's attribute structs hold them (match <= 0)."""
+
+    metric: int = GAP_AFFINE
+    match: int = 0
+    mismatch: int = 4
+    gap_opening1: int = 6
+    gap_extension1: int = 2
+    gap_opening2: int = 24
+    gap_extension2: int = 1
+
+    def cfg(self, memory_mode=MEM_HIGH, score_only=False, max_steps=0):
+        return np.array(
+            [self.metric, self.match, self.mismatch, self.gap_opening1, self.gap_extension1,
+             self.gap_opening2, self.gap_extension2, memory_mode, int(bool(score_only)),
+             max_steps], dtype=np.int32)
+
+
+def build(ref: bool = False) -> None:
+    targets = ["oracle"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+_LIBS = {}
+
+
+def _lib(kind: str):
+    if kind in _LIBS:
+        return _LIBS[kind]
+    path = PORT_LIB if kind == "port" else REF_LIB
+    if not os.path.exists(path):
+        build(ref=(kind == "reference"))
+    lib = ctypes.CDLL(path)
+    fn = lib.oracle_align_batch if kind == "port" else lib.ref_align_batch
+    P = ctypes.c_void_p
+    fn.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+    fn.restype = ctypes.c_int
+    _LIBS[kind] = fn
+    return fn
+
+
+def have_reference() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+@dataclass
+class PairBatch:
+    """Pairs packed as one ASCII buffer with offsets/lengths (the batch layout)."""
+
+    seqs: np.ndarray  # uint8
+    p_off: np.ndarray  # int64
+    p_len: np.ndarray  # int32
+    t_off: np.ndarray  # int64
+    t_len: np.ndarray  # int32
+
+    @property
+    def n(self) -> int:
+        return int(self.p_len.shape[0])
+
+    @staticmethod
+    def from_lists(patterns, texts) -> "PairBatch":
+        parts, p_off, t_off = [], [], []
+        pos = 0
+        for p, t in zip(patterns, texts):
+            pb = p.encode() if isinstance(p, str) else bytes(p)
+            tb = t.encode() if isinstance(t, str) else bytes(t)
+            p_off.append(pos)
+            parts.append(pb)
+            pos += len(pb)
+            t_off.append(pos)
+            parts.append(tb)
+            pos += len(tb)
+        buf = np.frombuffer(b"".join(parts) + b"\0" * 16, dtype=np.uint8).copy()
+        return PairBatch(buf, np.array(p_off, np.int64),
+                         np.array([len(p) for p in patterns], np.int32),
+                         np.array(t_off, np.int64), np.array([len(t) for t in texts], np.int32))
+
+    def pattern(self, i) -> bytes:
+        o = int(self.p_off[i])
+        return self.seqs[o:o + int(self.p_len[i])].tobytes()
+
+    def text(self, i) -> bytes:
+        o = int(self.t_off[i])
+        return self.seqs[o:o + int(self.t_len[i])].tobytes()
+
+    def ops_offsets(self) -> np.ndarray:
+        cap = self.p_len.astype(np.int64) + self.t_len.astype(np.int64)
+        off = np.zeros(self.n + 1, np.int64)
+        np.cumsum(cap, out=off[1:])
+        return off
+
+
+@dataclass
+class AlignResult:
+    score: np.ndarray
+    status: np.ndarray
+    ops: np.ndarray  # uint8 buffer
+    ops_off: np.ndarray  # int64 (n+1)
+    ops_len: np.ndarray
+    cells: np.ndarray
+    ext: np.ndarray
+
+    def cigar(self, i) -> str:
+        o = int(self.ops_off[i])
+        return self.ops[o:o + int(self.ops_len[i])].tobytes().decode()
+
+
+def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=False,
+          max_steps=0, kind="port", nthreads=0) -> AlignResult:
+    fn = _lib(kind)
+    n = batch.n
+    cfg = pen.cfg(memory_mode, score_only, max_steps)
+    score = np.zeros(n, np.int32)
+    status = np.zeros(n, np.int32)
+    ops_off = batch.ops_offsets()
+    ops = np.zeros(max(int(ops_off[-1]), 1), np.uint8)
+    ops_len = np.zeros(n, np.int32)
+    cells = np.zeros(n, np.int64)
+    ext = np.zeros(n, np.int64)
+
+    def ptr(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    rc = fn(ptr(cfg), n, ptr(batch.seqs), ptr(batch.p_off), ptr(batch.p_len), ptr(batch.t_off),
+            ptr(batch.t_len), ptr(score), ptr(status), ptr(ops), ptr(ops_off), ptr(ops_len),
+            ptr(cells), ptr(ext), int(nthreads))
+    if rc != 0:
+        raise ValueError("invalid configuration for the CPU checker")
+    return AlignResult(score, status, ops, ops_off, ops_len, cells, ext)
+
+
+# ---------------------------------------------------------------- formats
+def read_seq_file(path) -> PairBatch:
+    """Reads the reference's '.seq' format: '>pattern' / '<text' line pairs."""
+    pats, txts = [], []
+    with open(path, "rb") as f:
+        lines = [l.rstrip(b"\r\n") for l in f if l.strip()]
+    for i in range(0, len(lines) - 1, 2):
+        assert lines[i][:1] == b">" and lines[i + 1][:1] == b"<"
+        pats.append(lines[i][1:])
+        txts.append(lines[i + 1][1:])
+    return PairBatch.from_lists(pats, txts)
+
+
+def cigar_rle(ops: str) -> str:
+    """RLE as the reference prints it with matches shown (alignment/cigar.c:436-470)."""
+    if not ops:
+        return "-"
+    out = []
+    last, n = ops[0], 1
+    for c in ops[1:]:
+        if c == last:
+            n += 1
+        else:
+            out.append(f"{n}{last}")
+            last, n = c, 1
+    out.append(f"{n}{last}")
+    return "".join(out)
+
+
+def rescore_affine(ops: str, match: int, x: int, o: int, e: int) -> int:
+    """Score of a CIGAR under gap-affine penalties (alignment/cigar.c:277-303)."""
+    score, last = 0, ""
+    for c in ops:
+        if c == "M":
+            score -= match
+        elif c == "X":
+            score -= x
+        elif c in "DI":
+            score -= e + (0 if last == c else o)
+        last = c
+    return score
+
+
+def rescore_affine2p(ops: str, match: int, x: int, o1: int, e1: int, o2: int, e2: int) -> int:
+    """Score under gap-affine-2p penalties (alignment/cigar.c:304-346)."""
+    def op_score(c, n):
+        if c == "M":
+            return match * n
+        if c == "X":
+            return x * n
+        return min(o1 + e1 * n, o2 + e2 * n)
+    if not ops:
+        return 0
+    score, last, n = 0, ops[0], 0
+    for c in ops:
+        if c != last:
+            score -= op_score(last, n)
+            last, n = c, 0
+        n += 1
+    score -= op_score(last, n)
+    return score
+
+
+def rescore(ops: str, pen: Penalties) -> int:
+    if pen.metric == GAP_AFFINE:
+        return rescore_affine(ops, pen.match, pen.mismatch, pen.gap_opening1, pen.gap_extension1)
+    return rescore_affine2p(ops, pen.match, pen.mismatch, pen.gap_opening1, pen.gap_extension1,
+                            pen.gap_opening2, pen.gap_extension2)
+
+
+def check_cigar(ops: str, pattern: bytes, text: bytes) -> bool:
+    """Replays a CIGAR against its sequences (alignment/cigar.c:347-420)."""
+    v = h = 0
+    for c in ops:
+        if c == "M":
+            if v >= len(pattern) or h >= len(text) or pattern[v] != text[h]:
+                return False
+            v += 1
+            h += 1
+        elif c == "X":
+            if v >= len(pattern) or h >= len(text) or pattern[v] == text[h]:
+                return False
+            v += 1
+            h += 1
+        elif c == "I":
+            h += 1
+        elif c == "D":
+            v += 1
+        else:
+            return False
+    return v == len(pattern) and h == len(text)

@@ -1,0 +1,503 @@
+/*
+ * wfa_oracle.c -- CPU restatement of WFA2-lib's exact wavefront alignment
+ * (gap-affine and gap-affine-2p, end-to-end, score-only or full CIGAR).
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the checker the GPU path is compared
+ * against.  Nothing in the product library links or calls it.
+ *
+ * It restates, in plain C and with the reference's own semantics, the
+ * unidirectional high-memory algorithm of smarco/WFA2-lib:
+ *   - penalty set-up and Eizenga transform  wavefront/wavefront_penalties.c:95-173
+ *   - max score scope                        wavefront/wavefront_components.c:81-120
+ *   - input fetch (score offsets)            wavefront/wavefront_compute.c:306-352
+ *   - output limits                          wavefront/wavefront_compute.c:40-87
+ *   - output allocation rule (I/D NULL)      wavefront/wavefront_compute.c:409-494
+ *   - compute kernels                        wavefront/wavefront_compute_affine.c:44-86,
+ *                                            wavefront/wavefront_compute_affine2p.c:45-106
+ *   - end trimming                           wavefront/wavefront_compute.c:579-613
+ *   - extend (exact LCP along diagonals)     wavefront/wavefront_extend.c:86-121,
+ *                                            wavefront/wavefront_extend_kernels.c:68-123
+ *   - end-to-end termination                 wavefront/wavefront_termination.c:37-60
+ *   - driver loop, limits, classic score     wavefront/wavefront_unialign.c:98-273,
+ *                                            wavefront/wavefront_compute.c:108-120
+ *   - backtrace with type priorities        wavefront/wavefront_backtrace.c:36-529
+ *
+ * The reference pads every input wavefront with NULL offsets beyond its
+ * trimmed range [lo,hi] (wavefront/wavefront_compute.c:498-575); here a read
+ * outside [lo,hi] simply returns NULL, which is the same value.
+ *
+ * Memory modes med/low (piggyback back-trace) are reported identical to high
+ * on the reference's golden files (tests/wfa.utest.sh:67-78), so they are
+ * served by the same high-memory restatement.  Ultralow (BiWFA) is restated
+ * in oracle_bialign() below.
+ */
+#include "wfa_oracle.h"
+#include "wfa_oracle_internal.h"
+
+#include <limits.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static orow_t k_null_row = {1, 1, 1, -1, 0, NULL};
+
+static int imin(int a, int b) { return a < b ? a : b; }
+static int imax(int a, int b) { return a > b ? a : b; }
+
+/* wavefront/wavefront_penalties.c:95-173 (Eizenga transform when match<0) */
+static int setup_penalties(const int* cfg, pen_t* p) {
+  p->metric = cfg[0];
+  const int m = cfg[1], x = cfg[2], o1 = cfg[3], e1 = cfg[4], o2 = cfg[5], e2 = cfg[6];
+  if (p->metric != 3 && p->metric != 4) return -1;
+  if (m > 0 || x <= 0 || o1 < 0 || e1 <= 0) return -1;
+  if (p->metric == 4 && (o2 < 0 || e2 <= 0)) return -1;
+  if (m < 0) {
+    p->match = m;
+    p->x = 2 * x - 2 * m;
+    p->o1 = 2 * o1;
+    p->e1 = 2 * e1 - m;
+    p->o2 = 2 * o2;
+    p->e2 = 2 * e2 - m;
+  } else {
+    p->match = 0;
+    p->x = x;
+    p->o1 = o1;
+    p->e1 = e1;
+    p->o2 = o2;
+    p->e2 = e2;
+  }
+  if (p->metric == 3) {
+    p->o2 = -1;
+    p->e2 = -1;
+  }
+  /* wavefront/wavefront_components.c:81-120 */
+  int indel = p->o1 + p->e1;
+  if (p->metric == 4) indel = imax(indel, p->o2 + p->e2);
+  p->scope = imax(indel, p->x) + 1;
+  p->score_only = cfg[8] != 0;
+  p->max_steps = cfg[9] > 0 ? cfg[9] : INT_MAX;
+  return 0;
+}
+
+static orow_t* row_at(oracle_ws_t* ws, int s, int c) { return &ws->rows[(int64_t)s * NCOMP + c]; }
+
+static void ws_ensure_rows(oracle_ws_t* ws, int s) {
+  if (s < ws->rows_cap) return;
+  int ncap = ws->rows_cap ? ws->rows_cap : 1024;
+  while (ncap <= s) ncap *= 2;
+  ws->rows = (orow_t*)realloc(ws->rows, (size_t)ncap * NCOMP * sizeof(orow_t));
+  memset(ws->rows + (size_t)ws->rows_cap * NCOMP, 0,
+         (size_t)(ncap - ws->rows_cap) * NCOMP * sizeof(orow_t));
+  ws->rows_cap = ncap;
+}
+
+static int32_t* ws_alloc(oracle_ws_t* ws, int n) {
+  while (ws->cur < ws->nchunks && ws->chunks[ws->cur].used + n > ws->chunks[ws->cur].cap) ws->cur++;
+  if (ws->cur == ws->nchunks) {
+    int64_t cap = (int64_t)1 << 20;
+    if (ws->nchunks) cap = ws->chunks[ws->nchunks - 1].cap * 2;
+    if (cap < n) cap = n;
+    ws->chunks = (chunk_t*)realloc(ws->chunks, (size_t)(ws->nchunks + 1) * sizeof(chunk_t));
+    ws->chunks[ws->nchunks].mem = (int32_t*)malloc((size_t)cap * sizeof(int32_t));
+    ws->chunks[ws->nchunks].cap = cap;
+    ws->chunks[ws->nchunks].used = 0;
+    ws->nchunks++;
+  }
+  chunk_t* c = &ws->chunks[ws->cur];
+  int32_t* p = c->mem + c->used;
+  c->used += n;
+  return p;
+}
+
+static void ws_reset(oracle_ws_t* ws) {
+  for (int i = 0; i < ws->nchunks; ++i) ws->chunks[i].used = 0;
+  ws->cur = 0;
+}
+
+static void ws_free(oracle_ws_t* ws) {
+  for (int i = 0; i < ws->nchunks; ++i) free(ws->chunks[i].mem);
+  free(ws->chunks);
+  free(ws->rows);
+}
+
+static inline int32_t rd(const orow_t* r, int k) {
+  if (!r->exists || r->null || k < r->lo || k > r->hi) return WF_NULL;
+  return r->mem[k - r->base];
+}
+
+/* wavefront/wavefront_compute.c:354-368 (fetch with NULL substitution) */
+static const orow_t* fetch(oracle_ws_t* ws, int s, int c) {
+  if (s < 0) return &k_null_row;
+  const orow_t* r = row_at(ws, s, c);
+  if (!r->exists || r->null) return &k_null_row;
+  return r;
+}
+
+/* wavefront/wavefront_compute.c:579-613 */
+static void trim_row(orow_t* r, int plen, int tlen) {
+  int k;
+  for (k = r->hi; k >= r->lo; --k) {
+    const int32_t off = r->mem[k - r->base];
+    const uint32_t h = (uint32_t)off;
+    const uint32_t v = (uint32_t)(off - k);
+    if (h <= (uint32_t)tlen && v <= (uint32_t)plen) break;
+  }
+  r->hi = k;
+  const int hi = r->hi;
+  for (k = r->lo; k <= hi; ++k) {
+    const int32_t off = r->mem[k - r->base];
+    const uint32_t h = (uint32_t)off;
+    const uint32_t v = (uint32_t)(off - k);
+    if (h <= (uint32_t)tlen && v <= (uint32_t)plen) break;
+  }
+  r->lo = k;
+  r->null = (r->lo > r->hi);
+}
+
+/* One compute step at score s (wavefront/wavefront_compute_affine.c:229-260 and
+ * wavefront/wavefront_compute_affine2p.c:322-360).  Returns cells computed. */
+static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, int tlen,
+                            int* null_steps) {
+  const int a2p = (p->metric == 4);
+  ws_ensure_rows(ws, s);
+  const orow_t* mx = fetch(ws, s - p->x, C_M);
+  const orow_t* mo1 = fetch(ws, s - p->o1 - p->e1, C_M);
+  const orow_t* i1e = fetch(ws, s - p->e1, C_I1);
+  const orow_t* d1e = fetch(ws, s - p->e1, C_D1);
+  const orow_t* mo2 = &k_null_row;
+  const orow_t* i2e = &k_null_row;
+  const orow_t* d2e = &k_null_row;
+  if (a2p) {
+    mo2 = fetch(ws, s - p->o2 - p->e2, C_M);
+    i2e = fetch(ws, s - p->e2, C_I2);
+    d2e = fetch(ws, s - p->e2, C_D2);
+  }
+  for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, s, c), 0, sizeof(orow_t));
+  if (mx->null && mo1->null && i1e->null && d1e->null && mo2->null && i2e->null && d2e->null) {
+    (*null_steps)++;
+    return 0;
+  }
+  *null_steps = 0;
+  /* wavefront/wavefront_compute.c:40-87 (null rows carry lo=1,hi=-1) */
+  int lo = mx->lo, hi = mx->hi;
+  lo = imin(lo, mo1->lo - 1);
+  hi = imax(hi, mo1->hi + 1);
+  lo = imin(lo, i1e->lo + 1);
+  hi = imax(hi, i1e->hi + 1);
+  lo = imin(lo, d1e->lo - 1);
+  hi = imax(hi, d1e->hi - 1);
+  if (a2p) {
+    lo = imin(lo, mo2->lo - 1);
+    hi = imax(hi, mo2->hi + 1);
+    lo = imin(lo, i2e->lo + 1);
+    hi = imax(hi, i2e->hi + 1);
+    lo = imin(lo, d2e->lo - 1);
+    hi = imax(hi, d2e->hi - 1);
+  }
+  const int width = hi - lo + 1;
+  /* wavefront/wavefront_compute.c:447-492: I/D outputs exist only if an input does */
+  const int has[NCOMP] = {1, (!mo1->null || !i1e->null), (!mo1->null || !d1e->null),
+                          a2p && (!mo2->null || !i2e->null), a2p && (!mo2->null || !d2e->null)};
+  int32_t* out[NCOMP];
+  for (int c = 0; c < NCOMP; ++c) {
+    orow_t* r = row_at(ws, s, c);
+    out[c] = NULL;
+    if (has[c]) {
+      r->mem = ws_alloc(ws, width);
+      r->exists = 1;
+      r->base = lo;
+      r->lo = lo;
+      r->hi = hi;
+      out[c] = r->mem;
+    }
+  }
+  int32_t victim[4]; /* output for non-existing I/D components */
+  for (int k = lo; k <= hi; ++k) {
+    const int idx = k - lo;
+    /* wavefront/wavefront_compute_affine.c:65-85 */
+    const int32_t ins1_o = rd(mo1, k - 1), ins1_e = rd(i1e, k - 1);
+    const int32_t ins1 = (ins1_o > ins1_e ? ins1_o : ins1_e) + 1;
+    const int32_t del1_o = rd(mo1, k + 1), del1_e = rd(d1e, k + 1);
+    const int32_t del1 = del1_o > del1_e ? del1_o : del1_e;
+    int32_t ins = ins1, del = del1;
+    if (out[C_I1]) out[C_I1][idx] = ins1; else victim[0] = ins1;
+    if (out[C_D1]) out[C_D1][idx] = del1; else victim[1] = del1;
+    if (a2p) {
+      /* wavefront/wavefront_compute_affine2p.c:72-101 */
+      const int32_t ins2_o = rd(mo2, k - 1), ins2_e = rd(i2e, k - 1);
+      const int32_t ins2 = (ins2_o > ins2_e ? ins2_o : ins2_e) + 1;
+      const int32_t del2_o = rd(mo2, k + 1), del2_e = rd(d2e, k + 1);
+      const int32_t del2 = del2_o > del2_e ? del2_o : del2_e;
+      if (out[C_I2]) out[C_I2][idx] = ins2; else victim[2] = ins2;
+      if (out[C_D2]) out[C_D2][idx] = del2; else victim[3] = del2;
+      ins = ins > ins2 ? ins : ins2;
+      del = del > del2 ? del : del2;
+    }
+    const int32_t misms = rd(mx, k) + 1;
+    int32_t mmax = misms > ins ? misms : ins;
+    mmax = del > mmax ? del : mmax;
+    const uint32_t h = (uint32_t)mmax;
+    const uint32_t v = (uint32_t)(mmax - k);
+    if (h > (uint32_t)tlen) mmax = WF_NULL;
+    if (v > (uint32_t)plen) mmax = WF_NULL;
+    out[C_M][idx] = mmax;
+  }
+  for (int c = 0; c < NCOMP; ++c) {
+    orow_t* r = row_at(ws, s, c);
+    if (r->exists) trim_row(r, plen, tlen);
+  }
+  return width;
+}
+
+/* Exact LCP along a diagonal, stopping at the sequence ends
+ * (wavefront/wavefront_extend_kernels.c:68-92; the reference stops on the EOS
+ * sentinels of wavefront/wavefront_sequences.c:37-39). */
+static inline int lcp(const char* P, int plen, const char* T, int tlen, int v, int h) {
+  int n = 0;
+  const int lim = imin(plen - v, tlen - h);
+  while (n + 8 <= lim) {
+    uint64_t a, b;
+    memcpy(&a, P + v + n, 8);
+    memcpy(&b, T + h + n, 8);
+    const uint64_t d = a ^ b;
+    if (d) {
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+      return n + (__builtin_ctzll(d) >> 3);
+#else
+      break;
+#endif
+    }
+    n += 8;
+  }
+  while (n < lim && P[v + n] == T[h + n]) ++n;
+  return n;
+}
+
+/* wavefront/wavefront_backtrace.c:36-59: (offset<<4)|type, larger wins */
+enum { BT_M = 9, BT_D2E = 8, BT_D2O = 7, BT_D1E = 6, BT_D1O = 5, BT_I2E = 4, BT_I2O = 3, BT_I1E = 2, BT_I1O = 1 };
+
+static inline int64_t cand(oracle_ws_t* ws, int s, int c, int k, int add, int type) {
+  if (s < 0) return WF_NULL;
+  const orow_t* r = row_at(ws, s, c);
+  if (!r->exists || k < r->lo || k > r->hi) return WF_NULL;
+  return ((int64_t)(r->mem[k - r->base] + add) << 4) | type;
+}
+static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+
+/* wavefront/wavefront_backtrace.c:320-529, writing into a reversed buffer.
+ * Returns the number of operations, or -1 on an inconsistent trace. */
+static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int score, int k_end,
+                     int32_t off_end, char* rev) {
+  int n = 0;
+  int mat = C_M;
+  int s = score, k = k_end;
+  int32_t offset = off_end;
+  int h = offset, v = offset - k;
+  const int a2p = (p->metric == 4);
+  /* end-to-end: v==plen, h==tlen, so no trailing gaps (wavefront/wavefront_backtrace.c:356-365) */
+  while (v > 0 && h > 0 && s > 0) {
+    const int sx = s - p->x, so1 = s - p->o1 - p->e1, so2 = s - p->o2 - p->e2;
+    const int se1 = s - p->e1, se2 = s - p->e2;
+    int64_t mall;
+    switch (mat) {
+      case C_M: {
+        const int64_t misms = cand(ws, sx, C_M, k, 1, BT_M);
+        const int64_t i1 = max64(cand(ws, so1, C_M, k - 1, 1, BT_I1O), cand(ws, se1, C_I1, k - 1, 1, BT_I1E));
+        const int64_t d1 = max64(cand(ws, so1, C_M, k + 1, 0, BT_D1O), cand(ws, se1, C_D1, k + 1, 0, BT_D1E));
+        if (!a2p) {
+          mall = max64(misms, max64(i1, d1));
+        } else {
+          const int64_t i2 = max64(cand(ws, so2, C_M, k - 1, 1, BT_I2O), cand(ws, se2, C_I2, k - 1, 1, BT_I2E));
+          const int64_t d2 = max64(cand(ws, so2, C_M, k + 1, 0, BT_D2O), cand(ws, se2, C_D2, k + 1, 0, BT_D2E));
+          mall = max64(misms, max64(max64(i1, i2), max64(d1, d2)));
+        }
+        break;
+      }
+      case C_I1:
+        mall = max64(cand(ws, so1, C_M, k - 1, 1, BT_I1O), cand(ws, se1, C_I1, k - 1, 1, BT_I1E));
+        break;
+      case C_I2:
+        mall = max64(cand(ws, so2, C_M, k - 1, 1, BT_I2O), cand(ws, se2, C_I2, k - 1, 1, BT_I2E));
+        break;
+      case C_D1:
+        mall = max64(cand(ws, so1, C_M, k + 1, 0, BT_D1O), cand(ws, se1, C_D1, k + 1, 0, BT_D1E));
+        break;
+      default: /* C_D2 */
+        mall = max64(cand(ws, so2, C_M, k + 1, 0, BT_D2O), cand(ws, se2, C_D2, k + 1, 0, BT_D2E));
+        break;
+    }
+    if (mall < 0) break;
+    if (mat == C_M) {
+      const int moff = (int)(mall >> 4);
+      const int nm = offset - moff;
+      for (int i = 0; i < nm; ++i) rev[n++] = 'M';
+      offset = moff;
+      v = offset - k;
+      h = offset;
+      if (v <= 0 || h <= 0) break;
+    }
+    const int type = (int)(mall & 0xF);
+    switch (type) {
+      case BT_M: s = sx; mat = C_M; break;
+      case BT_I1O: s = so1; mat = C_M; break;
+      case BT_I1E: s = se1; mat = C_I1; break;
+      case BT_I2O: s = so2; mat = C_M; break;
+      case BT_I2E: s = se2; mat = C_I2; break;
+      case BT_D1O: s = so1; mat = C_M; break;
+      case BT_D1E: s = se1; mat = C_D1; break;
+      case BT_D2O: s = so2; mat = C_M; break;
+      case BT_D2E: s = se2; mat = C_D2; break;
+      default: return -1;
+    }
+    switch (type) {
+      case BT_M: rev[n++] = 'X'; --offset; break;
+      case BT_I1O: case BT_I1E: case BT_I2O: case BT_I2E: rev[n++] = 'I'; --k; --offset; break;
+      default: rev[n++] = 'D'; ++k; break;
+    }
+    v = offset - k;
+    h = offset;
+  }
+  if (mat == C_M) {
+    if (v > 0 && h > 0) {
+      const int nm = imin(v, h);
+      for (int i = 0; i < nm; ++i) rev[n++] = 'M';
+      v -= nm;
+      h -= nm;
+    }
+    while (v > 0) { rev[n++] = 'D'; --v; }
+    while (h > 0) { rev[n++] = 'I'; --h; }
+  } else if (v != 0 || h != 0 || (s != 0 && p->match == 0)) {
+    return -1;
+  }
+  return n;
+}
+
+/* wavefront/wavefront_compute.c:108-120 */
+static int classic_score(const pen_t* p, int plen, int tlen, int s) {
+  if (p->match == 0) return -s;
+  const int swg_match = -p->match;
+  return (swg_match * (plen + tlen) - s) / 2;
+}
+
+/* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273). */
+void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
+                      int tlen, int32_t* out_score, int32_t* out_status, char* ops,
+                      int32_t* ops_len, int64_t* cells, int64_t* ext) {
+  ws_reset(ws);
+  ws_ensure_rows(ws, 0);
+  for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, 0, c), 0, sizeof(orow_t));
+  /* wavefront/wavefront_aligner.c:236-253: M[0][0] = 0 */
+  {
+    orow_t* m0 = row_at(ws, 0, C_M);
+    m0->mem = ws_alloc(ws, 1);
+    m0->exists = 1;
+    m0->base = 0;
+    m0->lo = 0;
+    m0->hi = 0;
+    m0->mem[0] = 0;
+  }
+  int s = 0;
+  int null_steps = 0;
+  int64_t ncells = 0, next = 0;
+  const int k_end = tlen - plen;
+  int status;
+  while (1) {
+    /* extend + termination (wavefront/wavefront_extend.c:86-121) */
+    orow_t* m = row_at(ws, s, C_M);
+    if (!m->exists) {
+      if (null_steps > p->scope) {
+        status = ST_END_UNREACHABLE;
+        break;
+      }
+    } else {
+      for (int k = m->lo; k <= m->hi; ++k) {
+        const int32_t off = m->mem[k - m->base];
+        if (off == WF_NULL) continue;
+        const int L = lcp(P, plen, T, tlen, off - k, off);
+        m->mem[k - m->base] = off + L;
+        next += L;
+      }
+      if (m->lo <= k_end && k_end <= m->hi && m->mem[k_end - m->base] >= tlen) {
+        status = ST_END_REACHED;
+        break;
+      }
+    }
+    ++s;
+    ncells += compute_step(ws, p, s, plen, tlen, &null_steps);
+    /* wavefront/wavefront_unialign.c:102-107 */
+    if (s >= p->max_steps) {
+      if (ext) *ext = next;
+      *out_score = -p->max_steps;
+      *out_status = ST_MAX_STEPS;
+      *ops_len = 0;
+      if (cells) *cells = ncells;
+      return;
+    }
+  }
+  if (cells) *cells = ncells;
+  if (ext) *ext = next;
+  if (status == ST_END_UNREACHABLE) {
+    *out_score = classic_score(p, 0, 0, s);
+    *out_status = 1; /* WF_STATUS_ALG_PARTIAL */
+    *ops_len = 0;
+    return;
+  }
+  /* wavefront/wavefront_unialign.c:147-237 */
+  *out_score = classic_score(p, plen, tlen, s);
+  *out_status = ST_COMPLETED;
+  if (p->score_only || ops == NULL) {
+    *ops_len = 0;
+    return;
+  }
+  char* rev = (char*)malloc((size_t)(plen + tlen + 8));
+  const int n = backtrace(ws, p, plen, tlen, s, k_end, tlen, rev);
+  if (n < 0) {
+    *out_status = ST_UNATTAINABLE;
+    *ops_len = 0;
+  } else {
+    for (int i = 0; i < n; ++i) ops[i] = rev[n - 1 - i];
+    *ops_len = n;
+  }
+  free(rev);
+}
+
+int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, const int64_t* p_off,
+                       const int32_t* p_len, const int64_t* t_off, const int32_t* t_len,
+                       int32_t* out_score, int32_t* out_status, char* out_ops,
+                       const int64_t* ops_off, int32_t* out_ops_len, int64_t* out_cells,
+                       int64_t* out_ext, int nthreads) {
+  pen_t p;
+  if (setup_penalties(cfg, &p) != 0) return -1;
+  const int ultralow = (cfg[7] == 3);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    oracle_ws_t ws;
+    memset(&ws, 0, sizeof(ws));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int i = 0; i < num_pairs; ++i) {
+      char* ops = (out_ops && !p.score_only) ? out_ops + ops_off[i] : NULL;
+      int64_t* cells = out_cells ? &out_cells[i] : NULL;
+      int64_t* ext = out_ext ? &out_ext[i] : NULL;
+      if (ultralow) {
+        oracle_bialign(&p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i], &ws,
+                       &out_score[i], &out_status[i], ops, &out_ops_len[i]);
+        if (cells) *cells = 0;
+        if (ext) *ext = 0;
+      } else {
+        oracle_align_one(&ws, &p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i],
+                  &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext);
+      }
+    }
+    ws_free(&ws);
+  }
+  return 0;
+}
+

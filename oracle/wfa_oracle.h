@@ -1,0 +1,62 @@
+/*
+ * wfa_oracle.h -- CPU restatement of WFA2-lib's exact wavefront alignment.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the GPU path is
+ * compared against (tests/, __graft_entry__.smoke(), and the cpu_baseline /
+ * --impl reference legs of bench.py).  It is never linked into, loaded by or
+ * called from the product library (wfa2-lib_gb300/).
+ *
+ * Parity is pinned: tests/test_oracle_golden.py checks this restatement against
+ * every in-scope golden file of the reference test-suite
+ * (tests/wfa.utest.check/*.alg, 305 pairs), and tests/golden/ holds outputs of
+ * the reference itself (built from its sources by oracle/Makefile) on seeded
+ * synthetic pairs.
+ */
+#ifndef WFA_ORACLE_H_
+#define WFA_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Configuration vector (plain ints, ctypes friendly).
+ *   cfg[0] distance metric   (3 = gap_affine, 4 = gap_affine_2p; wavefront/wavefront_penalties.h:42-48)
+ *   cfg[1] match  (<= 0)     cfg[2] mismatch (> 0)
+ *   cfg[3] gap_opening1      cfg[4] gap_extension1
+ *   cfg[5] gap_opening2      cfg[6] gap_extension2   (affine2p only)
+ *   cfg[7] memory mode       (0 high, 1 med, 2 low, 3 ultralow)
+ *   cfg[8] score only        (1 = compute_score, 0 = compute_alignment)
+ *   cfg[9] max alignment steps (<= 0 means unlimited)
+ */
+#define ORACLE_CFG_LEN 10
+
+/* Align num_pairs pairs with nthreads host threads (OpenMP, one aligner per
+ * thread, as tools/align_benchmark/align_benchmark.c:504-586 does).
+ *   sequences       concatenated ASCII buffer
+ *   p_off/p_len     pattern offsets/lengths into it, t_off/t_len likewise
+ *   out_score       cigar->score as the reference reports it
+ *   out_status      align_status.status (WF_STATUS_*)
+ *   out_ops         CIGAR operations ('M','X','I','D'); pair i writes at
+ *                   ops_off[i] and may use up to p_len[i]+t_len[i] bytes.
+ *                   May be NULL in score-only mode.
+ *   out_ops_len     number of operations written (0 in score-only mode)
+ *   out_cells       optional (may be NULL): WFA cells computed for the pair
+ *                   (sum over scores of hi-lo+1 of the compute loop)
+ *   out_ext         optional (may be NULL): characters matched by extend
+ *                   (sum of offset increments over all extended diagonals)
+ * Returns 0, or -1 on an invalid configuration. */
+int oracle_align_batch(
+    const int* cfg, int num_pairs,
+    const char* sequences,
+    const int64_t* p_off, const int32_t* p_len,
+    const int64_t* t_off, const int32_t* t_len,
+    int32_t* out_score, int32_t* out_status,
+    char* out_ops, const int64_t* ops_off, int32_t* out_ops_len,
+    int64_t* out_cells, int64_t* out_ext, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WFA_ORACLE_H_ */

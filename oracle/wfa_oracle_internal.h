@@ -1,0 +1,64 @@
+/*
+ * wfa_oracle_internal.h -- types shared by the CPU restatement's translation
+ * units (TEST INFRASTRUCTURE ONLY; see wfa_oracle.h).
+ */
+#ifndef WFA_ORACLE_INTERNAL_H_
+#define WFA_ORACLE_INTERNAL_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+/* wavefront/wavefront_offset.h:40-46 */
+#define WF_NULL (INT32_MIN / 2)
+
+/* wavefront/wfa.h:46-55 */
+#define ST_COMPLETED 0
+#define ST_MAX_STEPS -100
+#define ST_UNATTAINABLE -300
+#define ST_END_REACHED -2
+#define ST_END_UNREACHABLE -3
+
+enum { C_M = 0, C_I1 = 1, C_D1 = 2, C_I2 = 3, C_D2 = 4, NCOMP = 5 };
+
+typedef struct {
+  int metric; /* 3 affine, 4 affine2p */
+  int match, x, o1, e1, o2, e2;
+  int scope; /* max_score_scope */
+  int score_only;
+  int max_steps;
+} pen_t;
+
+typedef struct {
+  int exists; /* wavefront stored for this score/component */
+  int null;   /* wavefront->null after trimming */
+  int lo, hi; /* trimmed limits */
+  int base;   /* offsets[k] stored at mem[k-base] */
+  int32_t* mem;
+} orow_t;
+
+typedef struct {
+  int32_t* mem;
+  int64_t cap, used;
+} chunk_t;
+
+typedef struct {
+  /* per score, per component */
+  orow_t* rows;
+  int rows_cap; /* in scores */
+  /* chunked bump arena for offsets (chunks are never moved) */
+  chunk_t* chunks;
+  int nchunks, cur;
+} oracle_ws_t;
+
+
+/* One unidirectional end-to-end alignment (high-memory semantics). */
+void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
+                      int tlen, int32_t* out_score, int32_t* out_status, char* ops,
+                      int32_t* ops_len, int64_t* cells, int64_t* ext);
+
+/* BiWFA (ultralow memory mode). */
+void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int tlen,
+                    oracle_ws_t* ws, int32_t* out_score, int32_t* out_status, char* ops,
+                    int32_t* ops_len);
+
+#endif /* WFA_ORACLE_INTERNAL_H_ */

@@ -1,0 +1,109 @@
+"""Regenerates the golden fixtures under tests/golden/ (run where the reference
+sources are available; the fixtures themselves travel with the repo).
+
+1. ``utest.seq.gz`` -- the reference test-suite's 305 input pairs
+   (tests/wfa.utest.seq of smarco/WFA2-lib), gzipped.
+2. ``utest_expected.json`` -- for every in-scope configuration of the
+   reference test-suite (tests/wfa.utest.sh:35-64: gap-affine, gap-affine-2p
+   and penalty sets p0..p5; modes full CIGAR/high, score-only, med, BiWFA
+   score-only), the reference's own expected output per pair from
+   tests/wfa.utest.check/*.alg: the printed score and the CRC32 of the
+   printed RLE CIGAR ("-" when there is none).
+3. ``synthetic_expected.json`` -- outputs of the UNMODIFIED reference library
+   (oracle/_ref/libwfa_ref.so, built from the reference sources by
+   oracle/Makefile) on seeded synthetic pairs of each workload shape
+   (wfa2-lib_gb300/csrc/wfa_datagen.c): cigar->score and CRC32 of the
+   operations string per pair.
+
+Usage:  python tests/golden/make_golden.py [/path/to/WFA2-lib]
+"""
+import gzip
+import json
+import os
+import sys
+import zlib
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "wfa2-lib_gb300"))
+
+# name -> (metric, match, mismatch, o1, e1, o2, e2); tests/wfa.utest.sh:47-57
+PENALTY_SETS = {
+    "affine": (3, 0, 4, 6, 2, 24, 1),
+    "affine2p": (4, 0, 4, 6, 2, 24, 1),
+    "affine.p0": (3, 0, 1, 2, 1, 24, 1),
+    "affine.p1": (3, 0, 3, 1, 4, 24, 1),
+    "affine.p2": (3, 0, 5, 3, 2, 24, 1),
+    "affine.p3": (3, -5, 1, 2, 1, 24, 1),
+    "affine.p4": (3, -2, 3, 1, 4, 24, 1),
+    "affine.p5": (3, -3, 5, 3, 2, 24, 1),
+}
+# file prefix -> (memory mode, score only); tests/wfa.utest.sh:35-40
+MODES = {
+    "test": (0, False),
+    "test.score": (0, True),
+    "test.pb": (1, False),
+    "test.biwfa.score": (3, True),
+}
+# synthetic fixture sets: name -> (workload, n, penalty set, score_only, memory mode)
+SYNTHETIC = {
+    "w0_affine_full": (0, 2000, "affine", False, 0),
+    "w0_affine_score": (0, 2000, "affine", True, 0),
+    "w1_affine_full": (1, 300, "affine", False, 0),
+    "w1_affine_score": (1, 300, "affine", True, 0),
+    "w2_affine2p_full": (2, 40, "affine2p", False, 0),
+    "w5_affine_p3_full": (5, 300, "affine.p3", False, 0),
+}
+
+
+def crc(s: str) -> int:
+    return zlib.crc32(s.encode()) & 0xFFFFFFFF
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    with open(os.path.join(ref, "tests", "wfa.utest.seq"), "rb") as f:
+        raw = f.read()
+    with gzip.open(os.path.join(HERE, "utest.seq.gz"), "wb", compresslevel=9) as f:
+        f.write(raw)
+    expected = {}
+    for mode_prefix in MODES:
+        for name in PENALTY_SETS:
+            path = os.path.join(ref, "tests", "wfa.utest.check", f"{mode_prefix}.{name}.alg")
+            rows = []
+            with open(path) as f:
+                for line in f:
+                    line = line.rstrip("\n")
+                    if not line:
+                        continue
+                    score, cig = line.split("\t")
+                    rows.append([int(score), crc(cig)])
+            expected[f"{mode_prefix}.{name}"] = rows
+    with open(os.path.join(HERE, "utest_expected.json"), "w") as f:
+        json.dump({"penalty_sets": PENALTY_SETS, "modes": MODES, "expected": expected}, f,
+                  separators=(",", ":"))
+
+    from oracle import oracle as O
+    import wfa2gpu as W
+    O.build(ref=True)
+    W.build()
+    synth = {}
+    for name, (wl, n, pset, so, mm) in SYNTHETIC.items():
+        m, mi, mm_, o1, e1, o2, e2 = PENALTY_SETS[pset][0], *PENALTY_SETS[pset][1:]
+        pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
+                          gap_opening2=o2, gap_extension2=e2)
+        param, param2 = (400, 80) if wl == 5 else (0, 0)
+        p = W.generate(wl, n, param=param, param2=param2)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        r = O.align(b, pen, memory_mode=mm, score_only=so, kind="reference")
+        rows = [[int(r.score[i]), int(r.status[i]), crc(r.cigar(i))] for i in range(n)]
+        synth[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
+                       "penalties": pset, "score_only": so, "memory_mode": mm, "rows": rows}
+        print(name, "done")
+    with open(os.path.join(HERE, "synthetic_expected.json"), "w") as f:
+        json.dump(synth, f, separators=(",", ":"))
+
+
+if __name__ == "__main__":
+    main()

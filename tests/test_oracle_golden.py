@@ -1,0 +1,91 @@
+"""The CPU checker against the reference's own golden vectors (CPU only).
+
+Pins the C restatement (oracle/wfa_oracle.c) to
+  * every in-scope golden file of the reference test-suite
+    (tests/wfa.utest.check/*.alg via tests/golden/utest_expected.json), and
+  * outputs of the reference library itself on seeded synthetic pairs
+    (tests/golden/synthetic_expected.json).
+"""
+import numpy as np
+import pytest
+
+import helpers
+
+
+def _pen(O, spec):
+    m, match, x, o1, e1, o2, e2 = spec
+    return O.Penalties(metric=m, match=match, mismatch=x, gap_opening1=o1, gap_extension1=e1,
+                       gap_opening2=o2, gap_extension2=e2)
+
+
+UT = helpers.utest_expected()
+
+
+@pytest.mark.parametrize("key", sorted(UT["expected"].keys()))
+def test_oracle_matches_reference_goldens(oracle_mod, key):
+    O = oracle_mod
+    prefix, name = key.split(".", 1) if key.startswith("test.") is False else (None, None)
+    # key = "<mode prefix>.<penalty set>", mode prefixes contain dots
+    for mp in sorted(UT["modes"], key=len, reverse=True):
+        if key.startswith(mp + "."):
+            prefix, name = mp, key[len(mp) + 1:]
+            break
+    mode, score_only = UT["modes"][prefix]
+    pen = _pen(O, UT["penalty_sets"][name])
+    pats, txts = helpers.utest_pairs()
+    b = O.PairBatch.from_lists(pats, txts)
+    r = O.align(b, pen, memory_mode=mode, score_only=score_only)
+    exp = UT["expected"][key]
+    assert len(exp) == b.n
+    bad = []
+    for i in range(b.n):
+        if score_only:
+            got = [int(r.score[i]), helpers.crc("-")]
+        else:
+            ops = r.cigar(i)
+            got = [O.rescore(ops, pen), helpers.crc(helpers.rle(ops))]
+            assert O.check_cigar(ops, b.pattern(i), b.text(i))
+        if got != exp[i]:
+            bad.append(i)
+    assert not bad, f"{key}: {len(bad)} pairs differ, first {bad[:5]}"
+
+
+SY = helpers.synthetic_expected()
+
+
+@pytest.mark.parametrize("name", sorted(SY.keys()))
+def test_oracle_matches_reference_on_synthetic(oracle_mod, wfa, name):
+    O, W = oracle_mod, wfa
+    fx = SY[name]
+    pen = _pen(O, UT["penalty_sets"][fx["penalties"]])
+    p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    r = O.align(b, pen, memory_mode=fx["memory_mode"], score_only=fx["score_only"])
+    for i, (score, status, c) in enumerate(fx["rows"]):
+        assert int(r.score[i]) == score and int(r.status[i]) == status, (name, i)
+        assert helpers.crc(r.cigar(i)) == c, (name, i)
+
+
+def test_oracle_rescoring_and_replay(oracle_mod, wfa):
+    """Every CIGAR replays against its pair and rescoring gives cigar->score."""
+    O, W = oracle_mod, wfa
+    p = W.generate(1, 200)
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    pen = O.Penalties()
+    r = O.align(b, pen)
+    for i in range(b.n):
+        ops = r.cigar(i)
+        assert O.check_cigar(ops, b.pattern(i), b.text(i))
+        assert O.rescore(ops, pen) == int(r.score[i])
+
+
+def test_oracle_edge_cases(oracle_mod):
+    O = oracle_mod
+    pats = [b"", b"A", b"", b"ACGT", b"ACGT" * 10, b"AAAA"]
+    txts = [b"", b"", b"ACG", b"ACGT", b"ACGT" * 10, b"TTTT"]
+    b = O.PairBatch.from_lists(pats, txts)
+    r = O.align(b, O.Penalties())
+    assert list(r.score) == [0, -8, -12, 0, 0, -16]
+    assert [r.cigar(i) for i in range(b.n)] == ["", "D", "III", "MMMM", "M" * 40, "XXXX"]
+    rs = O.align(b, O.Penalties(), max_steps=5)
+    assert int(rs.status[5]) == -100 and int(rs.score[5]) == -5

@@ -1,0 +1,47 @@
+/*
+ * wfa_engine.h -- internal C interface between the host C layer
+ * (wfa_aligner.c) and the CUDA engine (wfa_engine.cu).  Not installed.
+ */
+#ifndef WFA2GPU_ENGINE_H_
+#define WFA2GPU_ENGINE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Alignment configuration after the reference's penalty set-up
+ * (wavefront/wavefront_penalties.c:95-173): x/o/e are the internal
+ * (possibly Eizenga-transformed) penalties, match the user's match (<=0). */
+typedef struct {
+  int metric; /* 3 gap_affine, 4 gap_affine_2p */
+  int match;
+  int x, o1, e1, o2, e2;
+  int score_only;
+  int max_steps; /* INT32_MAX when unlimited */
+} wf2g_cfg_t;
+
+/* Creates an engine on the current CUDA device; NULL (and *err set to a
+ * WF2G_ERR_* code) if no usable GPU is present. */
+void* wf2g_engine_new(int* err);
+void wf2g_engine_free(void* engine);
+
+/* Aligns a batch.  on_device=0: every pointer is host memory, the call copies
+ * in, computes and copies out, and returns when the results are in place.
+ * on_device=1: every pointer is device memory, work is queued on `stream`
+ * (NULL: the engine's own stream) and the call returns without waiting.
+ * max_len bounds the pattern and text lengths (computed when on_device=0). */
+int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int num_pairs, int on_device,
+                      const char* seqs, const int64_t* p_off, const int32_t* p_len,
+                      const int64_t* t_off, const int32_t* t_len, int max_len,
+                      int32_t* scores, int32_t* status, char* ops, const int64_t* ops_off,
+                      int32_t* ops_len, void* stream);
+
+int64_t wf2g_engine_launches(const void* engine);
+int wf2g_engine_device(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WFA2GPU_ENGINE_H_ */
