@@ -231,7 +231,9 @@ def main():
 
     cfg = W.Config(score_only=args.score_only)
     al = W.Aligner(cfg)
-    stream = torch.cuda.current_stream(dev)
+    # a non-default stream: the C ABI maps a NULL stream to the aligner's own
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
 
     def step_device():
         rc = al.align_batch_device(

@@ -3,14 +3,16 @@
 //
 // A batch runs in two passes, both persistent kernels that pull pairs from a
 // device work queue (no host round trip between them):
-//   pass 1  2-bit packed sequences, wavefront ring in shared memory, ring
-//           width sized for the common case; pairs whose wavefront outgrows
-//           the ring, whose back-trace outgrows the warp's choice-byte slice,
-//           or that hold non-ACGT bytes are appended to a retry list;
-//   pass 2  8-bit sequences, ring in a private global-memory slice wide enough
-//           for any wavefront of the batch (plen+tlen+3 diagonals); runs only
-//           over the retry list and reports a remaining overflow as
-//           WF_STATUS_OOM.
+//   pass 1  every pair: 2-bit packed sequences, 1 MB of back-trace bytes per
+//           warp; pairs with non-ACGT bytes or a longer back-trace go to a
+//           retry list;
+//   pass 2  the retry list only: 8-bit sequences and a back-trace slice sized
+//           for any alignment of the batch; a remaining overflow is reported
+//           as WF_STATUS_OOM.
+// Each warp owns a global-memory slice holding its wavefront ring (every
+// diagonal the pair can reach, so rows never wrap) and back-trace bytes; the
+// slices stay L1/L2 resident.  On GB300 this measured 2x faster than a ring in
+// shared memory, whose footprint capped residency at a few warps per SM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -34,6 +36,7 @@
 
 namespace wf2g {
 extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes);
+extern "C" int wf2g_seq_bytes(int enc, int max_len);
 }
 
 namespace {
@@ -74,28 +77,12 @@ struct Engine {
   DevBuf scratch1, scratch2;
 };
 
-constexpr int kWarpsPerCta2 = 2;
-constexpr int64_t kBits1PerWarp = int64_t(2) << 20;     // pass-1 choice bytes per warp
-constexpr int64_t kScratch2Budget = int64_t(24) << 30;  // pass-2 global scratch budget
 
 int env_int(const char* name, int dflt) {
   const char* v = getenv(name);
   return (v && *v) ? atoi(v) : dflt;
 }
 
-int next_pow2(int v) {
-  int p = 1;
-  while (p < v) p <<= 1;
-  return p;
-}
-
-struct PassPlan {
-  KParams kp;
-  int warps_per_cta;
-  int blocks;
-  size_t smem;
-  void* fn;
-};
 
 Penalties make_pen(const wf2g_cfg_t& c) {
   Penalties p;
@@ -114,8 +101,6 @@ Penalties make_pen(const wf2g_cfg_t& c) {
   return p;
 }
 
-int num_rows(const Penalties& p, bool a2p) { return a2p ? p.R + 2 * p.RI1 + 2 * p.RI2 : p.R + 2 * p.RI1; }
-
 // Upper bound of the alignment score, as the reference sizes its wavefront
 // table (wavefront/wavefront_components.c:101-108), for lengths <= max_len.
 int score_bound(const wf2g_cfg_t& c, int max_len) {
@@ -123,19 +108,6 @@ int score_bound(const wf2g_cfg_t& c, int max_len) {
   if (c.metric == 4) b = std::max<int64_t>(b, (int64_t)c.x * max_len + c.o2 + (int64_t)c.e2 * max_len);
   b += 8;
   return (int)std::min<int64_t>(b, INT32_MAX / 4);
-}
-
-int launch(Engine* E, const PassPlan& pl, cudaStream_t st) {
-  if (pl.blocks <= 0) return 0;
-  void* args[] = {(void*)&pl.kp};
-  cudaError_t e = cudaLaunchKernel(pl.fn, dim3(pl.blocks), dim3(32 * pl.warps_per_cta), args,
-                                   pl.smem, st);
-  if (e != cudaSuccess) {
-    fprintf(stderr, "[wfa2gpu] kernel launch failed: %s\n", cudaGetErrorString(e));
-    return WF2G_ERR_CUDA_;
-  }
-  E->launches++;
-  return 0;
 }
 
 }  // namespace
@@ -201,17 +173,72 @@ extern "C" int64_t wf2g_engine_launches(const void* engine) {
   return engine ? ((const Engine*)engine)->launches : 0;
 }
 
+// One persistent launch over a work list.
+struct Pass {
+  int enc;          // 2 or 8 bits per staged base
+  int final_pass;   // 1: overflow -> WF_STATUS_OOM
+  int64_t bits_cap; // back-trace bytes per warp (full CIGAR)
+  int max_blocks_per_sm;
+};
+
+static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const Pass& ps,
+                    int n_upper, DevBuf& scratch, cudaStream_t st) {
+  const bool a2p = (cfg.metric == 4);
+  const bool cigar = !cfg.score_only;
+  const int off_bytes = (base.max_len < 32000) ? 2 : 4;
+  const Penalties& pen = base.pen;
+  const int nrows = a2p ? pen.R + 2 * pen.RI1 + 2 * pen.RI2 : pen.R + 2 * pen.RI1;
+  KParams kp = base;
+  kp.final_pass = ps.final_pass;
+  kp.kofs = base.max_len + 2;
+  kp.row_stride = ((2 * base.max_len + 6) + 63) & ~63;
+  kp.ring_bytes = (((int64_t)(nrows + 1) * kp.row_stride * off_bytes) + 255) & ~int64_t(255);
+  const int64_t seq_bytes = wf2g_seq_bytes(ps.enc, base.max_len);
+  kp.seq_in_smem = seq_bytes <= 48 * 1024;
+  kp.seq_bytes = kp.seq_in_smem ? 0 : ((seq_bytes + 255) & ~int64_t(255));
+  kp.smem_per_warp = (int)((((kp.seq_in_smem ? seq_bytes : 0) + (int64_t)nrows * 8) + 15) & ~int64_t(15));
+  kp.bits_cap = cigar ? ps.bits_cap : 0;
+  const int64_t table_bytes = cigar ? (int64_t)kp.table_cap * 8 : 0;
+  kp.gscratch_per_warp = (kp.ring_bytes + kp.seq_bytes + table_bytes + kp.bits_cap + 255) & ~int64_t(255);
+
+  int wpc = (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_warp, 1));
+  wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
+  const size_t smem = (size_t)kp.smem_per_warp * wpc;
+  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes);
+  // shared memory holds only the staged sequences and row limits; give the
+  // rest of the SM's unified storage to L1, which caches the wavefront rows
+  const int want_blocks = std::max(1, 64 / wpc);
+  int carve = (int)((smem * want_blocks * 100 + 228 * 1024 - 1) / (228 * 1024)) + 1;
+  carve = std::max(1, std::min(carve, 100));
+  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+  int bps = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32 * wpc, smem);
+  bps = std::max(1, std::min(bps, ps.max_blocks_per_sm));
+  const int need = (n_upper + wpc - 1) / wpc;
+  int blocks = std::min(bps * E->num_sms, std::max(need, 1));
+  // bound the scratch slices by the budget
+  const int64_t budget = (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
+  if ((int64_t)blocks * wpc * kp.gscratch_per_warp > budget)
+    blocks = std::max(1, (int)(budget / (wpc * kp.gscratch_per_warp)));
+  if (ensure(scratch, (size_t)blocks * wpc * kp.gscratch_per_warp)) return WF2G_ERR_OOM_;
+  kp.gscratch = (uint8_t*)scratch.p;
+  void* args[] = {(void*)&kp};
+  cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args, smem, st);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "[wfa2gpu] kernel launch failed: %s\n", cudaGetErrorString(e));
+    return WF2G_ERR_CUDA_;
+  }
+  E->launches++;
+  return 0;
+}
+
 static int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                         const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                         const int32_t* d_tlen, int max_len, int32_t* d_scores,
                         int32_t* d_status, char* d_ops, const int64_t* d_opsoff,
                         int32_t* d_opslen, cudaStream_t st) {
-  const bool a2p = (cfg.metric == 4);
   const bool cigar = !cfg.score_only;
-  const Penalties pen = make_pen(cfg);
-  const int nrows = num_rows(pen, a2p);
   if (max_len < 1) max_len = 1;
-
   if (ensure(E->counters, 4 * sizeof(int32_t)) || ensure(E->retry, (size_t)n * sizeof(int32_t)))
     return WF2G_ERR_OOM_;
   int32_t* counters = (int32_t*)E->counters.p;
@@ -219,7 +246,7 @@ static int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_s
 
   KParams base;
   memset(&base, 0, sizeof(base));
-  base.pen = pen;
+  base.pen = make_pen(cfg);
   base.max_steps = cfg.max_steps;
   base.seqs = (const uint8_t*)d_seqs;
   base.p_off = d_poff;
@@ -234,123 +261,28 @@ static int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_s
   base.ops_off = d_opsoff;
   base.ops_len = d_opslen;
   base.max_len = max_len;
-  const int table_cap = score_bound(cfg, max_len) + 1;
+  base.table_cap = score_bound(cfg, max_len) + 1;
 
-  // ------------------------------------------------ pass 1 (2-bit sequences)
-  // Tuning knobs (environment): WF2G_RING1=0 puts the pass-1 ring in global
-  // memory, WF2G_WCAP1 sets its width, WF2G_WPC1 the warps per CTA.
-  const int off_bytes = (max_len < 32000) ? 2 : 4;
-  PassPlan p1;
-  p1.kp = base;
-  p1.kp.items = nullptr;
-  p1.kp.n_items = n;
-  p1.kp.num_items_dev = nullptr;
-  p1.kp.queue = counters + 0;
-  p1.kp.final_pass = 0;
-  p1.kp.ring_in_smem = env_int("WF2G_RING1", 1);
-  p1.kp.wcap = next_pow2(std::min(env_int("WF2G_WCAP1", 1024), next_pow2(2 * max_len + 3)));
-  p1.kp.seq_in_smem = 1;
-  {
-    const int nwords = ((max_len + 31) >> 5) + 2;
-    size_t b = (size_t)2 * nwords * 8 + (size_t)nrows * 8;
-    b = (b + 15) & ~size_t(15);
-    if (p1.kp.ring_in_smem) b += (size_t)nrows * p1.kp.wcap * off_bytes;
-    b = (b + 15) & ~size_t(15);
-    p1.kp.smem_per_warp = (int)b;
-  }
-  {
-    int wpc = (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(p1.kp.smem_per_warp, 1));
-    wpc = env_int("WF2G_WPC1", wpc);
-    p1.warps_per_cta = std::max(1, std::min(wpc, 8));
-  }
-  p1.smem = (size_t)p1.kp.smem_per_warp * p1.warps_per_cta;
-  p1.fn = wf2g_kernel_ptr(a2p, cigar, 2, off_bytes);
-  bool pass1 = p1.smem <= E->smem_optin && env_int("WF2G_PASS1", 1);
-  if (pass1) {
-    int bps = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, p1.fn, 32 * p1.warps_per_cta, p1.smem);
-    if (bps <= 0) pass1 = false;
-    const int need = (n + p1.warps_per_cta - 1) / p1.warps_per_cta;
-    p1.blocks = std::min(std::max(bps, 1) * E->num_sms, need);
-  }
-  if (pass1) {
-    const int64_t warps = (int64_t)p1.blocks * p1.warps_per_cta;
-    p1.kp.ring_bytes_global =
-        p1.kp.ring_in_smem ? 0 : (((int64_t)nrows * p1.kp.wcap * off_bytes + 255) & ~int64_t(255));
-    p1.kp.table_cap = table_cap;
-    p1.kp.bits_cap = cigar ? kBits1PerWarp : 0;
-    p1.kp.gscratch_per_warp =
-        (p1.kp.ring_bytes_global + (cigar ? (int64_t)table_cap * 8 + kBits1PerWarp : 0) + 255) &
-        ~int64_t(255);
-    if (p1.kp.gscratch_per_warp > 0) {
-      if (ensure(E->scratch1, (size_t)(warps * p1.kp.gscratch_per_warp))) return WF2G_ERR_OOM_;
-      p1.kp.gscratch = (uint8_t*)E->scratch1.p;
-    }
-    int rc = launch(E, p1, st);
-    if (rc) return rc;
-  }
-
-  // ------------------------------------------------ pass 2 (global ring, 8-bit)
-  PassPlan p2;
-  p2.kp = base;
-  if (pass1) {
-    p2.kp.items = (const int32_t*)E->retry.p;
-    p2.kp.num_items_dev = counters + 2;
-    p2.kp.n_items = 0;
-  } else {
-    p2.kp.items = nullptr;
-    p2.kp.num_items_dev = nullptr;
-    p2.kp.n_items = n;
-  }
-  p2.kp.queue = counters + 1;
-  p2.kp.final_pass = 1;
-  p2.kp.wcap = next_pow2(2 * max_len + 3);
-  const int off2 = off_bytes;
-  p2.kp.ring_in_smem = 0;
-  const int nwords8 = ((max_len + 7) >> 3) + 2;
-  const int64_t seq_bytes = (int64_t)2 * nwords8 * 8;
-  p2.kp.seq_in_smem = seq_bytes <= 64 * 1024;
-  {
-    size_t b = (p2.kp.seq_in_smem ? (size_t)seq_bytes : 0) + (size_t)nrows * 8;
-    b = (b + 15) & ~size_t(15);
-    p2.kp.smem_per_warp = (int)b;
-  }
-  p2.warps_per_cta = kWarpsPerCta2;
-  p2.smem = (size_t)p2.kp.smem_per_warp * p2.warps_per_cta;
-  p2.fn = wf2g_kernel_ptr(a2p, cigar, 8, off2);
-  if (p2.smem > E->smem_optin) return WF2G_ERR_ARGS_;
-  {
-    int bps = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, p2.fn, 32 * p2.warps_per_cta, p2.smem);
-    bps = std::max(1, std::min(bps, 2));
-    const int need = (n + p2.warps_per_cta - 1) / p2.warps_per_cta;
-    p2.blocks = std::min(bps * E->num_sms, need);
-  }
-  {
-    int64_t warps = (int64_t)p2.blocks * p2.warps_per_cta;
-    p2.kp.ring_bytes_global = ((int64_t)nrows * p2.kp.wcap * off2 + 255) & ~int64_t(255);
-    p2.kp.seq_bytes_global = p2.kp.seq_in_smem ? 0 : ((seq_bytes + 255) & ~int64_t(255));
-    p2.kp.table_cap = table_cap;
-    int64_t fixed = p2.kp.ring_bytes_global + p2.kp.seq_bytes_global + (int64_t)table_cap * 8;
-    int64_t bits = 0;
-    if (cigar) {
-      // every cell of every score fits: (scores) x (plen+tlen+1) diagonals
-      const int64_t want = (int64_t)table_cap * (2 * (int64_t)max_len + 1) + 4 * (int64_t)max_len + 64;
-      int64_t per_warp_budget = kScratch2Budget / std::max<int64_t>(warps, 1) - fixed;
-      if (per_warp_budget < want && warps > E->num_sms) {
-        // fewer, larger warps rather than starving each slice
-        p2.blocks = std::max(1, E->num_sms / p2.warps_per_cta);
-        warps = (int64_t)p2.blocks * p2.warps_per_cta;
-        per_warp_budget = kScratch2Budget / warps - fixed;
-      }
-      bits = std::max<int64_t>(std::min(want, per_warp_budget), int64_t(1) << 20);
-    }
-    p2.kp.bits_cap = bits;
-    p2.kp.gscratch_per_warp = (fixed + bits + 255) & ~int64_t(255);
-    if (ensure(E->scratch2, (size_t)(warps * p2.kp.gscratch_per_warp))) return WF2G_ERR_OOM_;
-    p2.kp.gscratch = (uint8_t*)E->scratch2.p;
-  }
-  return launch(E, p2, st);
+  // pass 1: every pair, 2-bit sequences, 1 MB of back-trace bytes per warp
+  KParams k1 = base;
+  k1.items = nullptr;
+  k1.num_items_dev = nullptr;
+  k1.n_items = n;
+  k1.queue = counters + 0;
+  Pass p1{2, 0, int64_t(1) << 20, 8};
+  int rc = run_pass(E, cfg, k1, p1, n, E->scratch1, st);
+  if (rc) return rc;
+  // pass 2: the retry list (non-ACGT bytes, back-trace overflow), 8-bit
+  // sequences and a back-trace slice sized for any alignment of the batch
+  KParams k2 = base;
+  k2.items = (const int32_t*)E->retry.p;
+  k2.num_items_dev = counters + 2;
+  k2.n_items = 0;
+  k2.queue = counters + 1;
+  int64_t bits2 = 0;
+  if (cigar) bits2 = (int64_t)base.table_cap * (2 * (int64_t)max_len + 1) + 4 * (int64_t)max_len + 64;
+  Pass p2{8, 1, bits2, 2};
+  return run_pass(E, cfg, k2, p2, std::min(n, 2 * E->num_sms * 8), E->scratch2, st);
 }
 
 extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int on_device,

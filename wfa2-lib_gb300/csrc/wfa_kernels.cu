@@ -13,10 +13,10 @@
 //             (offset<<4|type) maximum does: mismatch > D2 > D1 > I2 > I1,
 //             extension > opening (wavefront/wavefront_backtrace.c:49-59).
 //
-// GPU design: one warp per pair, lanes striped over diagonals k; wavefront
-// rows live in a (k mod WCAP) ring; a row is NULL outside its trimmed range
-// (the reference's NULL padding, wavefront/wavefront_compute.c:498-575), so
-// reads need no bounds checks.  Offsets are int32 with any negative == NULL.
+// GPU design: one warp per pair, lanes striped over diagonals k.  Every
+// wavefront row is NULL outside its trimmed range (the reference's NULL
+// padding, wavefront/wavefront_compute.c:498-575), so the cell loop reads its
+// inputs without bounds checks; empty inputs read an all-NULL row.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -25,83 +25,119 @@
 
 namespace wf2g {
 
-// NULL as stored in a ring of OffT (int16 rings serve sequences < 32000).
+// NULL as stored in a row of OffT (int16 rows serve sequences < 32000).
 template <typename OffT>
 __device__ __forceinline__ OffT null_of() {
   return sizeof(OffT) == 2 ? (OffT)(-32768) : (OffT)kNull;
 }
-// Stores an offset; every negative value is NULL.
-template <typename OffT>
-__device__ __forceinline__ void put(OffT* row, int idx, int32_t v) {
-  row[idx] = v < 0 ? null_of<OffT>() : (OffT)v;
-}
 
-__device__ __forceinline__ int ring_mod_back(int cur, int d, int R) {
-  // slot of score (s-d) when slot of s is cur, 0 <= d < R
+// ---------------------------------------------------------------- checking
+// Built with -DWF2G_CHECKED every ring, sequence, back-trace and output access
+// is bounds-checked: a violation is recorded (first one wins) and the access
+// is skipped, so a faulty index is reported instead of faulting the GPU.
+#ifdef WF2G_CHECKED
+__device__ unsigned long long g_fault[4];  // site, index, pair, count
+__device__ __forceinline__ bool wf2g_ok(bool ok, int site, long long idx, int pair) {
+  if (!ok) {
+    if (atomicCAS(&g_fault[0], 0ull, (unsigned long long)site) == 0ull) {
+      g_fault[1] = (unsigned long long)idx;
+      g_fault[2] = (unsigned long long)pair;
+    }
+    atomicAdd(&g_fault[3], 1ull);
+  }
+  return ok;
+}
+#define CHK(cond, site, idx) wf2g_ok((cond), (site), (long long)(idx), g_pair)
+#else
+#define CHK(cond, site, idx) true
+#endif
+
+__device__ __forceinline__ int ring_back(int cur, int d, int R) {
+  // slot of score (s-d) when the slot of s is cur, 0 <= d < R
   const int t = cur - d;
   return t < 0 ? t + R : t;
 }
 
 // ---------------------------------------------------------------- sequences
-// 2-bit: base i of a sequence at bits [63-2(i%32), 62-2(i%32)] of word i/32.
-__device__ __forceinline__ uint64_t window2(const uint64_t* W, int pos) {
-  const int w = pos >> 5;
-  const int sh = (pos & 31) << 1;
-  uint64_t x = W[w];
-  if (sh) x = (x << sh) | (W[w + 1] >> (64 - sh));
-  return x;
-}
-// 8-bit: byte i at bits [63-8(i%8), 56-8(i%8)] of word i/8.
-__device__ __forceinline__ uint64_t window8(const uint64_t* W, int pos) {
-  const int w = pos >> 3;
-  const int sh = (pos & 7) << 3;
-  uint64_t x = W[w];
-  if (sh) x = (x << sh) | (W[w + 1] >> (64 - sh));
-  return x;
-}
+// ENC==2: base i at bits [31-2(i%16), 30-2(i%16)] of 32-bit word i/16.
+// ENC==8: byte i at bits [63-8(i%8), 56-8(i%8)] of 64-bit word i/8.
+template <int ENC>
+struct Seq;
+
+template <>
+struct Seq<2> {
+  typedef uint32_t Word;
+  static constexpr int kPer = 16;
+  static __device__ __forceinline__ uint32_t window(const uint32_t* W, int pos) {
+    const int w = pos >> 4;
+    return __funnelshift_l(W[w + 1], W[w], (pos & 15) << 1);
+  }
+  static __device__ __forceinline__ int equal_prefix(uint32_t d) { return __clz(d) >> 1; }
+  static __host__ __device__ int words(int len) { return ((len + 15) >> 4) + 2; }
+};
+
+template <>
+struct Seq<8> {
+  typedef uint64_t Word;
+  static constexpr int kPer = 8;
+  static __device__ __forceinline__ uint64_t window(const uint64_t* W, int pos) {
+    const int w = pos >> 3;
+    const int sh = (pos & 7) << 3;
+    uint64_t x = W[w];
+    if (sh) x = (x << sh) | (W[w + 1] >> (64 - sh));
+    return x;
+  }
+  static __device__ __forceinline__ int equal_prefix(uint64_t d) { return __clzll(d) >> 3; }
+  static __host__ __device__ int words(int len) { return ((len + 7) >> 3) + 2; }
+};
 
 // Longest common prefix of P[v..] and T[h..], at most lim characters:
-// 64-bit XOR + count-leading-zeros per block (wavefront/wavefront_extend_kernels.c:68-92).
+// word-wide XOR + count-leading-zeros (wavefront/wavefront_extend_kernels.c:68-92).
 template <int ENC>
-__device__ __forceinline__ int lcp(const uint64_t* P, const uint64_t* T, int v, int h, int lim) {
-  constexpr int kPer = (ENC == 2) ? 32 : 8;
-  constexpr int kShift = (ENC == 2) ? 1 : 3;
+__device__ __forceinline__ int lcp(const typename Seq<ENC>::Word* P,
+                                   const typename Seq<ENC>::Word* T, int v, int h, int lim,
+                                   int nw = 0, int g_pair = 0) {
   int L = 0;
   while (L < lim) {
-    const uint64_t a = (ENC == 2) ? window2(P, v + L) : window8(P, v + L);
-    const uint64_t b = (ENC == 2) ? window2(T, h + L) : window8(T, h + L);
-    const uint64_t d = a ^ b;
+    const int wp = (v + L) / Seq<ENC>::kPer, wt = (h + L) / Seq<ENC>::kPer;
+    if (!CHK(v + L >= 0 && wp + 1 < nw, 20, v + L) || !CHK(h + L >= 0 && wt + 1 < nw, 21, h + L))
+      return 0;
+    const auto d = Seq<ENC>::window(P, v + L) ^ Seq<ENC>::window(T, h + L);
     if (d) {
-      L += __clzll(d) >> kShift;
+      L += Seq<ENC>::equal_prefix(d);
       break;
     }
-    L += kPer;
+    L += Seq<ENC>::kPer;
   }
   return L < lim ? L : lim;
 }
 
-// Stages one sequence into W (warp-cooperative).  Returns false if ENC==2 and
-// the sequence holds a byte outside {A,C,G,T}.
+// Stages one sequence into W (warp-cooperative).  Returns false if ENC==2
+// and the sequence holds a byte outside {A,C,G,T}.
 template <int ENC>
-__device__ bool stage_sequence(const uint8_t* __restrict__ src, int len, uint64_t* W, int nwords,
-                               int lane) {
+__device__ bool stage_sequence(const uint8_t* __restrict__ src, int len,
+                               typename Seq<ENC>::Word* W, int lane) {
+  const int nwords = Seq<ENC>::words(len);
   bool ok = true;
   if (ENC == 2) {
-    const int nblk = (len + 31) >> 5;
+    const int nblk = (len + 31) >> 5;  // 32 bases -> 2 words
     for (int b = 0; b < nblk; ++b) {
       const int i = (b << 5) + lane;
       uint32_t code = 0;
       if (i < len) {
         const uint8_t c = src[i];
-        const bool valid = (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
-        ok &= valid;
-        code = (c >> 1) & 3u;  // A0 C1 T2 G3 -- a bijection on ACGT
+        ok &= (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
+        code = (c >> 1) & 3u;  // A0 C1 T2 G3: a bijection on ACGT
       }
-      const uint32_t hi = __reduce_or_sync(kFull, lane < 16 ? code << (30 - 2 * lane) : 0u);
-      const uint32_t lo = __reduce_or_sync(kFull, lane >= 16 ? code << (30 - 2 * (lane - 16)) : 0u);
-      if (lane == 0) W[b] = ((uint64_t)hi << 32) | lo;
+      const int sh = 30 - 2 * (lane & 15);
+      const uint32_t w0 = __reduce_or_sync(kFull, lane < 16 ? code << sh : 0u);
+      const uint32_t w1 = __reduce_or_sync(kFull, lane >= 16 ? code << sh : 0u);
+      if (lane == 0) {
+        W[2 * b] = w0;
+        if (2 * b + 1 < nwords) W[2 * b + 1] = w1;
+      }
     }
-    for (int b = nblk + lane; b < nwords; b += 32) W[b] = 0;
+    for (int b = 2 * nblk + lane; b < nwords; b += 32) W[b] = 0;
     ok = __all_sync(kFull, ok);
   } else {
     uint8_t* B = reinterpret_cast<uint8_t*>(W);
@@ -115,74 +151,100 @@ __device__ bool stage_sequence(const uint8_t* __restrict__ src, int len, uint64_
   return ok;
 }
 
-// ------------------------------------------------------------------ kernel
-template <typename OffT>
-struct WarpMem {
-  uint64_t* P;
-  uint64_t* T;
-  int2* meta;    // [nrows] trimmed (lo,hi) of each ring row; lo>hi == empty
-  OffT* ring;    // [nrows][wcap]
-  int2* table;   // [table_cap] back-trace row table (choice-byte base, lo)
-  uint8_t* bits; // [bits_cap] back-trace choice bytes
+// Ring bounds of the calling warp (checked builds only).
+struct RingBounds {
+  const void* lo;
+  const void* hi;
 };
 
-template <bool A2P>
-__device__ __forceinline__ int num_rows(const Penalties& pen) {
-  return A2P ? pen.R + 2 * pen.RI1 + 2 * pen.RI2 : pen.R + 2 * pen.RI1;
+// NULL-fill row elements of diagonals [a,b].
+template <typename OffT>
+__device__ __forceinline__ void null_range(OffT* row, int a, int b, int lane,
+                                           RingBounds rb = RingBounds{nullptr, nullptr},
+                                           int g_pair = 0) {
+  if (a > b) return;  // also keeps a + lane from overflowing on empty ranges
+  for (int k = a + lane; k <= b; k += 32) {
+    if (CHK(rb.lo == nullptr || ((const void*)(row + k) >= rb.lo && (const void*)(row + k) < rb.hi), 1, k))
+      row[k] = null_of<OffT>();
+  }
 }
 
-// NULL-fill a row over [a,b] (positions mod wcap).
+// After computing [lo,hi] and finding the trimmed range [tlo,thi]: NULL the
+// trimmed-away ends (wavefront/wavefront_compute.c:579-613).
 template <typename OffT>
-__device__ __forceinline__ void null_range(OffT* row, int a, int b, int mask, int lane) {
-  for (int k = a + lane; k <= b; k += 32) row[k & mask] = null_of<OffT>();
+__device__ __forceinline__ void trim_fill(OffT* row, int lo, int hi, int tlo, int thi, int lane,
+                                          RingBounds rb, int g_pair) {
+  if (tlo > thi) {
+    null_range(row, lo, hi, lane, rb, g_pair);
+  } else {
+    null_range(row, lo, tlo - 1, lane, rb, g_pair);
+    null_range(row, thi + 1, hi, lane, rb, g_pair);
+  }
+}
+
+// Clears what a reused slot holds outside the new range [lo,hi].
+template <typename OffT>
+__device__ __forceinline__ void clear_outside(OffT* row, int2 old, int lo, int hi, int lane,
+                                              RingBounds rb, int g_pair) {
+  if (old.x <= old.y) {
+    null_range(row, old.x, min(old.y, lo - 1), lane, rb, g_pair);
+    null_range(row, max(old.x, hi + 1), old.y, lane, rb, g_pair);
+  }
+}
+
+__device__ __forceinline__ bool in_bounds(int32_t off, int k, int plen, int tlen) {
+  return (uint32_t)off <= (uint32_t)tlen && (uint32_t)(off - k) <= (uint32_t)plen;
 }
 
 template <bool A2P, bool CIGAR, int ENC, typename OffT>
 __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
+  typedef typename Seq<ENC>::Word Word;
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int wpc = blockDim.x >> 5;
   const int64_t gwarp = (int64_t)blockIdx.x * wpc + warp;
   const Penalties pen = p.pen;
-  const int nrows = num_rows<A2P>(pen);
-  const int wcap = p.wcap;
-  const int mask = wcap - 1;
-  const int nwords = (ENC == 2) ? ((p.max_len + 31) >> 5) + 2 : ((p.max_len + 7) >> 3) + 2;
+  const int nrows = A2P ? pen.R + 2 * pen.RI1 + 2 * pen.RI2 : pen.R + 2 * pen.RI1;
+  const int stride = p.row_stride;
+  const int kofs = p.kofs;
+  const int nwords = Seq<ENC>::words(p.max_len);
 
   // ---- carve per-warp memory
-  WarpMem<OffT> m;
-  {
-    // shared memory of this warp: [P,T if staged here][meta][ring if here]
-    uint8_t* ws = smem + (size_t)warp * p.smem_per_warp;
-    uint8_t* gs = p.gscratch ? p.gscratch + gwarp * p.gscratch_per_warp : nullptr;
-    if (p.seq_in_smem) {
-      m.P = reinterpret_cast<uint64_t*>(ws);
-      ws += (size_t)2 * nwords * sizeof(uint64_t);
-    } else {
-      m.P = reinterpret_cast<uint64_t*>(gs + (p.ring_in_smem ? 0 : p.ring_bytes_global));
-    }
-    m.T = m.P + nwords;
-    m.meta = reinterpret_cast<int2*>(ws);
-    ws += (size_t)nrows * sizeof(int2);
-    if (p.ring_in_smem) {
-      m.ring = reinterpret_cast<OffT*>((reinterpret_cast<uintptr_t>(ws) + 15) & ~uintptr_t(15));
-    } else {
-      m.ring = reinterpret_cast<OffT*>(gs);
-      gs += p.ring_bytes_global;
-    }
-    if (!p.seq_in_smem) gs += p.seq_bytes_global;
-    if (CIGAR) {
-      m.table = reinterpret_cast<int2*>(gs);
-      m.bits = reinterpret_cast<uint8_t*>(m.table + p.table_cap);
-    } else {
-      m.table = nullptr;
-      m.bits = nullptr;
-    }
+  uint8_t* ws = smem + (size_t)warp * p.smem_per_warp;
+  uint8_t* gs = p.gscratch + gwarp * p.gscratch_per_warp;
+  OffT* const ring = reinterpret_cast<OffT*>(gs);  // (nrows+1) rows; row nrows is all-NULL
+  gs += p.ring_bytes;
+  Word* P;
+  if (p.seq_in_smem) {
+    P = reinterpret_cast<Word*>(ws);
+    ws += (size_t)2 * nwords * sizeof(Word);
+  } else {
+    P = reinterpret_cast<Word*>(gs);
+    gs += p.seq_bytes;
   }
+  Word* const T = P + nwords;
+  int2* const meta = reinterpret_cast<int2*>(ws);  // [nrows] trimmed (lo,hi); lo>hi == empty
+  int2* const table = CIGAR ? reinterpret_cast<int2*>(gs) : nullptr;
+  uint8_t* const bits = CIGAR ? reinterpret_cast<uint8_t*>(table + p.table_cap) : nullptr;
+  auto row = [=](int r) -> OffT* { return ring + (size_t)r * stride + kofs; };
+  const OffT* const null_row = row(nrows);
+  const RingBounds rb{ring, ring + (size_t)(nrows + 1) * stride};
+  int g_pair = -1;
+  (void)rb;
+  (void)g_pair;
+#ifdef WF2G_CHECKED
+#define RING_OK(ptr) CHK((const void*)(ptr) >= rb.lo && (const void*)(ptr) < rb.hi, 2, (const OffT*)(ptr) - ring)
+#define RING_LD(r, k) (RING_OK((r) + (k)) ? (int32_t)(r)[k] : (int32_t)null_of<OffT>())
+#define RING_ST(r, k, v) do { if (RING_OK((r) + (k))) (r)[k] = (v); } while (0)
+#else
+#define RING_LD(r, k) ((int32_t)(r)[k])
+#define RING_ST(r, k, v) ((r)[k] = (v))
+#endif
+
   // ring starts all-NULL, every row empty
-  for (int i = lane; i < nrows * wcap; i += 32) m.ring[i] = null_of<OffT>();
-  for (int r = lane; r < nrows; r += 32) m.meta[r] = make_int2(1, 0);
+  for (int64_t i = lane; i < (int64_t)(nrows + 1) * stride; i += 32) ring[i] = null_of<OffT>();
+  for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
   __syncwarp();
 
   const int n_items = p.num_items_dev ? *p.num_items_dev : p.n_items;
@@ -195,23 +257,23 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
     item = __shfl_sync(kFull, item, 0);
     if (item >= n_items) break;
     const int pair = p.items ? p.items[item] : item;
+    g_pair = pair;
     const int plen = p.p_len[pair];
     const int tlen = p.t_len[pair];
 
-    // ---- reset ring rows used by the previous pair
+    // ---- reset the rows the previous pair left non-NULL
     for (int r = 0; r < nrows; ++r) {
-      const int2 mt = m.meta[r];
-      if (mt.x <= mt.y) null_range(m.ring + (size_t)r * wcap, mt.x, mt.y, mask, lane);
+      const int2 mt = meta[r];
+      if (mt.x <= mt.y) null_range(row(r), mt.x, mt.y, lane, rb, g_pair);
     }
     __syncwarp();
-    for (int r = lane; r < nrows; r += 32) m.meta[r] = make_int2(1, 0);
+    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
 
     // ---- stage sequences
-    bool ok = true;
-    if (plen > p.max_len || tlen > p.max_len) ok = false;
+    bool ok = (plen <= p.max_len) && (tlen <= p.max_len);
     if (ok) {
-      ok &= stage_sequence<ENC>(p.seqs + p.p_off[pair], plen, m.P, nwords, lane);
-      ok &= stage_sequence<ENC>(p.seqs + p.t_off[pair], tlen, m.T, nwords, lane);
+      ok &= stage_sequence<ENC>(p.seqs + p.p_off[pair], plen, P, lane);
+      ok &= stage_sequence<ENC>(p.seqs + p.t_off[pair], tlen, T, lane);
     }
     if (!ok) {
       if (lane == 0) {
@@ -227,12 +289,11 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
       continue;
     }
 
-    // ---- score 0: M[0][0] = 0 (wavefront/wavefront_aligner.c:236-253)
-    OffT* const rowM0 = m.ring;  // slot 0
+    // ---- score 0: M[0][0] = 0 (wavefront/wavefront_aligner.c:236-253), slot 0
     if (lane == 0) {
-      rowM0[0] = 0;
-      m.meta[0] = make_int2(0, 0);
-      if (CIGAR) m.table[0] = make_int2(0, 0);
+      RING_ST(row(0), 0, (OffT)0);
+      meta[0] = make_int2(0, 0);
+      if (CIGAR) table[0] = make_int2(0, 0);
     }
     __syncwarp();
 
@@ -240,39 +301,36 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
     int curM = 0, cur1 = 0, cur2 = 0;  // ring slots of score s
     int null_steps = 0;
     int64_t cursor = 0;  // choice bytes used
-    int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable
+    int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable, 4 guard
     const int k_end = tlen - plen;
     int mlo = 0, mhi = 0;  // trimmed limits of M[s]
     bool m_exists = true;
 
     while (true) {
       // ================= extend M[s] and test termination
-      if (m_exists) {
-        OffT* rowM = m.ring + (size_t)curM * wcap;
+      if (m_exists && mlo <= mhi) {  // an empty M (mlo > mhi) has nothing to extend
+        OffT* const rowM = row(curM);
         for (int k = mlo + lane; k <= mhi; k += 32) {
-          const int32_t off = rowM[k & mask];
+          const int32_t off = RING_LD(rowM, k);
           if (off >= 0) {
             const int v = off - k;
-            const int lim = min(plen - v, tlen - off);
-            const int L = lcp<ENC>(m.P, m.T, v, off, lim);
-            if (L) rowM[k & mask] = (OffT)(off + L);
+            const int L = lcp<ENC>(P, T, v, off, min(plen - v, tlen - off), nwords, g_pair);
+            if (L) RING_ST(rowM, k, (OffT)(off + L));
           }
         }
         __syncwarp();
-        if (mlo <= k_end && k_end <= mhi && (int32_t)rowM[k_end & mask] >= tlen) {
+        if (mlo <= k_end && k_end <= mhi && RING_LD(rowM, k_end) >= tlen) {
           result = 1;
           break;
         }
-      } else if (null_steps > pen.R) {
+      } else if (!m_exists && null_steps > pen.R) {
         result = 3;
         break;
       }
 
       // ================= compute score s+1
       ++s;
-      // no end-to-end alignment scores above the reference's bound
-      // (wavefront/wavefront_components.c:101-108): a guard, never hit
-      if (s > p.table_cap) {
+      if (s > p.table_cap) {  // above the reference's score bound: a guard, never hit
         result = 4;
         break;
       }
@@ -280,23 +338,24 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
       cur1 = (cur1 + 1 == pen.RI1) ? 0 : cur1 + 1;
       if (A2P) cur2 = (cur2 + 1 == pen.RI2) ? 0 : cur2 + 1;
 
-      // input rows (score < 0 -> empty)
-      const int sMx = ring_mod_back(curM, pen.x, pen.R);
-      const int sMo1 = ring_mod_back(curM, pen.o1 + pen.e1, pen.R);
-      const int sI1 = ring_mod_back(cur1, pen.e1, pen.RI1);
-      const int2 eMx = (s - pen.x >= 0) ? m.meta[sMx] : make_int2(1, 0);
-      const int2 eMo1 = (s - pen.o1 - pen.e1 >= 0) ? m.meta[sMo1] : make_int2(1, 0);
-      const int2 eI1 = (s - pen.e1 >= 0) ? m.meta[rowI1 + sI1] : make_int2(1, 0);
-      const int2 eD1 = (s - pen.e1 >= 0) ? m.meta[rowD1 + sI1] : make_int2(1, 0);
+      // inputs (wavefront/wavefront_compute.c:306-352); score < 0 -> empty
+      const int sMx = ring_back(curM, pen.x, pen.R);
+      const int sMo1 = ring_back(curM, pen.o1 + pen.e1, pen.R);
+      const int sI1 = ring_back(cur1, pen.e1, pen.RI1);
+      const int2 kEmpty = make_int2(1, 0);
+      const int2 eMx = (s - pen.x >= 0) ? meta[sMx] : kEmpty;
+      const int2 eMo1 = (s - pen.o1 - pen.e1 >= 0) ? meta[sMo1] : kEmpty;
+      const int2 eI1 = (s - pen.e1 >= 0) ? meta[rowI1 + sI1] : kEmpty;
+      const int2 eD1 = (s - pen.e1 >= 0) ? meta[rowD1 + sI1] : kEmpty;
       int sMo2 = 0, sI2 = 0;
-      int2 eMo2 = make_int2(1, 0), eI2 = make_int2(1, 0), eD2 = make_int2(1, 0);
+      int2 eMo2 = kEmpty, eI2 = kEmpty, eD2 = kEmpty;
       if (A2P) {
-        sMo2 = ring_mod_back(curM, pen.o2 + pen.e2, pen.R);
-        sI2 = ring_mod_back(cur2, pen.e2, pen.RI2);
-        if (s - pen.o2 - pen.e2 >= 0) eMo2 = m.meta[sMo2];
+        sMo2 = ring_back(curM, pen.o2 + pen.e2, pen.R);
+        sI2 = ring_back(cur2, pen.e2, pen.RI2);
+        if (s - pen.o2 - pen.e2 >= 0) eMo2 = meta[sMo2];
         if (s - pen.e2 >= 0) {
-          eI2 = m.meta[rowI2 + sI2];
-          eD2 = m.meta[rowD2 + sI2];
+          eI2 = meta[rowI2 + sI2];
+          eD2 = meta[rowD2 + sI2];
         }
       }
       const bool vMx = eMx.x <= eMx.y, vMo1 = eMo1.x <= eMo1.y;
@@ -304,38 +363,33 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
       const bool vMo2 = A2P && eMo2.x <= eMo2.y;
       const bool vI2 = A2P && eI2.x <= eI2.y, vD2 = A2P && eD2.x <= eD2.y;
 
-      // output rows: clear the content left by the score that used the slot
-      OffT* oM = m.ring + (size_t)curM * wcap;
-      OffT* oI1 = m.ring + (size_t)(rowI1 + cur1) * wcap;
-      OffT* oD1 = m.ring + (size_t)(rowD1 + cur1) * wcap;
-      OffT* oI2 = A2P ? m.ring + (size_t)(rowI2 + cur2) * wcap : nullptr;
-      OffT* oD2 = A2P ? m.ring + (size_t)(rowD2 + cur2) * wcap : nullptr;
+      OffT* const oM = row(curM);
+      OffT* const oI1 = row(rowI1 + cur1);
+      OffT* const oD1 = row(rowD1 + cur1);
+      OffT* const oI2 = A2P ? row(rowI2 + cur2) : nullptr;
+      OffT* const oD2 = A2P ? row(rowD2 + cur2) : nullptr;
+      const int2 oldM = meta[curM], oldI1 = meta[rowI1 + cur1], oldD1 = meta[rowD1 + cur1];
+      const int2 oldI2 = A2P ? meta[rowI2 + cur2] : kEmpty;
+      const int2 oldD2 = A2P ? meta[rowD2 + cur2] : kEmpty;
 
       // wavefront/wavefront_compute_affine.c:236-243: all inputs null -> null step
       if (!(vMx | vMo1 | vI1 | vD1 | vMo2 | vI2 | vD2)) {
         ++null_steps;
-        {
-          int2 t = m.meta[curM];
-          if (t.x <= t.y) null_range(oM, t.x, t.y, mask, lane);
-          t = m.meta[rowI1 + cur1];
-          if (t.x <= t.y) null_range(oI1, t.x, t.y, mask, lane);
-          t = m.meta[rowD1 + cur1];
-          if (t.x <= t.y) null_range(oD1, t.x, t.y, mask, lane);
-          if (A2P) {
-            t = m.meta[rowI2 + cur2];
-            if (t.x <= t.y) null_range(oI2, t.x, t.y, mask, lane);
-            t = m.meta[rowD2 + cur2];
-            if (t.x <= t.y) null_range(oD2, t.x, t.y, mask, lane);
-          }
+        clear_outside(oM, oldM, 1, 0, lane, rb, g_pair);
+        clear_outside(oI1, oldI1, 1, 0, lane, rb, g_pair);
+        clear_outside(oD1, oldD1, 1, 0, lane, rb, g_pair);
+        if (A2P) {
+          clear_outside(oI2, oldI2, 1, 0, lane, rb, g_pair);
+          clear_outside(oD2, oldD2, 1, 0, lane, rb, g_pair);
         }
         __syncwarp();
         if (lane == 0) {
-          m.meta[curM] = make_int2(1, 0);
-          m.meta[rowI1 + cur1] = make_int2(1, 0);
-          m.meta[rowD1 + cur1] = make_int2(1, 0);
+          meta[curM] = kEmpty;
+          meta[rowI1 + cur1] = kEmpty;
+          meta[rowD1 + cur1] = kEmpty;
           if (A2P) {
-            m.meta[rowI2 + cur2] = make_int2(1, 0);
-            m.meta[rowD2 + cur2] = make_int2(1, 0);
+            meta[rowI2 + cur2] = kEmpty;
+            meta[rowD2 + cur2] = kEmpty;
           }
         }
         if (CIGAR) {
@@ -343,7 +397,7 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
             result = -1;
             break;
           }
-          if (lane == 0) m.table[s] = make_int2(-1, 0);
+          if (lane == 0 && CHK(s < p.table_cap, 32, s)) table[s] = make_int2(-1, 0);
         }
         __syncwarp();
         m_exists = false;
@@ -367,133 +421,82 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
         if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
       }
       const int width = hi - lo + 1;
-      if (width + 2 > wcap) {
+      if (CIGAR && (s >= p.table_cap || cursor + width > p.bits_cap)) {
         result = -1;
         break;
       }
-      if (CIGAR) {
-        if (s >= p.table_cap || cursor + width > p.bits_cap) {
-          result = -1;
-          break;
-        }
-      }
-      // clear old content of the output slots outside [lo,hi]
-      {
-        int2 t = m.meta[curM];
-        if (t.x <= t.y) {
-          null_range(oM, t.x, min(t.y, lo - 1), mask, lane);
-          null_range(oM, max(t.x, hi + 1), t.y, mask, lane);
-        }
-        t = m.meta[rowI1 + cur1];
-        if (t.x <= t.y) {
-          null_range(oI1, t.x, min(t.y, lo - 1), mask, lane);
-          null_range(oI1, max(t.x, hi + 1), t.y, mask, lane);
-        }
-        t = m.meta[rowD1 + cur1];
-        if (t.x <= t.y) {
-          null_range(oD1, t.x, min(t.y, lo - 1), mask, lane);
-          null_range(oD1, max(t.x, hi + 1), t.y, mask, lane);
-        }
-        if (A2P) {
-          t = m.meta[rowI2 + cur2];
-          if (t.x <= t.y) {
-            null_range(oI2, t.x, min(t.y, lo - 1), mask, lane);
-            null_range(oI2, max(t.x, hi + 1), t.y, mask, lane);
-          }
-          t = m.meta[rowD2 + cur2];
-          if (t.x <= t.y) {
-            null_range(oD2, t.x, min(t.y, lo - 1), mask, lane);
-            null_range(oD2, max(t.x, hi + 1), t.y, mask, lane);
-          }
-        }
+      clear_outside(oM, oldM, lo, hi, lane, rb, g_pair);
+      clear_outside(oI1, oldI1, lo, hi, lane, rb, g_pair);
+      clear_outside(oD1, oldD1, lo, hi, lane, rb, g_pair);
+      if (A2P) {
+        clear_outside(oI2, oldI2, lo, hi, lane, rb, g_pair);
+        clear_outside(oD2, oldD2, lo, hi, lane, rb, g_pair);
       }
       __syncwarp();
 
-      // input row pointers; a null input reads as all-NULL: point it at an
-      // output row position range that is NULL?  Simpler: select per read.
-      const OffT* rMx = m.ring + (size_t)sMx * wcap;
-      const OffT* rMo1 = m.ring + (size_t)sMo1 * wcap;
-      const OffT* rI1 = m.ring + (size_t)(rowI1 + sI1) * wcap;
-      const OffT* rD1 = m.ring + (size_t)(rowD1 + sI1) * wcap;
-      const OffT* rMo2 = A2P ? m.ring + (size_t)sMo2 * wcap : nullptr;
-      const OffT* rI2 = A2P ? m.ring + (size_t)(rowI2 + sI2) * wcap : nullptr;
-      const OffT* rD2 = A2P ? m.ring + (size_t)(rowD2 + sI2) * wcap : nullptr;
-      uint8_t* brow = CIGAR ? m.bits + cursor - lo : nullptr;
+      const OffT* const rMx = vMx ? row(sMx) : null_row;
+      const OffT* const rMo1 = vMo1 ? row(sMo1) : null_row;
+      const OffT* const rI1 = vI1 ? row(rowI1 + sI1) : null_row;
+      const OffT* const rD1 = vD1 ? row(rowD1 + sI1) : null_row;
+      const OffT* const rMo2 = vMo2 ? row(sMo2) : null_row;
+      const OffT* const rI2 = vI2 ? row(rowI2 + sI2) : null_row;
+      const OffT* const rD2 = vD2 ? row(rowD2 + sI2) : null_row;
+      uint8_t* const brow = CIGAR ? bits + cursor - lo : nullptr;
 
       int tloM = INT32_MAX, thiM = INT32_MIN;
       int tloI1 = INT32_MAX, thiI1 = INT32_MIN, tloD1 = INT32_MAX, thiD1 = INT32_MIN;
       int tloI2 = INT32_MAX, thiI2 = INT32_MIN, tloD2 = INT32_MAX, thiD2 = INT32_MIN;
       for (int k = lo + lane; k <= hi; k += 32) {
-        const int km = (k - 1) & mask, k0 = k & mask, kp = (k + 1) & mask;
-        // empty input rows read as NULL (a stale slot is never read)
-        const int32_t mo1_m = vMo1 ? rMo1[km] : kNull;
-        const int32_t mo1_p = vMo1 ? rMo1[kp] : kNull;
-        const int32_t i1_e = vI1 ? rI1[km] : kNull;
-        const int32_t d1_e = vD1 ? rD1[kp] : kNull;
-        const int32_t mx = vMx ? rMx[k0] : kNull;
+        const int32_t mo1_m = RING_LD(rMo1, k - 1), mo1_p = RING_LD(rMo1, k + 1);
+        const int32_t i1_e = RING_LD(rI1, k - 1), d1_e = RING_LD(rD1, k + 1);
+        const int32_t mx = RING_LD(rMx, k);
         // wavefront/wavefront_compute_affine.c:66-84
         int32_t i1 = max(mo1_m, i1_e) + 1;
-        int32_t d1 = max(mo1_p, d1_e);
+        const int32_t d1 = max(mo1_p, d1_e);
         const int32_t mis = mx + 1;
         int32_t ins = i1, del = d1;
-        int32_t i2 = kNull, d2 = kNull;
-        int32_t mo2_m = kNull, mo2_p = kNull, i2_e = kNull, d2_e = kNull;
+        int32_t i2 = kNull, d2 = kNull, mo2_m = kNull, mo2_p = kNull, i2_e = kNull, d2_e = kNull;
         if (A2P) {
           // wavefront/wavefront_compute_affine2p.c:78-95
-          mo2_m = vMo2 ? rMo2[km] : kNull;
-          mo2_p = vMo2 ? rMo2[kp] : kNull;
-          i2_e = vI2 ? rI2[km] : kNull;
-          d2_e = vD2 ? rD2[kp] : kNull;
+          mo2_m = RING_LD(rMo2, k - 1);
+          mo2_p = RING_LD(rMo2, k + 1);
+          i2_e = RING_LD(rI2, k - 1);
+          d2_e = RING_LD(rD2, k + 1);
           i2 = max(mo2_m, i2_e) + 1;
           d2 = max(mo2_p, d2_e);
           ins = max(i1, i2);
           del = max(d1, d2);
         }
-        int32_t mval = max(del, max(mis, ins));
-        if ((uint32_t)mval > (uint32_t)tlen || (uint32_t)(mval - k) > (uint32_t)plen) mval = kNull;
-        // canonical NULL for the gap components
-        if (i1 < 0) i1 = kNull;
-        if (d1 < 0) d1 = kNull;
-        put(oM, k0, mval);
-        put(oI1, k0, i1);
-        put(oD1, k0, d1);
-        if (mval >= 0) { tloM = min(tloM, k); thiM = max(thiM, k); }
-        if ((uint32_t)i1 <= (uint32_t)tlen && (uint32_t)(i1 - k) <= (uint32_t)plen) {
-          tloI1 = min(tloI1, k); thiI1 = max(thiI1, k);
-        }
-        if ((uint32_t)d1 <= (uint32_t)tlen && (uint32_t)(d1 - k) <= (uint32_t)plen) {
-          tloD1 = min(tloD1, k); thiD1 = max(thiD1, k);
-        }
+        const int32_t best = max(del, max(mis, ins));
+        const bool okM = in_bounds(best, k, plen, tlen);
+        // NULLs are stored canonically (insertion values would drift upwards)
+        RING_ST(oM, k, okM ? (OffT)best : null_of<OffT>());
+        RING_ST(oI1, k, i1 < 0 ? null_of<OffT>() : (OffT)i1);
+        RING_ST(oD1, k, d1 < 0 ? null_of<OffT>() : (OffT)d1);
+        if (okM) { tloM = min(tloM, k); thiM = k; }
+        if (in_bounds(i1, k, plen, tlen)) { tloI1 = min(tloI1, k); thiI1 = k; }
+        if (in_bounds(d1, k, plen, tlen)) { tloD1 = min(tloD1, k); thiD1 = k; }
         if (A2P) {
-          if (i2 < 0) i2 = kNull;
-          if (d2 < 0) d2 = kNull;
-          put(oI2, k0, i2);
-          put(oD2, k0, d2);
-          if ((uint32_t)i2 <= (uint32_t)tlen && (uint32_t)(i2 - k) <= (uint32_t)plen) {
-            tloI2 = min(tloI2, k); thiI2 = max(thiI2, k);
-          }
-          if ((uint32_t)d2 <= (uint32_t)tlen && (uint32_t)(d2 - k) <= (uint32_t)plen) {
-            tloD2 = min(tloD2, k); thiD2 = max(thiD2, k);
-          }
+          RING_ST(oI2, k, i2 < 0 ? null_of<OffT>() : (OffT)i2);
+          RING_ST(oD2, k, d2 < 0 ? null_of<OffT>() : (OffT)d2);
+          if (in_bounds(i2, k, plen, tlen)) { tloI2 = min(tloI2, k); thiI2 = k; }
+          if (in_bounds(d2, k, plen, tlen)) { tloD2 = min(tloD2, k); thiD2 = k; }
         }
         if (CIGAR) {
-          // M source; exact ties: mismatch > D2 > D1 > I2 > I1
-          // (wavefront/wavefront_backtrace.c:49-59 type codes)
-          const int32_t best = max(mis, max(ins, del));
-          uint8_t src;
-          if (mis == best) src = kSrcX;
-          else if (A2P && d2 == best) src = kSrcD2;
-          else if (d1 == best) src = kSrcD1;
-          else if (A2P && i2 == best) src = kSrcI2;
-          else src = kSrcI1;
-          uint8_t c = src;
+          // M source with the reference's tie order: mismatch > D2 > D1 > I2 > I1
+          uint8_t c;
+          if (mis == best) c = kSrcX;
+          else if (A2P && d2 == best) c = kSrcD2;
+          else if (d1 == best) c = kSrcD1;
+          else if (A2P && i2 == best) c = kSrcI2;
+          else c = kSrcI1;
           c |= (uint8_t)(i1_e >= mo1_m) << 3;
           c |= (uint8_t)(d1_e >= mo1_p) << 4;
           if (A2P) {
             c |= (uint8_t)(i2_e >= mo2_m) << 5;
             c |= (uint8_t)(d2_e >= mo2_p) << 6;
           }
-          brow[k] = c;
+          if (CHK(cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
         }
       }
       __syncwarp();
@@ -509,32 +512,23 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
         tloD2 = __reduce_min_sync(kFull, tloD2);
         thiD2 = __reduce_max_sync(kFull, thiD2);
       }
-      // NULL the trimmed-away ends (wavefront/wavefront_compute.c:579-613)
-      auto trim_fill = [&](OffT* row, int tlo_, int thi_) {
-        if (tlo_ > thi_) {
-          null_range(row, lo, hi, mask, lane);
-        } else {
-          null_range(row, lo, tlo_ - 1, mask, lane);
-          null_range(row, thi_ + 1, hi, mask, lane);
-        }
-      };
-      trim_fill(oM, tloM, thiM);
-      trim_fill(oI1, tloI1, thiI1);
-      trim_fill(oD1, tloD1, thiD1);
+      trim_fill(oM, lo, hi, tloM, thiM, lane, rb, g_pair);
+      trim_fill(oI1, lo, hi, tloI1, thiI1, lane, rb, g_pair);
+      trim_fill(oD1, lo, hi, tloD1, thiD1, lane, rb, g_pair);
       if (A2P) {
-        trim_fill(oI2, tloI2, thiI2);
-        trim_fill(oD2, tloD2, thiD2);
+        trim_fill(oI2, lo, hi, tloI2, thiI2, lane, rb, g_pair);
+        trim_fill(oD2, lo, hi, tloD2, thiD2, lane, rb, g_pair);
       }
       __syncwarp();
       if (lane == 0) {
-        m.meta[curM] = make_int2(tloM, thiM);
-        m.meta[rowI1 + cur1] = make_int2(tloI1, thiI1);
-        m.meta[rowD1 + cur1] = make_int2(tloD1, thiD1);
+        meta[curM] = make_int2(tloM, thiM);
+        meta[rowI1 + cur1] = make_int2(tloI1, thiI1);
+        meta[rowD1 + cur1] = make_int2(tloD1, thiD1);
         if (A2P) {
-          m.meta[rowI2 + cur2] = make_int2(tloI2, thiI2);
-          m.meta[rowD2 + cur2] = make_int2(tloD2, thiD2);
+          meta[rowI2 + cur2] = make_int2(tloI2, thiI2);
+          meta[rowD2 + cur2] = make_int2(tloD2, thiD2);
         }
-        if (CIGAR) m.table[s] = make_int2((int)cursor, lo);
+        if (CIGAR && CHK(s < p.table_cap, 31, s)) table[s] = make_int2((int)cursor, lo);
       }
       if (CIGAR) cursor += width;
       mlo = tloM;
@@ -548,52 +542,27 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
       }
     }
 
-    // ================= finish the pair
-    if (result == -1) {
+    // ================= finish the pair (warp-uniform from here on)
+    if (result != 1) {
       if (lane == 0) {
-        if (p.final_pass) {
-          p.status[pair] = kStOOM;
-          p.scores[pair] = 0;
-          if (CIGAR) p.ops_len[pair] = 0;
-        } else {
+        if (result == -1 && !p.final_pass) {
           p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
+        } else {
+          int st, sc;
+          if (result == -1) { st = kStOOM; sc = 0; }
+          else if (result == 2) { st = kStMaxSteps; sc = -p.max_steps; }
+          else if (result == 3) { st = kStPartial; sc = -s; }
+          else { st = kStUnattainable; sc = 0; }
+          p.status[pair] = st;
+          p.scores[pair] = sc;
+          if (CIGAR) p.ops_len[pair] = 0;
         }
       }
       __syncwarp();
       continue;
     }
-    if (result == 2) {
-      if (lane == 0) {
-        p.status[pair] = kStMaxSteps;
-        p.scores[pair] = -p.max_steps;
-        if (CIGAR) p.ops_len[pair] = 0;
-      }
-      __syncwarp();
-      continue;
-    }
-    if (result == 4) {
-      if (lane == 0) {
-        p.status[pair] = kStUnattainable;
-        p.scores[pair] = 0;
-        if (CIGAR) p.ops_len[pair] = 0;
-      }
-      __syncwarp();
-      continue;
-    }
-    if (result == 3) {
-      if (lane == 0) {
-        p.status[pair] = kStPartial;
-        p.scores[pair] = -s;
-        if (CIGAR) p.ops_len[pair] = 0;
-      }
-      __syncwarp();
-      continue;
-    }
     // classic score (wavefront/wavefront_compute.c:108-120)
-    int score;
-    if (pen.match == 0) score = -s;
-    else score = ((-pen.match) * (plen + tlen) - s) / 2;
-
+    const int score = (pen.match == 0) ? -s : ((-pen.match) * (plen + tlen) - s) / 2;
     if (!CIGAR) {
       if (lane == 0) {
         p.scores[pair] = score;
@@ -603,100 +572,103 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
       continue;
     }
 
-    // ================= back-trace (choice bytes) then forward replay
-    if (lane == 0) {
-      uint8_t* items = m.bits + cursor;
-      const int64_t items_cap = p.bits_cap - cursor;
-      int64_t n = 0;
+    // ================= back-trace over choice bytes (uniform walk), then a
+    // forward replay that re-extends the matches of every M visit
+    uint8_t* const items = bits + cursor;
+    const int64_t items_cap = p.bits_cap - cursor;
+    int64_t n = 0;
+    bool bad = false;
+    {
       int st = 0;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
       int ss = s, kk = k_end;
-      bool bad = false;
       while (true) {
         if (n + 2 > items_cap || ss < 0) { bad = true; break; }
         if (st == 0) {
-          items[n++] = 'E';
+          if (lane == 0 && CHK(n < items_cap, 33, n)) items[n] = 'E';
+          ++n;
           if (ss == 0) {
-            if (kk != 0) bad = true;
+            bad = (kk != 0);
             break;
           }
         }
-        const int2 te = m.table[ss];
+        if (!CHK(ss < p.table_cap, 34, ss)) { bad = true; break; }
+        const int2 te = table[ss];
         const int64_t bi = (int64_t)te.x + (kk - te.y);
         if (te.x < 0 || kk < te.y || bi >= cursor) { bad = true; break; }
-        const uint8_t c = m.bits[bi];
+        if (!CHK(bi >= 0 && bi < p.bits_cap, 35, bi)) { bad = true; break; }
+        const uint8_t c = bits[bi];
+        char op = 0;
         if (st == 0) {
           const int src = c & 7;
-          if (src == kSrcX) { items[n++] = 'X'; ss -= pen.x; }
+          if (src == kSrcX) { op = 'X'; ss -= pen.x; }
           else if (src == kSrcD1) st = 2;
           else if (src == kSrcI1) st = 1;
           else if (src == kSrcD2) st = 4;
           else st = 3;
         } else if (st == 1) {
-          items[n++] = 'I';
-          kk -= 1;
+          op = 'I'; kk -= 1;
           if (c & 8) ss -= pen.e1; else { ss -= pen.o1 + pen.e1; st = 0; }
         } else if (st == 2) {
-          items[n++] = 'D';
-          kk += 1;
+          op = 'D'; kk += 1;
           if (c & 16) ss -= pen.e1; else { ss -= pen.o1 + pen.e1; st = 0; }
         } else if (st == 3) {
-          items[n++] = 'I';
-          kk -= 1;
+          op = 'I'; kk -= 1;
           if (c & 32) ss -= pen.e2; else { ss -= pen.o2 + pen.e2; st = 0; }
         } else {
-          items[n++] = 'D';
-          kk += 1;
+          op = 'D'; kk += 1;
           if (c & 64) ss -= pen.e2; else { ss -= pen.o2 + pen.e2; st = 0; }
         }
-      }
-      int out_n = 0;
-      if (!bad) {
-        uint8_t* out = p.ops + p.ops_off[pair];
-        int v = 0, h = 0;
-        for (int64_t i = n - 1; i >= 0; --i) {
-          const uint8_t it = items[i];
-          if (it == 'E') {
-            const int L = lcp<ENC>(m.P, m.T, v, h, min(plen - v, tlen - h));
-            for (int j = 0; j < L; ++j) out[out_n++] = 'M';
-            v += L;
-            h += L;
-          } else if (it == 'X') {
-            if (v >= plen || h >= tlen) { bad = true; break; }
-            out[out_n++] = 'X'; ++v; ++h;
-          } else if (it == 'I') {
-            if (h >= tlen) { bad = true; break; }
-            out[out_n++] = 'I'; ++h;
-          } else {
-            if (v >= plen) { bad = true; break; }
-            out[out_n++] = 'D'; ++v;
-          }
+        if (op) {
+          if (lane == 0 && CHK(n < items_cap, 36, n)) items[n] = (uint8_t)op;
+          ++n;
         }
-        if (v != plen || h != tlen) bad = true;
       }
-      if (bad) {
-        p.status[pair] = kStUnattainable;
-        p.scores[pair] = score;
-        p.ops_len[pair] = 0;
-      } else {
-        p.status[pair] = kStCompleted;
-        p.scores[pair] = score;
-        p.ops_len[pair] = out_n;
+    }
+    __syncwarp();
+    int out_n = 0;
+    if (!bad) {
+      uint8_t* const out = p.ops + p.ops_off[pair];
+      int v = 0, h = 0;
+      for (int64_t i = n - 1; i >= 0; --i) {
+        const uint8_t it = items[i];
+        if (it == 'E') {
+          const int L = lcp<ENC>(P, T, v, h, min(plen - v, tlen - h), nwords, g_pair);
+          for (int j = lane; j < L; j += 32)
+            if (CHK(out_n + j < plen + tlen, 37, out_n + j)) out[out_n + j] = 'M';
+          out_n += L;
+          v += L;
+          h += L;
+        } else {
+          if (it == 'X') { bad = (v >= plen || h >= tlen); ++v; ++h; }
+          else if (it == 'I') { bad = (h >= tlen); ++h; }
+          else { bad = (v >= plen); ++v; }
+          if (bad) break;
+          if (lane == 0 && CHK(out_n < plen + tlen, 38, out_n)) out[out_n] = it;
+          ++out_n;
+        }
       }
+      if (v != plen || h != tlen) bad = true;
+    }
+    if (lane == 0) {
+      p.status[pair] = bad ? kStUnattainable : kStCompleted;
+      p.scores[pair] = score;
+      p.ops_len[pair] = bad ? 0 : out_n;
     }
     __syncwarp();
   }
 }
 
 // -------------------------------------------------------------- launchers
-#define WF2G_INST(A2P, CIG, ENC, T) template __global__ void wfa_align_kernel<A2P, CIG, ENC, T>(const KParams p);
-#define WF2G_INST_T(T)               \
-  WF2G_INST(false, false, 2, T)      \
-  WF2G_INST(false, true, 2, T)       \
-  WF2G_INST(true, false, 2, T)       \
-  WF2G_INST(true, true, 2, T)        \
-  WF2G_INST(false, false, 8, T)      \
-  WF2G_INST(false, true, 8, T)       \
-  WF2G_INST(true, false, 8, T)       \
+#define WF2G_INST(A2P, CIG, ENC, T) \
+  template __global__ void wfa_align_kernel<A2P, CIG, ENC, T>(const KParams p);
+#define WF2G_INST_T(T)          \
+  WF2G_INST(false, false, 2, T) \
+  WF2G_INST(false, true, 2, T)  \
+  WF2G_INST(true, false, 2, T)  \
+  WF2G_INST(true, true, 2, T)   \
+  WF2G_INST(false, false, 8, T) \
+  WF2G_INST(false, true, 8, T)  \
+  WF2G_INST(true, false, 8, T)  \
   WF2G_INST(true, true, 8, T)
 WF2G_INST_T(int16_t)
 WF2G_INST_T(int32_t)
@@ -714,6 +686,21 @@ static void* pick(int a2p, int cigar, int enc) {
 // Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or 4-byte offsets).
 extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes) {
   return off_bytes == 2 ? pick<int16_t>(a2p, cigar, enc) : pick<int32_t>(a2p, cigar, enc);
+}
+
+// First bounds violation seen by a checked build: {site, index, pair, count}.
+extern "C" int wf2g_fault_info(unsigned long long* out) {
+#ifdef WF2G_CHECKED
+  return (int)cudaMemcpyFromSymbol(out, g_fault, 4 * sizeof(unsigned long long));
+#else
+  for (int i = 0; i < 4; ++i) out[i] = 0;
+  return 0;
+#endif
+}
+
+// Bytes of both staged sequences of one warp for an encoding and length bound.
+extern "C" int wf2g_seq_bytes(int enc, int max_len) {
+  return enc == 2 ? 2 * Seq<2>::words(max_len) * 4 : 2 * Seq<8>::words(max_len) * 8;
 }
 
 }  // namespace wf2g

@@ -1,32 +1,31 @@
 // wfa_kernels.cuh -- device-side data structures of the GB300 wavefront aligner.
 //
-// One warp aligns one pair at a time (lane = a stripe of diagonals), pulling
-// pair indices from a device work queue.  Per warp the kernel keeps, in shared
-// memory (or, for wide wavefronts, in a private slice of global memory):
-//   * both sequences, packed 2 bits per base (32 bases per 64-bit word, first
-//     base in the most significant bits) or 8 bits per byte for non-ACGT input;
-//   * a ring of the last max_score_scope M-wavefronts and the last e+1 I/D
-//     wavefronts, indexed by (k mod WCAP);
-//   * the ring's per-row limits.
-// Full-CIGAR runs also write, per computed cell, one byte of back-trace choice
-// bits into a per-warp global region; the device back-trace walks those bytes.
+// One warp aligns one pair at a time (lanes striped over diagonals k),
+// pulling pair indices from a device work queue.  Per warp:
+//   shared memory  both sequences, packed 2 bits per base (16 bases per 32-bit
+//                  word, first base in the most significant bits) or 1 byte per
+//                  base (8 per 64-bit word) for non-ACGT input; the per-row
+//                  limits of the wavefront ring;
+//   global memory  (a private slice, L1/L2 resident) the wavefront ring: the
+//                  last max_score_scope M rows and the last e+1 I/D rows, each
+//                  row indexed by k + kofs over every diagonal the pair can
+//                  reach, plus one all-NULL row; and, for full-CIGAR runs, one
+//                  back-trace choice byte per computed cell.
 #pragma once
 #include <cstdint>
 
 namespace wf2g {
 
-// Offsets are int32; any negative value is NULL.  Stored NULLs are canonical.
+// Offsets: any negative value is NULL; stored NULLs are canonical.
 constexpr int32_t kNull = INT32_MIN / 2;  // wavefront/wavefront_offset.h:46
 constexpr unsigned kFull = 0xffffffffu;
 
-// Per-pair status values written by the kernels (reference codes, wavefront/wfa.h:46-55,
-// plus internal retry codes that never reach the caller).
+// Per-pair status values written by the kernels (wavefront/wfa.h:46-55).
 constexpr int kStCompleted = 0;
 constexpr int kStPartial = 1;
 constexpr int kStMaxSteps = -100;
 constexpr int kStOOM = -200;
 constexpr int kStUnattainable = -300;
-constexpr int kStRetry = -1000;  // internal: re-run in the next pass
 
 // Back-trace choice byte, one per computed cell (s,k):
 //   bits 0-2  source of M:  0 mismatch, 1 D1, 2 I1, 3 D2, 4 I2
@@ -35,8 +34,8 @@ constexpr int kStRetry = -1000;  // internal: re-run in the next pass
 enum : uint8_t { kSrcX = 0, kSrcD1 = 1, kSrcI1 = 2, kSrcD2 = 3, kSrcI2 = 4 };
 
 struct Penalties {
-  int match;  // <= 0 (transformed set keeps the original match)
-  int x, o1, e1, o2, e2;
+  int match;  // user match (<= 0)
+  int x, o1, e1, o2, e2;  // internal (possibly Eizenga-transformed) penalties
   int R;    // M ring depth = max_score_scope
   int RI1;  // I1/D1 ring depth = e1+1
   int RI2;  // I2/D2 ring depth = e2+1 (affine2p)
@@ -56,7 +55,7 @@ struct KParams {
   const int32_t* num_items_dev;  // if non-null, overrides n_items
   int n_items;
   int32_t* queue;  // work-queue head (zeroed before launch)
-  // retry list for pairs this pass cannot finish (overflow / non-ACGT)
+  // retry list for pairs this pass cannot finish (non-ACGT / back-trace overflow)
   int32_t* retry_items;
   int32_t* retry_count;
   int final_pass;  // 1: report overflow as WF_STATUS_OOM instead of retrying
@@ -67,25 +66,18 @@ struct KParams {
   const int64_t* ops_off;
   int32_t* ops_len;
   // geometry of this pass
-  int wcap;          // ring width, power of two
-  int max_len;       // longest sequence staged by this pass
-  int ring_in_smem;  // 1: ring in shared memory, 0: in gscratch
-  int seq_in_smem;   // 1: staged sequences in shared memory, 0: in gscratch
-  int smem_per_warp; // bytes
-  uint8_t* gscratch; // per-warp global scratch
+  int max_len;        // longest sequence of the batch
+  int row_stride;     // ring row length (elements), >= 2*max_len+6
+  int kofs;           // diagonal k lives at element k+kofs of a row
+  int seq_in_smem;    // 1: staged sequences in shared memory, 0: in gscratch
+  int smem_per_warp;  // bytes
+  uint8_t* gscratch;  // per-warp global slices
   int64_t gscratch_per_warp;
-  // per-warp gscratch slice: [ring if !ring_in_smem][P,T if !seq_in_smem][table][bits]
-  int64_t ring_bytes_global;
-  int64_t seq_bytes_global;
-  int table_cap;     // back-trace row table entries (scores)
-  int64_t bits_cap;  // back-trace choice bytes per warp
-};
-
-// Host-side helpers shared with the engine.
-struct Geometry {
-  int nrows;            // ring rows
-  int seq_words;        // 64-bit words per staged sequence
-  int smem_per_warp;    // bytes of shared memory per warp
+  // per-warp slice: [ring: (nrows+1) rows][sequences if !seq_in_smem][table][bits]
+  int64_t ring_bytes;
+  int64_t seq_bytes;
+  int table_cap;      // back-trace row table entries (scores); also the score bound
+  int64_t bits_cap;   // back-trace choice bytes per warp
 };
 
 }  // namespace wf2g
