@@ -323,14 +323,14 @@ def main():
     bl.wf2g_bench_per_pair.restype = C.c_double
     P = C.c_void_p
     bl.wf2g_bench_per_pair.argtypes = [P, C.c_int, P, P, P, P, P, P, P, P]
-    k = min(args.per_pair_sample, n)
+    k = max(1, min(args.per_pair_sample, n))
     ps, pst, pl = (np.zeros(k, np.int32) for _ in range(3))
 
     def ptr(a):
         return C.c_void_p(a.ctypes.data)
     pa = W.Aligner(cfg)
-    bl.wf2g_bench_per_pair(C.cast(pa._h, P), 50, ptr(p.seqs), ptr(p.p_off), ptr(p.p_len),
-                           ptr(p.t_off), ptr(p.t_len), ptr(ps), ptr(pst), ptr(pl))
+    bl.wf2g_bench_per_pair(C.cast(pa._h, P), min(k, 50), ptr(p.seqs), ptr(p.p_off),
+                           ptr(p.p_len), ptr(p.t_off), ptr(p.t_len), ptr(ps), ptr(pst), ptr(pl))
     per_pair_s = bl.wf2g_bench_per_pair(C.cast(pa._h, P), k, ptr(p.seqs), ptr(p.p_off),
                                         ptr(p.p_len), ptr(p.t_off), ptr(p.t_len), ptr(ps),
                                         ptr(pst), ptr(pl))

@@ -196,8 +196,14 @@ __device__ __forceinline__ bool in_bounds(int32_t off, int k, int plen, int tlen
   return (uint32_t)off <= (uint32_t)tlen && (uint32_t)(off - k) <= (uint32_t)plen;
 }
 
+// 4 resident 256-thread blocks per SM (64 registers per thread): the kernel
+// is latency-bound, so residency matters more than registers.
+#ifndef WF2G_MIN_BLOCKS
+#define WF2G_MIN_BLOCKS 4
+#endif
+
 template <bool A2P, bool CIGAR, int ENC, typename OffT>
-__global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
+__global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const KParams p) {
   typedef typename Seq<ENC>::Word Word;
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
@@ -289,9 +295,11 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
       continue;
     }
 
-    // ---- score 0: M[0][0] = 0 (wavefront/wavefront_aligner.c:236-253), slot 0
+    // ---- score 0: M[0][0] = 0 (wavefront/wavefront_aligner.c:236-253), slot 0,
+    // extended at once (every later M cell is extended as it is computed)
+    const int L0 = lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair);
     if (lane == 0) {
-      RING_ST(row(0), 0, (OffT)0);
+      RING_ST(row(0), 0, (OffT)L0);
       meta[0] = make_int2(0, 0);
       if (CIGAR) table[0] = make_int2(0, 0);
     }
@@ -307,23 +315,14 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
     bool m_exists = true;
 
     while (true) {
-      // ================= extend M[s] and test termination
-      if (m_exists && mlo <= mhi) {  // an empty M (mlo > mhi) has nothing to extend
-        OffT* const rowM = row(curM);
-        for (int k = mlo + lane; k <= mhi; k += 32) {
-          const int32_t off = RING_LD(rowM, k);
-          if (off >= 0) {
-            const int v = off - k;
-            const int L = lcp<ENC>(P, T, v, off, min(plen - v, tlen - off), nwords, g_pair);
-            if (L) RING_ST(rowM, k, (OffT)(off + L));
-          }
-        }
-        __syncwarp();
-        if (mlo <= k_end && k_end <= mhi && RING_LD(rowM, k_end) >= tlen) {
+      // ================= termination on the extended M[s]
+      // (wavefront/wavefront_termination.c:37-60)
+      if (m_exists) {
+        if (mlo <= k_end && k_end <= mhi && RING_LD(row(curM), k_end) >= tlen) {
           result = 1;
           break;
         }
-      } else if (!m_exists && null_steps > pen.R) {
+      } else if (null_steps > pen.R) {
         result = 3;
         break;
       }
@@ -469,18 +468,33 @@ __global__ void __launch_bounds__(256) wfa_align_kernel(const KParams p) {
         }
         const int32_t best = max(del, max(mis, ins));
         const bool okM = in_bounds(best, k, plen, tlen);
-        // NULLs are stored canonically (insertion values would drift upwards)
-        RING_ST(oM, k, okM ? (OffT)best : null_of<OffT>());
-        RING_ST(oI1, k, i1 < 0 ? null_of<OffT>() : (OffT)i1);
-        RING_ST(oD1, k, d1 < 0 ? null_of<OffT>() : (OffT)d1);
+        // Trim tests (wavefront/wavefront_compute.c:579-613), simplified: a
+        // non-NULL insertion keeps its source's v <= plen, a deletion its h <= tlen
+        const bool okI1 = (uint32_t)i1 <= (uint32_t)tlen;
+        const bool okD1 = (uint32_t)(d1 - k) <= (uint32_t)plen;
+        // insertion values drift upwards from NULL: keep narrow NULLs canonical
+        if (sizeof(OffT) == 2 && i1 < 0) i1 = null_of<OffT>();
+        // extend the new M cell now (wavefront/wavefront_extend.c:86-121): the
+        // reference extends M[s] right after computing it, before score s+1
+        int32_t mext = null_of<OffT>();
+        if (okM) {
+          const int v = best - k;
+          mext = best + lcp<ENC>(P, T, v, best, min(plen - v, tlen - best), nwords, g_pair);
+        }
+        RING_ST(oM, k, (OffT)mext);
+        RING_ST(oI1, k, (OffT)i1);
+        RING_ST(oD1, k, (OffT)d1);
         if (okM) { tloM = min(tloM, k); thiM = k; }
-        if (in_bounds(i1, k, plen, tlen)) { tloI1 = min(tloI1, k); thiI1 = k; }
-        if (in_bounds(d1, k, plen, tlen)) { tloD1 = min(tloD1, k); thiD1 = k; }
+        if (okI1) { tloI1 = min(tloI1, k); thiI1 = k; }
+        if (okD1) { tloD1 = min(tloD1, k); thiD1 = k; }
         if (A2P) {
-          RING_ST(oI2, k, i2 < 0 ? null_of<OffT>() : (OffT)i2);
-          RING_ST(oD2, k, d2 < 0 ? null_of<OffT>() : (OffT)d2);
-          if (in_bounds(i2, k, plen, tlen)) { tloI2 = min(tloI2, k); thiI2 = k; }
-          if (in_bounds(d2, k, plen, tlen)) { tloD2 = min(tloD2, k); thiD2 = k; }
+          const bool okI2 = (uint32_t)i2 <= (uint32_t)tlen;
+          const bool okD2 = (uint32_t)(d2 - k) <= (uint32_t)plen;
+          if (sizeof(OffT) == 2 && i2 < 0) i2 = null_of<OffT>();
+          RING_ST(oI2, k, (OffT)i2);
+          RING_ST(oD2, k, (OffT)d2);
+          if (okI2) { tloI2 = min(tloI2, k); thiI2 = k; }
+          if (okD2) { tloD2 = min(tloD2, k); thiD2 = k; }
         }
         if (CIGAR) {
           // M source with the reference's tie order: mismatch > D2 > D1 > I2 > I1
