@@ -42,8 +42,6 @@
 #include <omp.h>
 #endif
 
-static orow_t k_null_row = {1, 1, 1, -1, 0, NULL};
-
 static int imin(int a, int b) { return a < b ? a : b; }
 static int imax(int a, int b) { return a > b ? a : b; }
 
@@ -82,9 +80,15 @@ static int setup_penalties(const int* cfg, pen_t* p) {
   return 0;
 }
 
-static orow_t* row_at(oracle_ws_t* ws, int s, int c) { return &ws->rows[(int64_t)s * NCOMP + c]; }
+/* Score-only alignments keep only the last max_score_scope scores, as the
+ * reference's modular wavefronts do (wavefront/wavefront_compute.c:434-441). */
+static orow_t* row_at(oracle_ws_t* ws, int s, int c) {
+  if (ws->modular) s %= ws->scope;
+  return &ws->rows[(int64_t)s * NCOMP + c];
+}
 
 static void ws_ensure_rows(oracle_ws_t* ws, int s) {
+  if (ws->modular) s = ws->scope - 1;
   if (s < ws->rows_cap) return;
   int ncap = ws->rows_cap ? ws->rows_cap : 1024;
   while (ncap <= s) ncap *= 2;
@@ -94,7 +98,7 @@ static void ws_ensure_rows(oracle_ws_t* ws, int s) {
   ws->rows_cap = ncap;
 }
 
-static int32_t* ws_alloc(oracle_ws_t* ws, int n) {
+static int32_t* ws_alloc(oracle_ws_t* ws, int64_t n) {
   while (ws->cur < ws->nchunks && ws->chunks[ws->cur].used + n > ws->chunks[ws->cur].cap) ws->cur++;
   if (ws->cur == ws->nchunks) {
     int64_t cap = (int64_t)1 << 20;
@@ -117,43 +121,79 @@ static void ws_reset(oracle_ws_t* ws) {
   ws->cur = 0;
 }
 
+/* Grows a k-indexed buffer to cover [lo,hi]; NULL-fills it when fill is set. */
+static void kbuf_cover(kbuf_t* b, int lo, int hi, int fill) {
+  if (b->mem && b->lo <= lo && hi <= b->hi) return;
+  const int nlo = b->mem ? imin(lo, b->lo) - 256 : lo - 256;
+  const int nhi = b->mem ? imax(hi, b->hi) + 256 : hi + 256;
+  free(b->mem);
+  b->mem = (int32_t*)malloc((size_t)(nhi - nlo + 1) * sizeof(int32_t));
+  if (fill)
+    for (int i = 0; i <= nhi - nlo; ++i) b->mem[i] = WF_NULL;
+  b->lo = nlo;
+  b->hi = nhi;
+}
+static int32_t* kbuf_at0(kbuf_t* b) { return b->mem - b->lo; }
+
+/* Storage for row (s,c) over diagonals [lo,hi] (k-indexed pointer). */
+static int32_t* row_storage(oracle_ws_t* ws, int s, int c, int lo, int hi) {
+  if (!ws->modular) return ws_alloc(ws, hi - lo + 1) - lo;
+  kbuf_t* b = &ws->slotbuf[(s % ws->scope) * NCOMP + c];
+  kbuf_cover(b, lo, hi, 0);
+  return kbuf_at0(b);
+}
+
 static void ws_free(oracle_ws_t* ws) {
   for (int i = 0; i < ws->nchunks; ++i) free(ws->chunks[i].mem);
   free(ws->chunks);
   free(ws->rows);
+  free(ws->nullbuf.mem);
+  free(ws->victim.mem);
+  if (ws->slotbuf) {
+    for (int i = 0; i < ws->scope * NCOMP; ++i) free(ws->slotbuf[i].mem);
+    free(ws->slotbuf);
+  }
 }
 
-static inline int32_t rd(const orow_t* r, int k) {
-  if (!r->exists || r->null || k < r->lo || k > r->hi) return WF_NULL;
-  return r->mem[k - r->base];
-}
-
-/* wavefront/wavefront_compute.c:354-368 (fetch with NULL substitution) */
-static const orow_t* fetch(oracle_ws_t* ws, int s, int c) {
-  if (s < 0) return &k_null_row;
-  const orow_t* r = row_at(ws, s, c);
-  if (!r->exists || r->null) return &k_null_row;
+/* wavefront/wavefront_compute.c:354-368: NULL or null wavefronts read as the
+ * shared all-NULL wavefront (lo=1, hi=-1; wavefront/wavefront.c:118-145). */
+static orow_t* fetch(oracle_ws_t* ws, orow_t* nullrow, int s, int c) {
+  if (s < 0) return nullrow;
+  orow_t* r = row_at(ws, s, c);
+  if (!r->exists || r->null) return nullrow;
   return r;
+}
+
+/* wavefront/wavefront_compute.c:498-527: NULL-pad an input beyond its
+ * initialised window so the compute loop reads [lo,hi] without peeling. */
+static void init_ends(orow_t* r, int lo, int hi) {
+  if (r->null) return;
+  if (r->ilo > lo) {
+    for (int k = lo; k < r->ilo; ++k) r->off[k] = WF_NULL;
+    r->ilo = lo;
+  }
+  if (r->ihi < hi) {
+    for (int k = r->ihi + 1; k <= hi; ++k) r->off[k] = WF_NULL;
+    r->ihi = hi;
+  }
 }
 
 /* wavefront/wavefront_compute.c:579-613 */
 static void trim_row(orow_t* r, int plen, int tlen) {
   int k;
   for (k = r->hi; k >= r->lo; --k) {
-    const int32_t off = r->mem[k - r->base];
-    const uint32_t h = (uint32_t)off;
-    const uint32_t v = (uint32_t)(off - k);
-    if (h <= (uint32_t)tlen && v <= (uint32_t)plen) break;
+    const int32_t off = r->off[k];
+    if ((uint32_t)off <= (uint32_t)tlen && (uint32_t)(off - k) <= (uint32_t)plen) break;
   }
   r->hi = k;
+  r->ihi = k;
   const int hi = r->hi;
   for (k = r->lo; k <= hi; ++k) {
-    const int32_t off = r->mem[k - r->base];
-    const uint32_t h = (uint32_t)off;
-    const uint32_t v = (uint32_t)(off - k);
-    if (h <= (uint32_t)tlen && v <= (uint32_t)plen) break;
+    const int32_t off = r->off[k];
+    if ((uint32_t)off <= (uint32_t)tlen && (uint32_t)(off - k) <= (uint32_t)plen) break;
   }
   r->lo = k;
+  r->ilo = k;
   r->null = (r->lo > r->hi);
 }
 
@@ -163,17 +203,18 @@ static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, in
                             int* null_steps) {
   const int a2p = (p->metric == 4);
   ws_ensure_rows(ws, s);
-  const orow_t* mx = fetch(ws, s - p->x, C_M);
-  const orow_t* mo1 = fetch(ws, s - p->o1 - p->e1, C_M);
-  const orow_t* i1e = fetch(ws, s - p->e1, C_I1);
-  const orow_t* d1e = fetch(ws, s - p->e1, C_D1);
-  const orow_t* mo2 = &k_null_row;
-  const orow_t* i2e = &k_null_row;
-  const orow_t* d2e = &k_null_row;
+  orow_t nullrow = {1, 1, 1, -1, 1, -1, kbuf_at0(&ws->nullbuf)};
+  orow_t* mx = fetch(ws, &nullrow, s - p->x, C_M);
+  orow_t* mo1 = fetch(ws, &nullrow, s - p->o1 - p->e1, C_M);
+  orow_t* i1e = fetch(ws, &nullrow, s - p->e1, C_I1);
+  orow_t* d1e = fetch(ws, &nullrow, s - p->e1, C_D1);
+  orow_t* mo2 = &nullrow;
+  orow_t* i2e = &nullrow;
+  orow_t* d2e = &nullrow;
   if (a2p) {
-    mo2 = fetch(ws, s - p->o2 - p->e2, C_M);
-    i2e = fetch(ws, s - p->e2, C_I2);
-    d2e = fetch(ws, s - p->e2, C_D2);
+    mo2 = fetch(ws, &nullrow, s - p->o2 - p->e2, C_M);
+    i2e = fetch(ws, &nullrow, s - p->e2, C_I2);
+    d2e = fetch(ws, &nullrow, s - p->e2, C_D2);
   }
   for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, s, c), 0, sizeof(orow_t));
   if (mx->null && mo1->null && i1e->null && d1e->null && mo2->null && i2e->null && d2e->null) {
@@ -197,59 +238,97 @@ static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, in
     lo = imin(lo, d2e->lo - 1);
     hi = imax(hi, d2e->hi - 1);
   }
-  const int width = hi - lo + 1;
+  /* wavefront/wavefront_compute.c:88-104: allocation padded by scope+1 and
+   * never narrower than any earlier allocation of the alignment */
+  ws->hlo = imin(ws->hlo, lo - (p->scope + 1));
+  ws->hhi = imax(ws->hhi, hi + (p->scope + 1));
+  kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
+  kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
+  nullrow.off = kbuf_at0(&ws->nullbuf);
+  const int alo = ws->hlo, awidth = ws->hhi - ws->hlo + 1;
   /* wavefront/wavefront_compute.c:447-492: I/D outputs exist only if an input does */
   const int has[NCOMP] = {1, (!mo1->null || !i1e->null), (!mo1->null || !d1e->null),
                           a2p && (!mo2->null || !i2e->null), a2p && (!mo2->null || !d2e->null)};
   int32_t* out[NCOMP];
+  int32_t* const victim = kbuf_at0(&ws->victim);
   for (int c = 0; c < NCOMP; ++c) {
     orow_t* r = row_at(ws, s, c);
-    out[c] = NULL;
+    out[c] = victim;
     if (has[c]) {
-      r->mem = ws_alloc(ws, width);
+      r->off = row_storage(ws, s, c, alo, alo + awidth - 1);
       r->exists = 1;
-      r->base = lo;
       r->lo = lo;
       r->hi = hi;
-      out[c] = r->mem;
+      r->ilo = lo;
+      r->ihi = hi;
+      out[c] = r->off;
     }
   }
-  int32_t victim[4]; /* output for non-existing I/D components */
-  for (int k = lo; k <= hi; ++k) {
-    const int idx = k - lo;
-    /* wavefront/wavefront_compute_affine.c:65-85 */
-    const int32_t ins1_o = rd(mo1, k - 1), ins1_e = rd(i1e, k - 1);
-    const int32_t ins1 = (ins1_o > ins1_e ? ins1_o : ins1_e) + 1;
-    const int32_t del1_o = rd(mo1, k + 1), del1_e = rd(d1e, k + 1);
-    const int32_t del1 = del1_o > del1_e ? del1_o : del1_e;
-    int32_t ins = ins1, del = del1;
-    if (out[C_I1]) out[C_I1][idx] = ins1; else victim[0] = ins1;
-    if (out[C_D1]) out[C_D1][idx] = del1; else victim[1] = del1;
-    if (a2p) {
-      /* wavefront/wavefront_compute_affine2p.c:72-101 */
-      const int32_t ins2_o = rd(mo2, k - 1), ins2_e = rd(i2e, k - 1);
-      const int32_t ins2 = (ins2_o > ins2_e ? ins2_o : ins2_e) + 1;
-      const int32_t del2_o = rd(mo2, k + 1), del2_e = rd(d2e, k + 1);
-      const int32_t del2 = del2_o > del2_e ? del2_o : del2_e;
-      if (out[C_I2]) out[C_I2][idx] = ins2; else victim[2] = ins2;
-      if (out[C_D2]) out[C_D2][idx] = del2; else victim[3] = del2;
-      ins = ins > ins2 ? ins : ins2;
-      del = del > del2 ? del : del2;
+  /* wavefront/wavefront_compute.c:528-575 */
+  init_ends(mx, lo, hi);
+  init_ends(mo1, lo - 1, hi + 1);
+  init_ends(i1e, lo - 1, hi);
+  init_ends(d1e, lo, hi + 1);
+  if (a2p) {
+    init_ends(mo2, lo - 1, hi + 1);
+    init_ends(i2e, lo - 1, hi);
+    init_ends(d2e, lo, hi + 1);
+  }
+  const int32_t* __restrict__ const m_x = mx->off;
+  const int32_t* __restrict__ const m_o1 = mo1->off;
+  const int32_t* __restrict__ const i_e1 = i1e->off;
+  const int32_t* __restrict__ const d_e1 = d1e->off;
+  int32_t* __restrict__ const o_m = out[C_M];
+  int32_t* __restrict__ const o_i1 = out[C_I1];
+  int32_t* __restrict__ const o_d1 = out[C_D1];
+  if (!a2p) {
+    /* wavefront/wavefront_compute_affine.c:65-85 (the reference vectorises
+     * this loop with PRAGMA_LOOP_VECTORIZE, utils/commons.h:252-256) */
+#pragma GCC ivdep
+    for (int k = lo; k <= hi; ++k) {
+      const int32_t ins1 = (m_o1[k - 1] > i_e1[k - 1] ? m_o1[k - 1] : i_e1[k - 1]) + 1;
+      const int32_t del1 = m_o1[k + 1] > d_e1[k + 1] ? m_o1[k + 1] : d_e1[k + 1];
+      o_i1[k] = ins1;
+      o_d1[k] = del1;
+      const int32_t misms = m_x[k] + 1;
+      int32_t mmax = misms > ins1 ? misms : ins1;
+      mmax = del1 > mmax ? del1 : mmax;
+      if ((uint32_t)mmax > (uint32_t)tlen) mmax = WF_NULL;
+      if ((uint32_t)(mmax - k) > (uint32_t)plen) mmax = WF_NULL;
+      o_m[k] = mmax;
     }
-    const int32_t misms = rd(mx, k) + 1;
-    int32_t mmax = misms > ins ? misms : ins;
-    mmax = del > mmax ? del : mmax;
-    const uint32_t h = (uint32_t)mmax;
-    const uint32_t v = (uint32_t)(mmax - k);
-    if (h > (uint32_t)tlen) mmax = WF_NULL;
-    if (v > (uint32_t)plen) mmax = WF_NULL;
-    out[C_M][idx] = mmax;
+  } else {
+    /* wavefront/wavefront_compute_affine2p.c:71-105 */
+    const int32_t* __restrict__ const m_o2 = mo2->off;
+    const int32_t* __restrict__ const i_e2 = i2e->off;
+    const int32_t* __restrict__ const d_e2 = d2e->off;
+    int32_t* __restrict__ const o_i2 = out[C_I2];
+    int32_t* __restrict__ const o_d2 = out[C_D2];
+#pragma GCC ivdep
+    for (int k = lo; k <= hi; ++k) {
+      const int32_t ins1 = (m_o1[k - 1] > i_e1[k - 1] ? m_o1[k - 1] : i_e1[k - 1]) + 1;
+      const int32_t ins2 = (m_o2[k - 1] > i_e2[k - 1] ? m_o2[k - 1] : i_e2[k - 1]) + 1;
+      const int32_t del1 = m_o1[k + 1] > d_e1[k + 1] ? m_o1[k + 1] : d_e1[k + 1];
+      const int32_t del2 = m_o2[k + 1] > d_e2[k + 1] ? m_o2[k + 1] : d_e2[k + 1];
+      o_i1[k] = ins1;
+      o_i2[k] = ins2;
+      o_d1[k] = del1;
+      o_d2[k] = del2;
+      const int32_t ins = ins1 > ins2 ? ins1 : ins2;
+      const int32_t del = del1 > del2 ? del1 : del2;
+      const int32_t misms = m_x[k] + 1;
+      int32_t mmax = misms > ins ? misms : ins;
+      mmax = del > mmax ? del : mmax;
+      if ((uint32_t)mmax > (uint32_t)tlen) mmax = WF_NULL;
+      if ((uint32_t)(mmax - k) > (uint32_t)plen) mmax = WF_NULL;
+      o_m[k] = mmax;
+    }
   }
   for (int c = 0; c < NCOMP; ++c) {
     orow_t* r = row_at(ws, s, c);
     if (r->exists) trim_row(r, plen, tlen);
   }
-  return width;
+  return hi - lo + 1;
 }
 
 /* Exact LCP along a diagonal, stopping at the sequence ends
@@ -282,8 +361,8 @@ enum { BT_M = 9, BT_D2E = 8, BT_D2O = 7, BT_D1E = 6, BT_D1O = 5, BT_I2E = 4, BT_
 static inline int64_t cand(oracle_ws_t* ws, int s, int c, int k, int add, int type) {
   if (s < 0) return WF_NULL;
   const orow_t* r = row_at(ws, s, c);
-  if (!r->exists || k < r->lo || k > r->hi) return WF_NULL;
-  return ((int64_t)(r->mem[k - r->base] + add) << 4) | type;
+  if (!r->exists || k < r->ilo || k > r->ihi) return WF_NULL;
+  return ((int64_t)(r->off[k] + add) << 4) | type;
 }
 static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
 
@@ -387,17 +466,23 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
                       int tlen, int32_t* out_score, int32_t* out_status, char* ops,
                       int32_t* ops_len, int64_t* cells, int64_t* ext) {
   ws_reset(ws);
+  ws->hlo = 0;
+  ws->hhi = 0;
   ws_ensure_rows(ws, 0);
+  if (ws->modular) memset(ws->rows, 0, (size_t)ws->scope * NCOMP * sizeof(orow_t));
   for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, 0, c), 0, sizeof(orow_t));
-  /* wavefront/wavefront_aligner.c:236-253: M[0][0] = 0 */
+  /* wavefront/wavefront_aligner.c:236-253: M[0][0] = 0, allocation padded as
+   * wavefront_compute_limits_output does (wavefront/wavefront_compute.c:88-104) */
   {
+    ws->hlo = -(p->scope + 1);
+    ws->hhi = p->scope + 1;
+    kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
+    kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
     orow_t* m0 = row_at(ws, 0, C_M);
-    m0->mem = ws_alloc(ws, 1);
+    m0->off = row_storage(ws, 0, C_M, ws->hlo, ws->hhi);
     m0->exists = 1;
-    m0->base = 0;
-    m0->lo = 0;
-    m0->hi = 0;
-    m0->mem[0] = 0;
+    m0->lo = m0->hi = m0->ilo = m0->ihi = 0;
+    m0->off[0] = 0;
   }
   int s = 0;
   int null_steps = 0;
@@ -414,13 +499,13 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
       }
     } else {
       for (int k = m->lo; k <= m->hi; ++k) {
-        const int32_t off = m->mem[k - m->base];
+        const int32_t off = m->off[k];
         if (off == WF_NULL) continue;
         const int L = lcp(P, plen, T, tlen, off - k, off);
-        m->mem[k - m->base] = off + L;
+        m->off[k] = off + L;
         next += L;
       }
-      if (m->lo <= k_end && k_end <= m->hi && m->mem[k_end - m->base] >= tlen) {
+      if (m->lo <= k_end && k_end <= m->hi && m->off[k_end] >= tlen) {
         status = ST_END_REACHED;
         break;
       }
@@ -479,6 +564,9 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
   {
     oracle_ws_t ws;
     memset(&ws, 0, sizeof(ws));
+    ws.modular = p.score_only;
+    ws.scope = p.scope;
+    if (ws.modular) ws.slotbuf = (kbuf_t*)calloc((size_t)p.scope * NCOMP, sizeof(kbuf_t));
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 16)
 #endif

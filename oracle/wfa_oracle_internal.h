@@ -29,11 +29,11 @@ typedef struct {
 } pen_t;
 
 typedef struct {
-  int exists; /* wavefront stored for this score/component */
-  int null;   /* wavefront->null after trimming */
-  int lo, hi; /* trimmed limits */
-  int base;   /* offsets[k] stored at mem[k-base] */
-  int32_t* mem;
+  int exists;   /* wavefront stored for this score/component */
+  int null;     /* wavefront->null after trimming */
+  int lo, hi;   /* trimmed limits */
+  int ilo, ihi; /* NULL-initialised window (wf_elements_init_min/max) */
+  int32_t* off; /* off[k] addressable for every k of the allocated range */
 } orow_t;
 
 typedef struct {
@@ -42,14 +42,22 @@ typedef struct {
 } chunk_t;
 
 typedef struct {
-  /* per score, per component */
-  orow_t* rows;
-  int rows_cap; /* in scores */
-  /* chunked bump arena for offsets (chunks are never moved) */
-  chunk_t* chunks;
-  int nchunks, cur;
-} oracle_ws_t;
+  int32_t* mem; /* buffer */
+  int lo, hi;   /* covered diagonals */
+} kbuf_t;
 
+typedef struct {
+  orow_t* rows; /* per score, per component */
+  int rows_cap; /* in scores */
+  chunk_t* chunks; /* chunked bump arena (chunks never move) */
+  int nchunks, cur;
+  int hlo, hhi;   /* historic allocation bounds of the current pair */
+  int modular;    /* score-only: rows live in a ring of max_score_scope slots */
+  int scope;
+  kbuf_t* slotbuf; /* modular mode: one buffer per (slot, component) */
+  kbuf_t nullbuf; /* all-NULL row (the reference's wavefront_null) */
+  kbuf_t victim;  /* sink for non-allocated I/D outputs (wavefront_victim) */
+} oracle_ws_t;
 
 /* One unidirectional end-to-end alignment (high-memory semantics). */
 void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
