@@ -413,6 +413,42 @@ int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const in
     char* d_cigar_ops, const int64_t* d_cigar_offsets, int32_t* d_cigar_lengths,
     void* cuda_stream);
 
+/* Allocation-free variant of wavefront_align_batch_device().  No counterpart
+ * in the reference.
+ *
+ * For callers that cannot let a library allocate GPU memory: processes whose
+ * device memory belongs to a framework pool or is budgeted to the byte up
+ * front (long-running servers, plugins hosted inside another runtime), and
+ * code paths where cudaMalloc's implicit device-wide synchronisation cannot be
+ * tolerated.  This call never allocates or frees memory and calls no
+ * allocating library routine: its scratch (wavefront rows, back-trace bytes,
+ * work queue) is one fixed 64 MiB array compiled into the library, which every
+ * GPU that loads the library holds until the process exits.  The caller passes
+ * inputs and outputs in device memory of the CURRENT device, as for
+ * wavefront_align_batch_device(), and the work is queued on `cuda_stream`
+ * (NULL: the legacy default stream).
+ *
+ * Limits: every pattern and text at most 2048 characters (max_sequence_length
+ * above that is rejected with WF2G_ERR_ARGS and a message); a pair whose
+ * back-trace needs more than 512 KiB of choice bytes reports WF_STATUS_OOM.
+ * Concurrency is bounded by the array (tens of warps), so throughput is far
+ * below wavefront_align_batch_device().
+ *
+ * The first call on a device looks up that device's address of the array
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array and it keeps the last call's contents (the work
+ * queue head is cleared at the start of each call): calls whose GPU work
+ * overlaps -- on different streams, or from different threads -- race on it
+ * and must be serialised by the caller. */
+int wavefront_align_batch_device_noalloc(wavefront_aligner_t* const wf_aligner,
+    const int num_pairs, const char* d_seqs,
+    const int64_t* d_pattern_offsets, const int32_t* d_pattern_lengths,
+    const int64_t* d_text_offsets, const int32_t* d_text_lengths,
+    const int max_sequence_length,
+    int32_t* d_scores, int32_t* d_status,
+    char* d_cigar_ops, const int64_t* d_cigar_offsets, int32_t* d_cigar_lengths,
+    void* cuda_stream);
+
 /* Kernel launches issued by this aligner since it was created (an audit
  * counter for benchmarks). */
 int64_t wavefront_aligner_gpu_launches(const wavefront_aligner_t* const wf_aligner);

@@ -467,6 +467,27 @@ int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const in
                            cfg.score_only ? NULL : d_cigar_lengths, cuda_stream);
 }
 
+int wavefront_align_batch_device_noalloc(wavefront_aligner_t* const wf_aligner,
+                                         const int num_pairs, const char* d_seqs,
+                                         const int64_t* d_pattern_offsets,
+                                         const int32_t* d_pattern_lengths,
+                                         const int64_t* d_text_offsets,
+                                         const int32_t* d_text_lengths,
+                                         const int max_sequence_length, int32_t* d_scores,
+                                         int32_t* d_status, char* d_cigar_ops,
+                                         const int64_t* d_cigar_offsets, int32_t* d_cigar_lengths,
+                                         void* cuda_stream) {
+  if (!wf_aligner || num_pairs < 0) return WF2G_ERR_ARGS;
+  if (wf2g_engine_device() < 0) return WF2G_ERR_NO_GPU;
+  wf2g_cfg_t cfg;
+  if (make_cfg(wf_aligner, &cfg) != 0) return WF2G_ERR_CONFIG;
+  return wf2g_noalloc_align(&cfg, num_pairs, d_seqs, d_pattern_offsets, d_pattern_lengths,
+                            d_text_offsets, d_text_lengths, max_sequence_length, d_scores,
+                            d_status, cfg.score_only ? NULL : d_cigar_ops,
+                            cfg.score_only ? NULL : d_cigar_offsets,
+                            cfg.score_only ? NULL : d_cigar_lengths, cuda_stream);
+}
+
 int64_t wavefront_aligner_gpu_launches(const wavefront_aligner_t* const wf_aligner) {
   return wf_aligner ? wf2g_engine_launches(wf_aligner->engine) : 0;
 }

@@ -39,6 +39,13 @@ int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int num_pairs, int on
                       int32_t* ops_len, void* stream);
 
 int64_t wf2g_engine_launches(const void* engine);
+
+/* Allocation-free batch alignment on the current device (wfa_noalloc.cu):
+ * device pointers only, scratch from a fixed array in the library image. */
+int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int num_pairs, const char* d_seqs,
+                       const int64_t* d_p_off, const int32_t* d_p_len, const int64_t* d_t_off,
+                       const int32_t* d_t_len, int max_len, int32_t* d_scores, int32_t* d_status,
+                       char* d_ops, const int64_t* d_ops_off, int32_t* d_ops_len, void* stream);
 int wf2g_engine_device(void);
 
 #ifdef __cplusplus

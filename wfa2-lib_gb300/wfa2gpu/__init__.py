@@ -147,6 +147,7 @@ EXPORTED = [
     "cigar_print", "cigar_sprint", "cigar_print_SAM_CIGAR", "cigar_sprint_SAM_CIGAR",
     "cigar_print_pretty", "wavefront_align_batch", "wavefront_align_batch_device",
     "wavefront_aligner_gpu_launches", "wfa2gpu_device",
+    "wavefront_align_batch_device_noalloc",
 ]
 
 
@@ -181,6 +182,9 @@ def lib() -> C.CDLL:
     L.wavefront_align_batch_device.argtypes = [C.POINTER(Aligner_t), C.c_int, P, P, P, P, P,
                                                C.c_int, P, P, P, P, P, P]
     L.wavefront_align_batch_device.restype = C.c_int
+    L.wavefront_align_batch_device_noalloc.argtypes = [C.POINTER(Aligner_t), C.c_int, P, P, P,
+                                                       P, P, C.c_int, P, P, P, P, P, P]
+    L.wavefront_align_batch_device_noalloc.restype = C.c_int
     L.wavefront_aligner_gpu_launches.argtypes = [C.POINTER(Aligner_t)]
     L.wavefront_aligner_gpu_launches.restype = C.c_int64
     L.wfa2gpu_device.restype = C.c_int
@@ -319,6 +323,16 @@ class Aligner:
         """wavefront_align_batch_device() with raw device pointers (ints)."""
         V = C.c_void_p
         return lib().wavefront_align_batch_device(
+            self._h, n, V(d_seqs), V(d_poff), V(d_plen), V(d_toff), V(d_tlen), int(max_len),
+            V(d_scores), V(d_status), V(d_ops), V(d_ops_off), V(d_ops_len), V(stream))
+
+
+    def align_batch_device_noalloc(self, n, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len,
+                                   d_scores, d_status, d_ops=0, d_ops_off=0, d_ops_len=0,
+                                   stream=0) -> int:
+        """wavefront_align_batch_device_noalloc(): same arguments, no allocation."""
+        V = C.c_void_p
+        return lib().wavefront_align_batch_device_noalloc(
             self._h, n, V(d_seqs), V(d_poff), V(d_plen), V(d_toff), V(d_tlen), int(max_len),
             V(d_scores), V(d_status), V(d_ops), V(d_ops_off), V(d_ops_len), V(stream))
 
