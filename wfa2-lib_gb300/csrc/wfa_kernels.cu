@@ -445,22 +445,36 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       int tloM = INT32_MAX, thiM = INT32_MIN;
       int tloI1 = INT32_MAX, thiI1 = INT32_MIN, tloD1 = INT32_MAX, thiD1 = INT32_MIN;
       int tloI2 = INT32_MAX, thiI2 = INT32_MIN, tloD2 = INT32_MAX, thiD2 = INT32_MIN;
+      // Software-pipelined: the next cell's inputs are loaded before the
+      // current cell is computed, so one load latency overlaps the work.
+      int32_t n_mo1_m = 0, n_mo1_p = 0, n_i1_e = 0, n_d1_e = 0, n_mx = 0;
+      int32_t n_mo2_m = 0, n_mo2_p = 0, n_i2_e = 0, n_d2_e = 0;
+      auto load_inputs = [&](int kk) {
+        n_mo1_m = RING_LD(rMo1, kk - 1);
+        n_mo1_p = RING_LD(rMo1, kk + 1);
+        n_i1_e = RING_LD(rI1, kk - 1);
+        n_d1_e = RING_LD(rD1, kk + 1);
+        n_mx = RING_LD(rMx, kk);
+        if (A2P) {
+          n_mo2_m = RING_LD(rMo2, kk - 1);
+          n_mo2_p = RING_LD(rMo2, kk + 1);
+          n_i2_e = RING_LD(rI2, kk - 1);
+          n_d2_e = RING_LD(rD2, kk + 1);
+        }
+      };
+      if (lo + lane <= hi) load_inputs(lo + lane);
       for (int k = lo + lane; k <= hi; k += 32) {
-        const int32_t mo1_m = RING_LD(rMo1, k - 1), mo1_p = RING_LD(rMo1, k + 1);
-        const int32_t i1_e = RING_LD(rI1, k - 1), d1_e = RING_LD(rD1, k + 1);
-        const int32_t mx = RING_LD(rMx, k);
+        const int32_t mo1_m = n_mo1_m, mo1_p = n_mo1_p, i1_e = n_i1_e, d1_e = n_d1_e, mx = n_mx;
+        const int32_t mo2_m = n_mo2_m, mo2_p = n_mo2_p, i2_e = n_i2_e, d2_e = n_d2_e;
+        if (k + 32 <= hi) load_inputs(k + 32);
         // wavefront/wavefront_compute_affine.c:66-84
         int32_t i1 = max(mo1_m, i1_e) + 1;
         const int32_t d1 = max(mo1_p, d1_e);
         const int32_t mis = mx + 1;
         int32_t ins = i1, del = d1;
-        int32_t i2 = kNull, d2 = kNull, mo2_m = kNull, mo2_p = kNull, i2_e = kNull, d2_e = kNull;
+        int32_t i2 = kNull, d2 = kNull;
         if (A2P) {
           // wavefront/wavefront_compute_affine2p.c:78-95
-          mo2_m = RING_LD(rMo2, k - 1);
-          mo2_p = RING_LD(rMo2, k + 1);
-          i2_e = RING_LD(rI2, k - 1);
-          d2_e = RING_LD(rD2, k + 1);
           i2 = max(mo2_m, i2_e) + 1;
           d2 = max(mo2_p, d2_e);
           ins = max(i1, i2);
