@@ -369,9 +369,9 @@ static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
 /* wavefront/wavefront_backtrace.c:320-529, writing into a reversed buffer.
  * Returns the number of operations, or -1 on an inconsistent trace. */
 static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int score, int k_end,
-                     int32_t off_end, char* rev) {
+                     int32_t off_end, int comp_end, char* rev) {
   int n = 0;
-  int mat = C_M;
+  int mat = comp_end;
   int s = score, k = k_end;
   int32_t offset = off_end;
   int h = offset, v = offset - k;
@@ -462,91 +462,150 @@ static int classic_score(const pen_t* p, int plen, int tlen, int s) {
 }
 
 /* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273). */
-void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
-                      int tlen, int32_t* out_score, int32_t* out_status, char* ops,
-                      int32_t* ops_len, int64_t* cells, int64_t* ext) {
+const orow_t* oracle_row(oracle_ws_t* ws, int s, int c) { return row_at(ws, s, c); }
+
+void oracle_ws_init(oracle_ws_t* ws, int modular, int scope) {
+  memset(ws, 0, sizeof(*ws));
+  ws->modular = modular;
+  ws->scope = scope;
+  if (modular) ws->slotbuf = (kbuf_t*)calloc((size_t)scope * NCOMP, sizeof(kbuf_t));
+}
+
+void oracle_ws_free(oracle_ws_t* ws) { ws_free(ws); }
+
+/* ------------------------------------------------------------- stepper */
+/* Score-0 wavefront for an alignment that begins in component cb
+ * (wavefront/wavefront_aligner.c:236-382): M[0][0]=0, or the gap component's
+ * offset 0 on diagonal 0 with no M wavefront. */
+void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const char* P, int plen,
+                     const char* T, int tlen, int cb, int ce) {
+  ua->ws = ws;
+  ua->p = p;
+  ua->P = P;
+  ua->plen = plen;
+  ua->T = T;
+  ua->tlen = tlen;
+  ua->cb = cb;
+  ua->ce = ce;
+  ua->s = 0;
+  ua->null_steps = 0;
+  ua->k_end = tlen - plen;
+  ua->cells = 0;
+  ua->ext = 0;
   ws_reset(ws);
-  ws->hlo = 0;
-  ws->hhi = 0;
   ws_ensure_rows(ws, 0);
   if (ws->modular) memset(ws->rows, 0, (size_t)ws->scope * NCOMP * sizeof(orow_t));
   for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, 0, c), 0, sizeof(orow_t));
-  /* wavefront/wavefront_aligner.c:236-253: M[0][0] = 0, allocation padded as
-   * wavefront_compute_limits_output does (wavefront/wavefront_compute.c:88-104) */
-  {
-    ws->hlo = -(p->scope + 1);
-    ws->hhi = p->scope + 1;
-    kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
-    kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
-    orow_t* m0 = row_at(ws, 0, C_M);
-    m0->off = row_storage(ws, 0, C_M, ws->hlo, ws->hhi);
-    m0->exists = 1;
-    m0->lo = m0->hi = m0->ilo = m0->ihi = 0;
-    m0->off[0] = 0;
+  /* allocation padded as wavefront_compute_limits_output does
+   * (wavefront/wavefront_compute.c:88-104) */
+  ws->hlo = -(p->scope + 1);
+  ws->hhi = p->scope + 1;
+  kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
+  kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
+  orow_t* r0 = row_at(ws, 0, cb);
+  r0->off = row_storage(ws, 0, cb, ws->hlo, ws->hhi);
+  r0->exists = 1;
+  r0->lo = r0->hi = r0->ilo = r0->ihi = 0;
+  r0->off[0] = 0;
+}
+
+/* Extends M[s] and tests termination on component ce
+ * (wavefront/wavefront_extend.c:86-121,173-212,
+ * wavefront/wavefront_termination.c:37-114).  Returns ST_END_REACHED,
+ * ST_END_UNREACHABLE or 0; *max_ak (if given) receives the largest
+ * antidiagonal 2*offset-k of the extended cells, or 0
+ * (wavefront/wavefront_extend_kernels.c:130-153). */
+int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
+  oracle_ws_t* ws = ua->ws;
+  if (max_ak) *max_ak = 0;
+  orow_t* m = row_at(ws, ua->s, C_M);
+  if (!m->exists) {
+    if (ua->null_steps > ua->p->scope) return ST_END_UNREACHABLE;
+    return 0;
   }
-  int s = 0;
-  int null_steps = 0;
-  int64_t ncells = 0, next = 0;
-  const int k_end = tlen - plen;
+  int mak = 0;
+  for (int k = m->lo; k <= m->hi; ++k) {
+    const int32_t off = m->off[k];
+    if (off == WF_NULL) continue;
+    const int L = lcp(ua->P, ua->plen, ua->T, ua->tlen, off - k, off);
+    m->off[k] = off + L;
+    ua->ext += L;
+    const int ak = 2 * (off + L) - k;
+    if (mak < ak) mak = ak;
+  }
+  const orow_t* e = row_at(ws, ua->s, ua->ce);
+  const int k_end = ua->k_end;
+  if (e->exists && e->lo <= k_end && k_end <= e->hi && e->off[k_end] >= ua->tlen)
+    return ST_END_REACHED;
+  if (max_ak) *max_ak = mak;
+  return 0;
+}
+
+/* Computes wavefront s+1 (wavefront/wavefront_unialign.c:266-268). */
+void oracle_ua_compute(oracle_ua_t* ua) {
+  ua->s++;
+  ua->cells += compute_step(ua->ws, ua->p, ua->s, ua->plen, ua->tlen, &ua->null_steps);
+}
+
+/* Full back-trace of a finished stepper into ops (forward order); returns the
+ * number of operations or -1. */
+int oracle_ua_backtrace(oracle_ua_t* ua, char* ops) {
+  char* rev = (char*)malloc((size_t)(ua->plen + ua->tlen + 8));
+  const int n = backtrace(ua->ws, ua->p, ua->plen, ua->tlen, ua->s, ua->k_end, ua->tlen, ua->ce,
+                          rev);
+  if (n >= 0)
+    for (int i = 0; i < n; ++i) ops[i] = rev[n - 1 - i];
+  free(rev);
+  return n;
+}
+
+int oracle_classic_score(const pen_t* p, int plen, int tlen, int s) {
+  return classic_score(p, plen, tlen, s);
+}
+
+/* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273). */
+void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
+                      int tlen, int32_t* out_score, int32_t* out_status, char* ops,
+                      int32_t* ops_len, int64_t* cells, int64_t* ext) {
+  oracle_ua_t ua;
+  oracle_ua_start(&ua, ws, p, P, plen, T, tlen, C_M, C_M);
   int status;
   while (1) {
-    /* extend + termination (wavefront/wavefront_extend.c:86-121) */
-    orow_t* m = row_at(ws, s, C_M);
-    if (!m->exists) {
-      if (null_steps > p->scope) {
-        status = ST_END_UNREACHABLE;
-        break;
-      }
-    } else {
-      for (int k = m->lo; k <= m->hi; ++k) {
-        const int32_t off = m->off[k];
-        if (off == WF_NULL) continue;
-        const int L = lcp(P, plen, T, tlen, off - k, off);
-        m->off[k] = off + L;
-        next += L;
-      }
-      if (m->lo <= k_end && k_end <= m->hi && m->off[k_end] >= tlen) {
-        status = ST_END_REACHED;
-        break;
-      }
-    }
-    ++s;
-    ncells += compute_step(ws, p, s, plen, tlen, &null_steps);
+    status = oracle_ua_extend(&ua, NULL);
+    if (status) break;
+    oracle_ua_compute(&ua);
     /* wavefront/wavefront_unialign.c:102-107 */
-    if (s >= p->max_steps) {
-      if (ext) *ext = next;
+    if (ua.s >= p->max_steps) {
+      if (ext) *ext = ua.ext;
+      if (cells) *cells = ua.cells;
       *out_score = -p->max_steps;
       *out_status = ST_MAX_STEPS;
       *ops_len = 0;
-      if (cells) *cells = ncells;
       return;
     }
   }
-  if (cells) *cells = ncells;
-  if (ext) *ext = next;
+  if (cells) *cells = ua.cells;
+  if (ext) *ext = ua.ext;
   if (status == ST_END_UNREACHABLE) {
-    *out_score = classic_score(p, 0, 0, s);
+    *out_score = classic_score(p, 0, 0, ua.s);
     *out_status = 1; /* WF_STATUS_ALG_PARTIAL */
     *ops_len = 0;
     return;
   }
   /* wavefront/wavefront_unialign.c:147-237 */
-  *out_score = classic_score(p, plen, tlen, s);
+  *out_score = classic_score(p, plen, tlen, ua.s);
   *out_status = ST_COMPLETED;
   if (p->score_only || ops == NULL) {
     *ops_len = 0;
     return;
   }
-  char* rev = (char*)malloc((size_t)(plen + tlen + 8));
-  const int n = backtrace(ws, p, plen, tlen, s, k_end, tlen, rev);
+  const int n = oracle_ua_backtrace(&ua, ops);
   if (n < 0) {
     *out_status = ST_UNATTAINABLE;
     *ops_len = 0;
   } else {
-    for (int i = 0; i < n; ++i) ops[i] = rev[n - 1 - i];
     *ops_len = n;
   }
-  free(rev);
 }
 
 int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, const int64_t* p_off,
@@ -563,10 +622,7 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
 #endif
   {
     oracle_ws_t ws;
-    memset(&ws, 0, sizeof(ws));
-    ws.modular = p.score_only;
-    ws.scope = p.scope;
-    if (ws.modular) ws.slotbuf = (kbuf_t*)calloc((size_t)p.scope * NCOMP, sizeof(kbuf_t));
+    oracle_ws_init(&ws, p.score_only && !ultralow, p.scope);
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 16)
 #endif

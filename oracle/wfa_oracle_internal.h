@@ -59,6 +59,31 @@ typedef struct {
   kbuf_t victim;  /* sink for non-allocated I/D outputs (wavefront_victim) */
 } oracle_ws_t;
 
+/* Unidirectional stepper: an alignment of P against T that begins in
+ * component cb and ends in component ce (C_M, C_I1, C_D1, C_I2, C_D2). */
+typedef struct {
+  oracle_ws_t* ws;
+  const pen_t* p;
+  const char* P;
+  int plen;
+  const char* T;
+  int tlen;
+  int cb, ce;
+  int s, null_steps, k_end;
+  int64_t cells, ext;
+} oracle_ua_t;
+
+void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const char* P, int plen,
+                     const char* T, int tlen, int cb, int ce);
+int oracle_ua_extend(oracle_ua_t* ua, int* max_ak);
+void oracle_ua_compute(oracle_ua_t* ua);
+int oracle_ua_backtrace(oracle_ua_t* ua, char* ops);
+int oracle_classic_score(const pen_t* p, int plen, int tlen, int s);
+/* Wavefront row (s,c) of a stepper's workspace. */
+const orow_t* oracle_row(oracle_ws_t* ws, int s, int c);
+void oracle_ws_init(oracle_ws_t* ws, int modular, int scope);
+void oracle_ws_free(oracle_ws_t* ws);
+
 /* One unidirectional end-to-end alignment (high-memory semantics). */
 void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
                       int tlen, int32_t* out_score, int32_t* out_status, char* ops,

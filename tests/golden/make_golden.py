@@ -6,7 +6,7 @@ sources are available; the fixtures themselves travel with the repo).
 2. ``utest_expected.json`` -- for every in-scope configuration of the
    reference test-suite (tests/wfa.utest.sh:35-64: gap-affine, gap-affine-2p
    and penalty sets p0..p5; modes full CIGAR/high, score-only, med, BiWFA
-   score-only), the reference's own expected output per pair from
+   full CIGAR and BiWFA score-only), the reference's own expected output per pair from
    tests/wfa.utest.check/*.alg: the printed score and the CRC32 of the
    printed RLE CIGAR ("-" when there is none).
 3. ``synthetic_expected.json`` -- outputs of the UNMODIFIED reference library
@@ -45,15 +45,22 @@ MODES = {
     "test.score": (0, True),
     "test.pb": (1, False),
     "test.biwfa.score": (3, True),
+    "test.biwfa": (3, False),
 }
-# synthetic fixture sets: name -> (workload, n, penalty set, score_only, memory mode)
+# synthetic fixture sets:
+# name -> (workload, n, penalty set, score_only, memory mode, param, param2)
 SYNTHETIC = {
-    "w0_affine_full": (0, 2000, "affine", False, 0),
-    "w0_affine_score": (0, 2000, "affine", True, 0),
-    "w1_affine_full": (1, 300, "affine", False, 0),
-    "w1_affine_score": (1, 300, "affine", True, 0),
-    "w2_affine2p_full": (2, 40, "affine2p", False, 0),
-    "w5_affine_p3_full": (5, 300, "affine.p3", False, 0),
+    "w0_affine_full": (0, 2000, "affine", False, 0, 0, 0),
+    "w0_affine_score": (0, 2000, "affine", True, 0, 0, 0),
+    "w1_affine_full": (1, 300, "affine", False, 0, 0, 0),
+    "w1_affine_score": (1, 300, "affine", True, 0, 0, 0),
+    "w2_affine2p_full": (2, 40, "affine2p", False, 0, 0, 0),
+    "w5_affine_p3_full": (5, 300, "affine.p3", False, 0, 400, 80),
+    # BiWFA (ultralow memory mode) on pairs long enough to split at breakpoints
+    "w5_affine_biwfa_full": (5, 60, "affine", False, 3, 3000, 300),
+    "w5_affine2p_biwfa_full": (5, 30, "affine2p", False, 3, 3000, 300),
+    "w5_affine_p3_biwfa_full": (5, 30, "affine.p3", False, 3, 3000, 300),
+    "w1_affine_biwfa_score": (1, 100, "affine", True, 3, 0, 0),
 }
 
 
@@ -89,11 +96,10 @@ def main():
     O.build(ref=True)
     W.build()
     synth = {}
-    for name, (wl, n, pset, so, mm) in SYNTHETIC.items():
+    for name, (wl, n, pset, so, mm, param, param2) in SYNTHETIC.items():
         m, mi, mm_, o1, e1, o2, e2 = PENALTY_SETS[pset][0], *PENALTY_SETS[pset][1:]
         pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
                           gap_opening2=o2, gap_extension2=e2)
-        param, param2 = (400, 80) if wl == 5 else (0, 0)
         p = W.generate(wl, n, param=param, param2=param2)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
         r = O.align(b, pen, memory_mode=mm, score_only=so, kind="reference")
