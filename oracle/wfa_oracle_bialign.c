@@ -203,7 +203,12 @@ static int bi_base(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce) {
     st = oracle_ua_extend(&U, NULL);
     if (st) break;
     oracle_ua_compute(&U);
-    if (U.s >= p->max_steps) return ST_UNATTAINABLE;
+    if (U.s >= p->max_steps) {
+      /* wavefront/wavefront_unialign.c:102-107 sets the base CIGAR's score,
+       * which wavefront_bialign_base copies before failing */
+      b->score = -p->max_steps;
+      return ST_UNATTAINABLE;
+    }
   }
   if (st != ST_END_REACHED) return ST_UNATTAINABLE;
   const int n = oracle_ua_backtrace(&U, b->ops + b->nops);

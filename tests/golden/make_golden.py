@@ -48,7 +48,7 @@ MODES = {
     "test.biwfa": (3, False),
 }
 # synthetic fixture sets:
-# name -> (workload, n, penalty set, score_only, memory mode, param, param2)
+# name -> (workload, n, penalty set, score_only, memory mode, param, param2[, max_steps])
 SYNTHETIC = {
     "w0_affine_full": (0, 2000, "affine", False, 0, 0, 0),
     "w0_affine_score": (0, 2000, "affine", True, 0, 0, 0),
@@ -61,6 +61,12 @@ SYNTHETIC = {
     "w5_affine2p_biwfa_full": (5, 30, "affine2p", False, 3, 3000, 300),
     "w5_affine_p3_biwfa_full": (5, 30, "affine.p3", False, 3, 3000, 300),
     "w1_affine_biwfa_score": (1, 100, "affine", True, 3, 0, 0),
+    # 100 kbp pairs at 10-15 % divergence: nine levels of breakpoints
+    "w3_affine_biwfa_full": (3, 2, "affine", False, 3, 0, 0),
+    # max_alignment_steps inside the breakpoint search and inside base cases
+    "w5_affine_biwfa_ms700": (5, 40, "affine", False, 3, 3000, 300, 700),
+    "w0_affine_biwfa_ms12": (0, 200, "affine", False, 3, 0, 0, 12),
+    "w1_affine_biwfa_ms300_score": (1, 100, "affine", True, 3, 0, 0, 300),
 }
 
 
@@ -96,16 +102,19 @@ def main():
     O.build(ref=True)
     W.build()
     synth = {}
-    for name, (wl, n, pset, so, mm, param, param2) in SYNTHETIC.items():
+    for name, spec in SYNTHETIC.items():
+        wl, n, pset, so, mm, param, param2 = spec[:7]
+        max_steps = spec[7] if len(spec) > 7 else 0
         m, mi, mm_, o1, e1, o2, e2 = PENALTY_SETS[pset][0], *PENALTY_SETS[pset][1:]
         pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
                           gap_opening2=o2, gap_extension2=e2)
         p = W.generate(wl, n, param=param, param2=param2)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-        r = O.align(b, pen, memory_mode=mm, score_only=so, kind="reference")
+        r = O.align(b, pen, memory_mode=mm, score_only=so, kind="reference", max_steps=max_steps)
         rows = [[int(r.score[i]), int(r.status[i]), crc(r.cigar(i))] for i in range(n)]
         synth[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
-                       "penalties": pset, "score_only": so, "memory_mode": mm, "rows": rows}
+                       "penalties": pset, "score_only": so, "memory_mode": mm,
+                       "max_steps": max_steps, "rows": rows}
         print(name, "done")
     with open(os.path.join(HERE, "synthetic_expected.json"), "w") as f:
         json.dump(synth, f, separators=(",", ":"))

@@ -46,8 +46,8 @@ def _split_key(key):
     raise KeyError(key)
 
 
-# ultralow keys are checked on score (BiWFA CIGARs differ on ties; the GPU
-# ultralow path is the unidirectional kernel)
+# test.biwfa.* keys run the BiWFA path (ultralow memory mode): its CIGARs
+# break ties differently from the unidirectional ones, as the reference's do
 @pytest.mark.parametrize("key", sorted(UT["expected"].keys()))
 def test_gpu_matches_reference_goldens(gpu_available, wfa, oracle_mod, key):
     W, O = wfa, oracle_mod
@@ -80,7 +80,8 @@ def test_gpu_matches_reference_on_synthetic(gpu_available, wfa, name):
     spec = UT["penalty_sets"][fx["penalties"]]
     p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
     batch = (p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-    scores, status, cig = run_batch(W, cfg_of(W, spec, fx["score_only"], fx["memory_mode"]), batch)
+    cfg = cfg_of(W, spec, fx["score_only"], fx["memory_mode"], fx.get("max_steps", 0))
+    scores, status, cig = run_batch(W, cfg, batch)
     for i, (score, st, c) in enumerate(fx["rows"]):
         assert int(scores[i]) == score and int(status[i]) == st, (name, i)
         if cig is not None:

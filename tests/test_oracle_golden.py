@@ -60,7 +60,8 @@ def test_oracle_matches_reference_on_synthetic(oracle_mod, wfa, name):
     pen = _pen(O, UT["penalty_sets"][fx["penalties"]])
     p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
     b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-    r = O.align(b, pen, memory_mode=fx["memory_mode"], score_only=fx["score_only"])
+    r = O.align(b, pen, memory_mode=fx["memory_mode"], score_only=fx["score_only"],
+                max_steps=fx.get("max_steps", 0))
     for i, (score, status, c) in enumerate(fx["rows"]):
         assert int(r.score[i]) == score and int(r.status[i]) == status, (name, i)
         assert helpers.crc(r.cigar(i)) == c, (name, i)

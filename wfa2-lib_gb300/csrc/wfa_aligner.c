@@ -314,10 +314,6 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   if (p->distance_metric != gap_affine && p->distance_metric != gap_affine_2p) return -1;
   if (wf->alignment_form.span != alignment_end2end || wf->alignment_form.extension) return -1;
   if (wf->heuristic.strategy != wf_heuristic_none) return -1;
-  /* BiWFA (ultralow) yields the same score but may break CIGAR ties
-   * differently (README.md of the reference); until the BiWFA kernel computes
-   * those CIGARs, only its score-only form is served. */
-  if (wf->memory_mode == wavefront_memory_ultralow && wf->alignment_scope != compute_score) return -1;
   cfg->metric = (int)p->distance_metric;
   cfg->match = p->match;
   cfg->x = p->mismatch;
@@ -327,6 +323,8 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   cfg->e2 = p->gap_extension2;
   cfg->score_only = (wf->alignment_scope == compute_score);
   cfg->max_steps = wf->system.max_alignment_steps > 0 ? wf->system.max_alignment_steps : INT_MAX;
+  /* ultralow memory mode is BiWFA (wavefront/wavefront_align.c:138-146) */
+  cfg->ultralow = (wf->memory_mode == wavefront_memory_ultralow);
   return 0;
 }
 

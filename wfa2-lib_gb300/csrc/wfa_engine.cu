@@ -23,94 +23,10 @@
 #include <cstring>
 #include <new>
 
-#include "wfa_engine.h"
-#include "wfa_kernels.cuh"
-
-// WF2G_ERR_* values of include/wfa2gpu.h
-#define WF2G_OK_ 0
-#define WF2G_ERR_NO_GPU_ -1
-#define WF2G_ERR_CONFIG_ -2
-#define WF2G_ERR_ARGS_ -3
-#define WF2G_ERR_CUDA_ -4
-#define WF2G_ERR_OOM_ -5
+#include "wfa_engine_impl.cuh"
 
 namespace wf2g {
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes);
-extern "C" int wf2g_seq_bytes(int enc, int max_len);
-}
-
-namespace {
-
-using namespace wf2g;
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-};
-
-int ensure(DevBuf& b, size_t bytes) {
-  if (bytes == 0) bytes = 16;
-  if (bytes <= b.cap) return 0;
-  if (b.p) cudaFree(b.p);
-  b.p = nullptr;
-  b.cap = 0;
-  const size_t want = bytes + bytes / 4;
-  if (cudaMalloc(&b.p, want) != cudaSuccess) {
-    cudaGetLastError();
-    return -1;
-  }
-  b.cap = want;
-  return 0;
-}
-
-struct Engine {
-  int device = -1;
-  int num_sms = 0;
-  size_t smem_optin = 0;
-  cudaStream_t stream = nullptr;
-  int64_t launches = 0;
-  // batch buffers (host-input path)
-  DevBuf seqs, poff, plen, toff, tlen, scores, status, ops, opsoff, opslen;
-  // control
-  DevBuf counters;  // [0] queue pass 1, [1] queue pass 2, [2] retry count
-  DevBuf retry;
-  DevBuf scratch1, scratch2;
-};
-
-
-int env_int(const char* name, int dflt) {
-  const char* v = getenv(name);
-  return (v && *v) ? atoi(v) : dflt;
-}
-
-
-Penalties make_pen(const wf2g_cfg_t& c) {
-  Penalties p;
-  p.match = c.match;
-  p.x = c.x;
-  p.o1 = c.o1;
-  p.e1 = c.e1;
-  p.o2 = c.metric == 4 ? c.o2 : 0;
-  p.e2 = c.metric == 4 ? c.e2 : 1;
-  // wavefront/wavefront_components.c:81-120: max_score_scope
-  int indel = c.o1 + c.e1;
-  if (c.metric == 4) indel = std::max(indel, c.o2 + c.e2);
-  p.R = std::max(indel, c.x) + 1;
-  p.RI1 = c.e1 + 1;
-  p.RI2 = c.metric == 4 ? c.e2 + 1 : 1;
-  return p;
-}
-
-// Upper bound of the alignment score, as the reference sizes its wavefront
-// table (wavefront/wavefront_components.c:101-108), for lengths <= max_len.
-int score_bound(const wf2g_cfg_t& c, int max_len) {
-  int64_t b = (int64_t)c.x * max_len + c.o1 + (int64_t)c.e1 * max_len;
-  if (c.metric == 4) b = std::max<int64_t>(b, (int64_t)c.x * max_len + c.o2 + (int64_t)c.e2 * max_len);
-  b += 8;
-  return (int)std::min<int64_t>(b, INT32_MAX / 4);
-}
-
-}  // namespace
+namespace eng {
 
 
 extern "C" int wf2g_engine_device(void) {
@@ -165,6 +81,7 @@ extern "C" void wf2g_engine_free(void* engine) {
                     &E->counters, &E->retry,  &E->scratch1, &E->scratch2};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
+  bi_state_free(E->bi);
   if (E->stream) cudaStreamDestroy(E->stream);
   delete E;
 }
@@ -232,11 +149,11 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   return 0;
 }
 
-static int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
-                        const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
-                        const int32_t* d_tlen, int max_len, int32_t* d_scores,
-                        int32_t* d_status, char* d_ops, const int64_t* d_opsoff,
-                        int32_t* d_opslen, cudaStream_t st) {
+int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
+                 const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
+                 const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
+                 char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
+                 const int8_t* d_ce, int score_cap, cudaStream_t st) {
   const bool cigar = !cfg.score_only;
   if (max_len < 1) max_len = 1;
   if (ensure(E->counters, 4 * sizeof(int32_t)) || ensure(E->retry, (size_t)n * sizeof(int32_t)))
@@ -253,6 +170,8 @@ static int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_s
   base.p_len = d_plen;
   base.t_off = d_toff;
   base.t_len = d_tlen;
+  base.comp_begin = d_cb;
+  base.comp_end = d_ce;
   base.retry_items = (int32_t*)E->retry.p;
   base.retry_count = counters + 2;
   base.scores = d_scores;
@@ -262,6 +181,7 @@ static int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_s
   base.ops_len = d_opslen;
   base.max_len = max_len;
   base.table_cap = score_bound(cfg, max_len) + 1;
+  if (score_cap > 0) base.table_cap = std::min(base.table_cap, score_cap + 1);
 
   // pass 1: every pair, 2-bit sequences, 1 MB of back-trace bytes per warp
   KParams k1 = base;
@@ -300,9 +220,12 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
   cudaSetDevice(E->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : E->stream;
 
+  if (cfg->ultralow)
+    return bialign_run(E, *cfg, n, on_device, seqs, p_off, p_len, t_off, t_len, scores, status,
+                       ops, ops_off, ops_len, st);
   if (on_device) {
     return plan_and_run(E, *cfg, n, seqs, p_off, p_len, t_off, t_len, max_len, scores, status,
-                        ops, ops_off, ops_len, st);
+                        ops, ops_off, ops_len, nullptr, nullptr, 0, st);
   }
   // ---- host path: stage inputs, run, copy results back
   int64_t seq_end = 0, ops_end = 0;
@@ -334,7 +257,7 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
                         (const int32_t*)E->tlen.p, mlen, (int32_t*)E->scores.p,
                         (int32_t*)E->status.p, cigar ? (char*)E->ops.p : nullptr,
                         cigar ? (const int64_t*)E->opsoff.p : nullptr,
-                        cigar ? (int32_t*)E->opslen.p : nullptr, st);
+                        cigar ? (int32_t*)E->opslen.p : nullptr, nullptr, nullptr, 0, st);
   if (rc) return rc;
   e = cudaMemcpyAsync(scores, E->scores.p, n4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(status, E->status.p, n4, cudaMemcpyDeviceToHost, st);
@@ -347,3 +270,6 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
   }
   return WF2G_OK_;
 }
+
+}  // namespace eng
+}  // namespace wf2g

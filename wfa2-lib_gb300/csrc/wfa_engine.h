@@ -20,6 +20,7 @@ typedef struct {
   int x, o1, e1, o2, e2;
   int score_only;
   int max_steps; /* INT32_MAX when unlimited */
+  int ultralow;  /* 1: BiWFA (wavefront_memory_ultralow) */
 } wf2g_cfg_t;
 
 /* Creates an engine on the current CUDA device; NULL (and *err set to a

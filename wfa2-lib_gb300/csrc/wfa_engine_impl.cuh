@@ -1,0 +1,124 @@
+// wfa_engine_impl.cuh -- host-side internals shared by the engine's
+// translation units (wfa_engine.cu: unidirectional batches; wfa_bialign_host.cu:
+// the BiWFA ultralow-memory path).  Not installed.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdint>
+#include <cstdlib>
+
+#include "wfa_engine.h"
+#include "wfa_kernels.cuh"
+
+// WF2G_ERR_* values of include/wfa2gpu.h
+#define WF2G_OK_ 0
+#define WF2G_ERR_NO_GPU_ -1
+#define WF2G_ERR_CONFIG_ -2
+#define WF2G_ERR_ARGS_ -3
+#define WF2G_ERR_CUDA_ -4
+#define WF2G_ERR_OOM_ -5
+
+namespace wf2g {
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes);
+extern "C" int wf2g_seq_bytes(int enc, int max_len);
+extern "C" void* wf2g_bi_kernel_ptr(int a2p);
+extern "C" void* wf2g_bi_pack_ptr(void);
+extern "C" void* wf2g_bi_gather_ptr(void);
+extern "C" size_t wf2g_bi_smem_bytes(int a2p, int scope);
+
+namespace eng {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+inline int ensure(DevBuf& b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes <= b.cap) return 0;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  const size_t want = bytes + bytes / 4;
+  if (cudaMalloc(&b.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  b.cap = want;
+  return 0;
+}
+
+inline void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+struct BiState;  // BiWFA buffers (wfa_bialign_host.cu)
+void bi_state_free(BiState* b);
+
+struct Engine {
+  int device = -1;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  // batch buffers (host-input path)
+  DevBuf seqs, poff, plen, toff, tlen, scores, status, ops, opsoff, opslen;
+  // control
+  DevBuf counters;  // [0] queue pass 1, [1] queue pass 2, [2] retry count
+  DevBuf retry;
+  DevBuf scratch1, scratch2;
+  BiState* bi = nullptr;
+};
+
+inline int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  return (v && *v) ? atoi(v) : dflt;
+}
+
+inline Penalties make_pen(const wf2g_cfg_t& c) {
+  Penalties p;
+  p.match = c.match;
+  p.x = c.x;
+  p.o1 = c.o1;
+  p.e1 = c.e1;
+  p.o2 = c.metric == 4 ? c.o2 : 0;
+  p.e2 = c.metric == 4 ? c.e2 : 1;
+  // wavefront/wavefront_components.c:81-120: max_score_scope
+  int indel = c.o1 + c.e1;
+  if (c.metric == 4) indel = std::max(indel, c.o2 + c.e2);
+  p.R = std::max(indel, c.x) + 1;
+  p.RI1 = c.e1 + 1;
+  p.RI2 = c.metric == 4 ? c.e2 + 1 : 1;
+  return p;
+}
+
+// Upper bound of the alignment score, as the reference sizes its wavefront
+// table (wavefront/wavefront_components.c:101-108), for lengths <= max_len.
+inline int score_bound(const wf2g_cfg_t& c, int max_len) {
+  int64_t b = (int64_t)c.x * max_len + c.o1 + (int64_t)c.e1 * max_len;
+  if (c.metric == 4) b = std::max<int64_t>(b, (int64_t)c.x * max_len + c.o2 + (int64_t)c.e2 * max_len);
+  b += 8;
+  return (int)std::min<int64_t>(b, INT32_MAX / 4);
+}
+
+// Unidirectional batch over device arrays (two passes; see wfa_engine.cu).
+// d_cb/d_ce: begin/end component per pair (nullptr: M).  score_cap > 0
+// replaces the score bound derived from max_len (back-trace table size).
+int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
+                 const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
+                 const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
+                 char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
+                 const int8_t* d_ce, int score_cap, cudaStream_t st);
+
+// BiWFA batch (wfa_bialign_host.cu); synchronises `st`.
+int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const char* seqs,
+                const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
+                const int32_t* t_len, int32_t* scores, int32_t* status, char* ops,
+                const int64_t* ops_off, int32_t* ops_len, cudaStream_t st);
+
+}  // namespace eng
+}  // namespace wf2g

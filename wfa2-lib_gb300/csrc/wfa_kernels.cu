@@ -254,8 +254,6 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
   __syncwarp();
 
   const int n_items = p.num_items_dev ? *p.num_items_dev : p.n_items;
-  const int rowI1 = pen.R, rowD1 = pen.R + pen.RI1;
-  const int rowI2 = pen.R + 2 * pen.RI1, rowD2 = rowI2 + pen.RI2;
 
   while (true) {
     int item = 0;
@@ -295,12 +293,22 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       continue;
     }
 
-    // ---- score 0: M[0][0] = 0 (wavefront/wavefront_aligner.c:236-253), slot 0,
-    // extended at once (every later M cell is extended as it is computed)
-    const int L0 = lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair);
+    // ---- score 0 (wavefront/wavefront_aligner.c:311-382): M[0][0] = 0, slot
+    // 0, extended at once (every later M cell is extended as it is computed);
+    // an alignment that begins in a gap component has offset 0 there and no M
+    const int cb = p.comp_begin ? p.comp_begin[pair] : 0;
+    const int ce = p.comp_end ? p.comp_end[pair] : 0;
+    const int rowI1 = pen.R, rowD1 = pen.R + pen.RI1;
+    const int rowI2 = pen.R + 2 * pen.RI1, rowD2 = rowI2 + pen.RI2;
+    // ring row of component c for the current slots (cur1: I1/D1, cur2: I2/D2)
+    auto comp_row = [&](int c, int cM, int c1, int c2) -> int {
+      return c == 0 ? cM : c == 1 ? rowI1 + c1 : c == 2 ? rowD1 + c1 : c == 3 ? rowI2 + c2 : rowD2 + c2;
+    };
+    const int L0 = cb == 0 ? lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair) : 0;
     if (lane == 0) {
-      RING_ST(row(0), 0, (OffT)L0);
-      meta[0] = make_int2(0, 0);
+      const int r0 = comp_row(cb, 0, 0, 0);
+      RING_ST(row(r0), 0, (OffT)L0);
+      meta[r0] = make_int2(0, 0);
       if (CIGAR) table[0] = make_int2(0, 0);
     }
     __syncwarp();
@@ -311,16 +319,26 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int64_t cursor = 0;  // choice bytes used
     int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable, 4 guard
     const int k_end = tlen - plen;
-    int mlo = 0, mhi = 0;  // trimmed limits of M[s]
-    bool m_exists = true;
+    int mlo = cb == 0 ? 0 : 1, mhi = 0;  // trimmed limits of M[s]
+    bool m_exists = (cb == 0);
 
     while (true) {
-      // ================= termination on the extended M[s]
-      // (wavefront/wavefront_termination.c:37-60)
+      // ================= termination on the extended M[s], or on the end
+      // component (wavefront/wavefront_termination.c:37-108); checked only
+      // where M[s] exists (wavefront/wavefront_extend.c:93-106)
       if (m_exists) {
-        if (mlo <= k_end && k_end <= mhi && RING_LD(row(curM), k_end) >= tlen) {
-          result = 1;
-          break;
+        if (ce == 0) {
+          if (mlo <= k_end && k_end <= mhi && RING_LD(row(curM), k_end) >= tlen) {
+            result = 1;
+            break;
+          }
+        } else {
+          const int re = comp_row(ce, curM, cur1, cur2);
+          const int2 em = meta[re];
+          if (em.x <= k_end && k_end <= em.y && RING_LD(row(re), k_end) >= tlen) {
+            result = 1;
+            break;
+          }
         }
       } else if (null_steps > pen.R) {
         result = 3;
@@ -607,7 +625,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int64_t n = 0;
     bool bad = false;
     {
-      int st = 0;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
+      int st = ce;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
       int ss = s, kk = k_end;
       while (true) {
         if (n + 2 > items_cap || ss < 0) { bad = true; break; }
@@ -615,9 +633,13 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           if (lane == 0 && CHK(n < items_cap, 33, n)) items[n] = 'E';
           ++n;
           if (ss == 0) {
-            bad = (kk != 0);
+            bad = (kk != 0) || (cb != 0);
             break;
           }
+        } else if (ss == 0) {
+          // the score-0 cell of an alignment that begins in a gap component
+          bad = (kk != 0) || (st != cb);
+          break;
         }
         if (!CHK(ss < p.table_cap, 34, ss)) { bad = true; break; }
         const int2 te = table[ss];

@@ -50,6 +50,10 @@ struct KParams {
   const int32_t* p_len;
   const int64_t* t_off;
   const int32_t* t_len;
+  // components the alignment of a pair begins and ends in (0 M, 1 I1, 2 D1,
+  // 3 I2, 4 D2; nullptr: M), for the BiWFA base cases
+  const int8_t* comp_begin;
+  const int8_t* comp_end;
   // work list: items[i] is a pair index (items == nullptr: identity)
   const int32_t* items;
   const int32_t* num_items_dev;  // if non-null, overrides n_items

@@ -79,6 +79,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
     return -3;  // WF2G_ERR_ARGS
   }
   if (cfg->metric != 3 && cfg->metric != 4) return -2;  // WF2G_ERR_CONFIG
+  if (cfg->ultralow) return -2;  // BiWFA allocates per recursion level
   const bool cigar = !cfg->score_only;
   if (cigar && (!d_ops || !d_opsoff || !d_opslen)) return -3;
   int err = 0;
