@@ -32,8 +32,23 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "wfa2-lib_gb300"))
 
 METRIC = "pairs/s bit-exact score+CIGAR, batched vs per-pair on 1 GB300; p50/p99 latency"
-INT_OPS_PER_CELL = 20      # gap-affine int32 ops per WFA cell
+INT_OPS_PER_CELL = {3: 20, 4: 32}  # int32 ops per WFA cell: gap-affine, gap-affine-2p
 INT_OPS_PER_EXT_WORD = 8   # per additional 32-base extend word
+MEM_HIGH, MEM_ULTRALOW = 0, 3
+
+# The benchmark configurations: workload of the seeded generator, pairs per
+# GPU, distance metric, memory mode, pairs of the per-pair drop-in sample and
+# first size of the CPU sample.
+CONFIGS = {
+    0: dict(workload=0, pairs=10_000, metric=3, memory=MEM_HIGH, per_pair=2000, cpu_n=1000,
+            name="100bp, 5% single-base edits"),
+    1: dict(workload=1, pairs=1_000_000, metric=3, memory=MEM_HIGH, per_pair=2000, cpu_n=1000,
+            name="500-1500bp, 0-15% divergence, 10% geometric indels"),
+    2: dict(workload=2, pairs=50_000, metric=4, memory=MEM_HIGH, per_pair=200, cpu_n=64,
+            name="1-10kbp log-uniform, 5% divergence, 20% long indels, affine2p (4,6,2,24,1)"),
+    3: dict(workload=3, pairs=1000, metric=3, memory=MEM_ULTRALOW, per_pair=4, cpu_n=16,
+            name="100kbp, 10-15% divergence, BiWFA (ultralow memory)"),
+}
 
 
 def parse():
@@ -42,14 +57,22 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--pairs", type=int, default=1_000_000, help="pairs per GPU")
-    ap.add_argument("--workload", type=int, default=1)
+    ap.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS),
+                    help="benchmark configuration (1: the headline batched workload)")
+    ap.add_argument("--pairs", type=int, default=0, help="pairs per GPU (0: the config's)")
     ap.add_argument("--score-only", action="store_true")
-    ap.add_argument("--per-pair-sample", type=int, default=2000)
+    ap.add_argument("--per-pair-sample", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="target wall time of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
-    return ap.parse_args()
+    a = ap.parse_args()
+    c = CONFIGS[a.config]
+    a.workload = c["workload"]
+    a.metric = c["metric"]
+    a.memory = c["memory"]
+    a.pairs = a.pairs or c["pairs"]
+    a.per_pair_sample = a.per_pair_sample or c["per_pair"]
+    return a
 
 
 def dist_env():
@@ -127,16 +150,17 @@ def gen_pinned(W, torch, workload, n, first):
     return W.Pairs(p.seqs, pin(p.p_off), pin(p.p_len), pin(p.t_off), pin(p.t_len))
 
 
-def cpu_sample(O, W, workload, score_only, target_s, first, kind):
+def cpu_sample(O, W, args, target_s, first, kind):
     """Times the CPU path on a bounded sample; returns (pairs/s, sample n, threads, res)."""
     threads = os.cpu_count() or 1
-    pen = O.Penalties()
-    n = 1000
+    pen = O.Penalties(metric=args.metric)
+    n = CONFIGS[args.config]["cpu_n"]
     while True:
-        p = W.generate(workload, n, first=first)
+        p = W.generate(args.workload, n, first=first)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
         t0 = time.perf_counter()
-        r = O.align(b, pen, score_only=score_only, kind=kind, nthreads=threads)
+        r = O.align(b, pen, memory_mode=args.memory, score_only=args.score_only, kind=kind,
+                    nthreads=threads)
         dt = time.perf_counter() - t0
         if dt >= target_s * 0.5 or n >= 200_000:
             return n / dt, n, threads, r, p, dt
@@ -154,10 +178,10 @@ def run_reference(args, rank):
     kind = "reference" if O.have_reference() else "port"
     vals = []
     for _ in range(args.warmup):
-        cpu_sample(O, W, args.workload, args.score_only, 1.0, 0, kind)
+        cpu_sample(O, W, args, 1.0, 0, kind)
     for _ in range(args.steps):
-        v, n, threads, _, _, dt = cpu_sample(O, W, args.workload, args.score_only,
-                                             args.cpu_seconds / max(args.steps, 1), 0, kind)
+        v, n, threads, _, _, dt = cpu_sample(O, W, args, args.cpu_seconds / max(args.steps, 1),
+                                             0, kind)
         vals.append(v)
     value = statistics.median(vals)
     line = {
@@ -175,14 +199,14 @@ def run_reference(args, rank):
 
 
 def workload_config(args):
-    names = {0: "100bp x 5 edits", 1: "500-1500bp, 0-15% divergence, 10% geometric indels",
-             2: "1-10kbp log-uniform, 5%, 20% long indels", 4: "lognormal 2kbp median, 1-20%"}
-    return {"workload": f"batched gap-affine(0,4,6,2) end-to-end "
-                        f"{'score-only' if args.score_only else 'full CIGAR'}, memory high, "
-                        f"{args.pairs} pairs/GPU of workload {args.workload} "
-                        f"({names.get(args.workload, '')})",
+    c = CONFIGS[args.config]
+    pen = "gap-affine-2p(0,4,6,2,24,1)" if args.metric == 4 else "gap-affine(0,4,6,2)"
+    mem = "ultralow (BiWFA)" if args.memory == MEM_ULTRALOW else "high"
+    return {"workload": f"config {args.config}: batched {pen} end-to-end "
+                        f"{'score-only' if args.score_only else 'full CIGAR'}, memory {mem}, "
+                        f"{args.pairs} pairs/GPU of workload {args.workload} ({c['name']})",
             "pairs_per_gpu": args.pairs, "seq": "uint8 ASCII ACGT",
-            "l2": "inputs (~2 GB/GPU) larger than L2; no flush needed",
+            "l2": "inputs larger than L2 (126 MB) at the default sizes; no flush needed",
             "parallelism": f"replicas x{args.gpus} (pairs sharded, no collective)"}
 
 
@@ -229,7 +253,7 @@ def main():
     d_opsoff = torch.from_numpy(ops_off).to(dev)
     d_opslen = torch.empty(n, dtype=torch.int32, device=dev)
 
-    cfg = W.Config(score_only=args.score_only)
+    cfg = W.Config(metric=args.metric, score_only=args.score_only, memory_mode=args.memory)
     al = W.Aligner(cfg)
     # a non-default stream: the C ABI maps a NULL stream to the aligner's own
     stream = torch.cuda.Stream(dev)
@@ -339,15 +363,14 @@ def main():
     assert np.array_equal(ps, d_scores[:k].cpu().numpy())
 
     # CPU baseline (bounded sample) and work units (WFA cells, extend chars)
-    cpu_v, cpu_n, cpu_threads, r, sp, _ = cpu_sample(O, W, args.workload, args.score_only,
-                                                     args.cpu_seconds, 0, "port")
+    cpu_v, cpu_n, cpu_threads, r, sp, _ = cpu_sample(O, W, args, args.cpu_seconds, 0, "port")
     # the bounded sample doubles as a parity spot-check of the timed results
     if rank == 0 and first == 0:
         m = min(cpu_n, n)
         assert np.array_equal(r.score[:m], d_scores[:m].cpu().numpy())
     cells_pp = float(r.cells.mean())
     ext_words_pp = float(np.ceil(r.ext / 32.0).mean())
-    ops_pp = INT_OPS_PER_CELL * cells_pp + INT_OPS_PER_EXT_WORD * ext_words_pp
+    ops_pp = INT_OPS_PER_CELL[args.metric] * cells_pp + INT_OPS_PER_EXT_WORD * ext_words_pp
     step_s = dev_s / args.steps
     sm_mhz = clk.get("sm_mhz") or 2070.0
     num_sms = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -369,7 +392,7 @@ def main():
         "roofline": {"bound": "int32", "achieved": achieved_tops, "peak": peak_tops,
                      "unit": "Tops/s", "frac": achieved_tops / peak_tops, "traffic": None,
                      "units_per_launch": {"wfa_cells": n * cells_pp,
-                                          "ops_per_cell": INT_OPS_PER_CELL,
+                                          "ops_per_cell": INT_OPS_PER_CELL[args.metric],
                                           "ext_words": n * ext_words_pp},
                      "peak_basis": f"{num_sms} SMs x 128 int32 lanes x {sm_mhz:.0f} MHz "
                                    "(median SM clock sampled during the run)",

@@ -632,9 +632,7 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
       int64_t* ext = out_ext ? &out_ext[i] : NULL;
       if (ultralow) {
         oracle_bialign(&p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i], &ws,
-                       &out_score[i], &out_status[i], ops, &out_ops_len[i]);
-        if (cells) *cells = 0;
-        if (ext) *ext = 0;
+                       &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext);
       } else {
         oracle_align_one(&ws, &p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i],
                   &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext);

@@ -43,6 +43,7 @@ typedef struct {
   char* ops;
   int nops;
   int score; /* cigar->score */
+  int64_t cells, ext; /* work counters: wavefront cells computed, bases matched */
 } bi_t;
 
 /* wavefront/wavefront_bialign.c:798-874 */
@@ -140,8 +141,8 @@ static void bp_overlap(const pen_t* p, oracle_ua_t* a0, oracle_ua_t* a1, int for
 /* wavefront/wavefront_bialign.c:975-1083.  Returns ST_OK, a stepper status
  * (ST_END_REACHED / ST_END_UNREACHABLE) or ST_MAX_STEPS; *reached_score gets
  * the score of the aligner that reached its end. */
-static int find_breakpoint(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce, bp_t* bp,
-                           int* reached_score) {
+static int find_breakpoint_(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce, bp_t* bp,
+                            int* reached_score) {
   const pen_t* p = b->p;
   const int plen = pe - pb, tlen = te - tb;
   oracle_ua_t* F = &b->F;
@@ -192,6 +193,14 @@ static int find_breakpoint(bi_t* b, int pb, int pe, int tb, int te, int cb, int 
   return ST_OK;
 }
 
+static int find_breakpoint(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce, bp_t* bp,
+                           int* reached_score) {
+  const int st = find_breakpoint_(b, pb, pe, tb, te, cb, ce, bp, reached_score);
+  b->cells += b->F.cells + b->R.cells;
+  b->ext += b->F.ext + b->R.ext;
+  return st;
+}
+
 /* wavefront/wavefront_bialign.c:159-194: regular WFA on the sub-problem with
  * the given boundary components, appended to the CIGAR. */
 static int bi_base(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce) {
@@ -203,6 +212,8 @@ static int bi_base(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce) {
     st = oracle_ua_extend(&U, NULL);
     if (st) break;
     oracle_ua_compute(&U);
+    b->cells += U.cells;
+    U.cells = 0;
     if (U.s >= p->max_steps) {
       /* wavefront/wavefront_unialign.c:102-107 sets the base CIGAR's score,
        * which wavefront_bialign_base copies before failing */
@@ -210,6 +221,7 @@ static int bi_base(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce) {
       return ST_UNATTAINABLE;
     }
   }
+  b->ext += U.ext;
   if (st != ST_END_REACHED) return ST_UNATTAINABLE;
   const int n = oracle_ua_backtrace(&U, b->ops + b->nops);
   if (n < 0) return ST_UNATTAINABLE;
@@ -259,7 +271,7 @@ static char* reversed(const char* s, int n) {
 
 void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int tlen,
                     oracle_ws_t* ws, int32_t* out_score, int32_t* out_status, char* ops,
-                    int32_t* ops_len) {
+                    int32_t* ops_len, int64_t* cells, int64_t* ext) {
   (void)ws;
   bi_t b;
   memset(&b, 0, sizeof(b));
@@ -304,6 +316,8 @@ void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int 
   if (st == ST_OK) *out_status = ST_COMPLETED;
   else if (st == ST_MAX_STEPS) *out_status = ST_MAX_STEPS;
   else *out_status = ST_UNATTAINABLE;
+  if (cells) *cells = b.cells;
+  if (ext) *ext = b.ext;
   oracle_ws_free(&b.wsf);
   oracle_ws_free(&b.wsr);
   oracle_ws_free(&b.wsb);

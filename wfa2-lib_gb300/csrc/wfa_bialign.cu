@@ -142,6 +142,41 @@ struct BiCtx {
     return L;
   }
 
+  // First 16-base window of an extension from (v,h), XORed (ACGT pairs).
+  __device__ __forceinline__ uint32_t first_window(int d, int v, int h) const {
+    if (d == 0) return win2(PW, pb + v + 16) ^ win2(TW, tb + h + 16);
+    return win2(PW, pe - v) ^ win2(TW, te - h);
+  }
+  // Equal characters at the start of a non-zero window XOR.
+  __device__ __forceinline__ int eq_count(int d, uint32_t x) const {
+    return d == 0 ? (__clz(x) >> 1) : ((__ffs(x) - 1) >> 1);
+  }
+  // lcp of ACGT pairs from L already-equal characters on.
+  __device__ int lcp_from(int d, int v, int h, int L, int lim) const {
+    if (d == 0) {
+      const int ps = pb + v + 16, ts = tb + h + 16;
+      while (L < lim) {
+        const uint32_t x = win2(PW, ps + L) ^ win2(TW, ts + L);
+        if (x) {
+          L += __clz(x) >> 1;
+          break;
+        }
+        L += 16;
+      }
+    } else {
+      const int ps = pe - v, ts = te - h;
+      while (L < lim) {
+        const uint32_t x = win2(PW, ps - L) ^ win2(TW, ts - L);
+        if (x) {
+          L += (__ffs(x) - 1) >> 1;
+          break;
+        }
+        L += 16;
+      }
+    }
+    return L < lim ? L : lim;
+  }
+
   // ------------------------------------------------------------ row upkeep
   __device__ void null_range(int32_t* r, int a, int b) const {
     for (int k = a + tid; k <= b; k += nt) r[k] = kNull;
@@ -273,42 +308,80 @@ struct BiCtx {
       th[c] = INT_MIN;
     }
     int mak = 0;
-    for (int k = lo + tid; k <= hi; k += nt) {
-      // wavefront/wavefront_compute_affine.c:66-84
-      const int32_t i1 = max(rMo1[k - 1], rI1[k - 1]) + 1;
-      const int32_t d1 = max(rMo1[k + 1], rD1[k + 1]);
-      const int32_t mis = rMx[k] + 1;
-      int32_t ins = i1, del = d1;
-      int32_t i2 = kNull, d2 = kNull;
-      if (A2P) {
-        // wavefront/wavefront_compute_affine2p.c:78-95
-        i2 = max(rMo2[k - 1], rI2[k - 1]) + 1;
-        d2 = max(rMo2[k + 1], rD2[k + 1]);
-        ins = max(i1, i2);
-        del = max(d1, d2);
+    // kU cells per thread per iteration: every input load of the group is
+    // issued before the first compute, and the first extend window of each
+    // M cell is fetched for the whole group before any is compared
+    constexpr int kU = 4;
+    for (int kb = lo + tid; kb <= hi; kb += kU * nt) {
+      int32_t bestv[kU], i1v[kU], d1v[kU], i2v[kU], d2v[kU];
+      bool live[kU];
+#pragma unroll
+      for (int j = 0; j < kU; ++j) {
+        const int k = kb + j * nt;
+        live[j] = k <= hi;
+        const int kk = live[j] ? k : lo;  // in-range stand-in for cells past hi
+        // wavefront/wavefront_compute_affine.c:66-84
+        const int32_t i1 = max(rMo1[kk - 1], rI1[kk - 1]) + 1;
+        const int32_t d1 = max(rMo1[kk + 1], rD1[kk + 1]);
+        const int32_t mis = rMx[kk] + 1;
+        int32_t ins = i1, del = d1;
+        int32_t i2 = kNull, d2 = kNull;
+        if (A2P) {
+          // wavefront/wavefront_compute_affine2p.c:78-95
+          i2 = max(rMo2[kk - 1], rI2[kk - 1]) + 1;
+          d2 = max(rMo2[kk + 1], rD2[kk + 1]);
+          ins = max(i1, i2);
+          del = max(d1, d2);
+        }
+        bestv[j] = max(del, max(mis, ins));
+        i1v[j] = i1;
+        d1v[j] = d1;
+        i2v[j] = i2;
+        d2v[j] = d2;
       }
-      const int32_t best = max(del, max(mis, ins));
-      // M out of bounds -> NULL; trims of wavefront/wavefront_compute.c:579-613
-      const bool okM = (uint32_t)best <= (uint32_t)tlen && (uint32_t)(best - k) <= (uint32_t)plen;
-      const bool okI1 = (uint32_t)i1 <= (uint32_t)tlen;
-      const bool okD1 = (uint32_t)(d1 - k) <= (uint32_t)plen;
-      int32_t mext = kNull;
-      if (okM) {
-        const int v = best - k;
-        mext = best + lcp(d, v, best, min(plen - v, tlen - best));
-        mak = max(mak, 2 * mext - k);
+      uint32_t xw[kU];
+      bool okm[kU];
+#pragma unroll
+      for (int j = 0; j < kU; ++j) {
+        const int k = kb + j * nt;
+        const int32_t best = bestv[j];
+        // M out of bounds -> NULL
+        okm[j] = live[j] && (uint32_t)best <= (uint32_t)tlen &&
+                 (uint32_t)(best - k) <= (uint32_t)plen;
+        xw[j] = enc2 ? first_window(d, okm[j] ? best - k : 0, okm[j] ? best : 0) : 0u;
       }
-      oM[k] = mext;
-      oI1[k] = i1;
-      oD1[k] = d1;
-      if (okM) { tl[0] = min(tl[0], k); th[0] = k; }
-      if (okI1) { tl[1] = min(tl[1], k); th[1] = k; }
-      if (okD1) { tl[2] = min(tl[2], k); th[2] = k; }
-      if (A2P) {
-        oI2[k] = i2;
-        oD2[k] = d2;
-        if ((uint32_t)i2 <= (uint32_t)tlen) { tl[NC - 2] = min(tl[NC - 2], k); th[NC - 2] = k; }
-        if ((uint32_t)(d2 - k) <= (uint32_t)plen) { tl[NC - 1] = min(tl[NC - 1], k); th[NC - 1] = k; }
+#pragma unroll
+      for (int j = 0; j < kU; ++j) {
+        if (!live[j]) continue;
+        const int k = kb + j * nt;
+        const int32_t best = bestv[j], i1 = i1v[j], d1 = d1v[j];
+        // trims of wavefront/wavefront_compute.c:579-613
+        const bool okI1 = (uint32_t)i1 <= (uint32_t)tlen;
+        const bool okD1 = (uint32_t)(d1 - k) <= (uint32_t)plen;
+        int32_t mext = kNull;
+        if (okm[j]) {
+          const int v = best - k;
+          const int lim = min(plen - v, tlen - best);
+          int L;
+          if (!enc2) L = lcp(d, v, best, lim);
+          else if (xw[j]) L = min(eq_count(d, xw[j]), lim);
+          else L = lim <= 16 ? lim : lcp_from(d, v, best, 16, lim);
+          mext = best + L;
+          mak = max(mak, 2 * mext - k);
+        }
+        oM[k] = mext;
+        oI1[k] = i1;
+        oD1[k] = d1;
+        if (okm[j]) { tl[0] = min(tl[0], k); th[0] = k; }
+        if (okI1) { tl[1] = min(tl[1], k); th[1] = k; }
+        if (okD1) { tl[2] = min(tl[2], k); th[2] = k; }
+        if (A2P) {
+          const int32_t i2 = i2v[j], d2 = d2v[j];
+          oI2[k] = i2;
+          oD2[k] = d2;
+          if ((uint32_t)i2 <= (uint32_t)tlen) { tl[NC - 2] = min(tl[NC - 2], k); th[NC - 2] = k; }
+          if ((uint32_t)(d2 - k) <= (uint32_t)plen) { tl[NC - 1] = min(tl[NC - 1], k); th[NC - 1] = k; }
+        }
       }
     }
     // block reductions: per-warp partials, then warp 0

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdint>
 #include <cstdio>
@@ -89,6 +90,15 @@ struct Ctx {
   const int64_t* d_toff;
   std::vector<int64_t> h_poff, h_toff;
   std::vector<int32_t> h_plen, h_tlen;
+  // WF2G_BI_VERBOSE=1: per-phase wall times on stderr
+  int verbose = 0;
+  std::chrono::steady_clock::time_point mark;
+  double ms_since_mark() {
+    const auto now = std::chrono::steady_clock::now();
+    const double ms = std::chrono::duration<double, std::milli>(now - mark).count();
+    mark = now;
+    return ms;
+  }
 };
 
 // One breakpoint launch over segs; fills outs (same order).
@@ -158,6 +168,9 @@ int run_breakpoints(Ctx& C, const std::vector<BiSeg>& segs, std::vector<BiOut>& 
   BI_CUDA(cudaMemcpyAsync(outs.data(), B->out.p, (size_t)nseg * sizeof(BiOut),
                           cudaMemcpyDeviceToHost, C.st));
   BI_CUDA(cudaStreamSynchronize(C.st));
+  if (C.verbose)
+    fprintf(stderr, "[wfa2gpu] breakpoints: %d segments (max %d x %d), %d CTAs x %d threads, %.3f ms\n",
+            nseg, maxP, maxT, ctas, nt, C.ms_since_mark());
   return 0;
 }
 
@@ -189,7 +202,9 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
   }
   BiState* B = E->bi;
   const bool cigar = !cfg.score_only;
-  Ctx C{E, B, cfg, st, n, nullptr, nullptr, nullptr, {}, {}, {}, {}};
+  Ctx C{E, B, cfg, st, n, nullptr, nullptr, nullptr, {}, {}, {}, {}, 0, {}};
+  C.verbose = env_int("WF2G_BI_VERBOSE", 0);
+  C.mark = std::chrono::steady_clock::now();
   C.h_poff.resize(n);
   C.h_toff.resize(n);
   C.h_plen.resize(n);
@@ -274,6 +289,10 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
   }
 
   std::vector<int32_t> r_score(n), r_status(n), r_len(n, 0);
+  if (C.verbose) {
+    BI_CUDA(cudaStreamSynchronize(st));
+    fprintf(stderr, "[wfa2gpu] BiWFA inputs + packing: %.3f ms\n", C.ms_since_mark());
+  }
 
   // ---- score only (wavefront/wavefront_bialign.c:1226-1263)
   if (!cigar) {
@@ -417,6 +436,7 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
       BI_CUDA(cudaMemcpyAsync(lstatus.data(), B->lstatus.p, l4, cudaMemcpyDeviceToHost, st));
       BI_CUDA(cudaMemcpyAsync(lopslen.data(), B->lopslen.p, l4, cudaMemcpyDeviceToHost, st));
       BI_CUDA(cudaStreamSynchronize(st));
+      if (C.verbose) fprintf(stderr, "[wfa2gpu] base cases: %d, %.3f ms\n", nl, C.ms_since_mark());
     }
 
     // ---- depth-first replay per pair: pieces, score, status
@@ -507,6 +527,10 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
   }
 
   // ---- per-pair results
+  if (C.verbose) {
+    BI_CUDA(cudaStreamSynchronize(st));
+    fprintf(stderr, "[wfa2gpu] assembly: %.3f ms\n", C.ms_since_mark());
+  }
   if (on_device) {
     BI_CUDA(cudaMemcpyAsync(scores, r_score.data(), n4, cudaMemcpyHostToDevice, st));
     BI_CUDA(cudaMemcpyAsync(status, r_status.data(), n4, cudaMemcpyHostToDevice, st));
