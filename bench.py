@@ -48,7 +48,11 @@ CONFIGS = {
             name="1-10kbp log-uniform, 5% divergence, 20% long indels, affine2p (4,6,2,24,1)"),
     3: dict(workload=3, pairs=1000, metric=3, memory=MEM_ULTRALOW, per_pair=4, cpu_n=16,
             name="100kbp, 10-15% divergence, BiWFA (ultralow memory)"),
+    4: dict(workload=4, pairs=50_000, metric=3, memory=MEM_HIGH, per_pair=0, cpu_n=200,
+            name="serving: Poisson arrivals at 200k pairs/s, lognormal length (median 2kbp, "
+                 "100bp-50kbp), 1-20% divergence, 80 GB budget, BiWFA fallback"),
 }
+SERVE_RATE = 200_000.0  # offered load of the serving configuration (pairs/s)
 
 
 def parse():
@@ -210,11 +214,131 @@ def workload_config(args):
             "parallelism": f"replicas x{args.gpus} (pairs sharded, no collective)"}
 
 
+def run_serving(args, rank, world, local):
+    """Config 4: the serving loop under open-loop Poisson arrivals.
+
+    One step = n requests submitted at their arrival times by a native
+    submitter thread (libwfa2bench.so) and polled until all have returned.
+    value = requests completed per second over the step; latency = submit to
+    result, per request.  The same pairs are also aligned offline in one
+    batch (wavefront_align_batch) for comparison, and every served result is
+    checked against the batch path in the memory mode the server used."""
+    import torch
+    import zlib
+    import wfa2gpu as W
+    from oracle import oracle as O
+    torch.cuda.set_device(local)
+    if not os.path.exists(W.LIB_PATH):
+        W.build()
+    n = args.pairs
+    first = rank * n
+    p = W.generate(args.workload, n, first=first)
+    rng = np.random.default_rng(1234 + rank)
+    arrivals = np.cumsum(rng.exponential(1e6 / SERVE_RATE, n)).astype(np.float64)
+    cfg = W.Config()
+    srv = W.Server(cfg, hbm_budget_bytes=80 << 30, lanes=2)
+    bl = C.CDLL(os.path.join(W.PKG_DIR, "lib", "libwfa2bench.so"))
+    P = C.c_void_p
+    bl.wf2g_bench_serve.restype = C.c_double
+    bl.wf2g_bench_serve.argtypes = [P, C.c_int64, C.c_int] + [P] * 11
+
+    def ptr(a):
+        return C.c_void_p(a.ctypes.data)
+    lat = np.zeros(n, np.float64)
+    st = np.zeros(n, np.int32)
+    sc = np.zeros(n, np.int32)
+    md = np.zeros(n, np.int32)
+    crc = np.zeros(n, np.uint32)
+    submitted = 0
+
+    def serve(m, arr):
+        nonlocal submitted
+        wall = bl.wf2g_bench_serve(C.c_void_p(srv._h), submitted, m, ptr(p.seqs), ptr(p.p_off),
+                                   ptr(p.p_len), ptr(p.t_off), ptr(p.t_len), ptr(arr), ptr(lat),
+                                   ptr(st), ptr(sc), ptr(md), ptr(crc))
+        submitted += m
+        if wall < 0:
+            raise RuntimeError(f"serving run failed ({wall})")
+        return wall
+    # warm-up: short runs at the same rate (engines size their buffers)
+    wm = min(n, 5000)
+    for _ in range(max(args.warmup, 3)):
+        serve(wm, np.ascontiguousarray(arrivals[:wm] - arrivals[0]))
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    l0 = srv.launches
+    walls, lats = [], []
+    for _ in range(args.steps):
+        walls.append(serve(n, arrivals))
+        lats.append(lat.copy())
+        assert (st == 0).all(), f"{int((st != 0).sum())} requests failed"
+    launches = srv.launches - l0
+    clk = clocks.stop()
+    srv.close()
+    wall = statistics.median(walls)
+    value = n / wall
+    L = np.concatenate(lats) / 1000.0
+    # offline batched form on the same pairs (host API, all pairs in one call)
+    al = W.Aligner(cfg)
+    al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    t0 = time.perf_counter()
+    rc, b_sc, b_st, ops, ops_len, ops_off = al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off,
+                                                          p.t_len)
+    t_batch = time.perf_counter() - t0
+    al.close()
+    # parity of the last step: high-mode results against the batch path, BiWFA
+    # re-runs against the ultralow batch path
+    hi = md == MEM_HIGH
+    b_crc = np.array([zlib.crc32(ops[ops_off[i]:ops_off[i] + ops_len[i]].tobytes())
+                      for i in range(n)], np.uint32)
+    assert np.array_equal(sc[hi], b_sc[hi]) and np.array_equal(crc[hi], b_crc[hi])
+    fb = np.nonzero(~hi)[0]
+    if len(fb):
+        ul = W.Aligner(W.Config(memory_mode=MEM_ULTRALOW))
+        sub = W.Pairs(p.seqs, np.ascontiguousarray(p.p_off[fb]), np.ascontiguousarray(p.p_len[fb]),
+                      np.ascontiguousarray(p.t_off[fb]), np.ascontiguousarray(p.t_len[fb]))
+        rc2, u_sc, u_st, uops, uol, uoo = ul.align_batch(sub.seqs, sub.p_off, sub.p_len,
+                                                         sub.t_off, sub.t_len)
+        ul.close()
+        u_crc = np.array([zlib.crc32(uops[uoo[j]:uoo[j] + uol[j]].tobytes())
+                          for j in range(len(fb))], np.uint32)
+        assert np.array_equal(sc[fb], u_sc) and np.array_equal(crc[fb], u_crc)
+    if rank != 0:
+        return
+    cpu_v, cpu_n, cpu_threads, _, _, _ = cpu_sample(O, W, args, args.cpu_seconds, 0, "port")
+    seq_bytes = int(np.sum(p.p_len) + np.sum(p.t_len))
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded SplitMix64 generator; seeded Poisson arrivals)",
+        "config": workload_config(args),
+        "serving": {"offered_rate": SERVE_RATE, "requests_per_step": n,
+                    "latency_ms": {"p50": float(np.percentile(L, 50)),
+                                   "p99": float(np.percentile(L, 99)),
+                                   "max": float(L.max())},
+                    "biwfa_fallback_pairs": int(len(fb)),
+                    "offline_batched_pairs_per_s": n / t_batch,
+                    "lanes": 2, "hbm_budget_gb": 80},
+        "roofline": None,
+        "cpu_baseline": {"value": cpu_v, "unit": "pairs/s", "cores": cpu_threads, "kind": "port",
+                         "sample": f"first {cpu_n} pairs of the workload, all host threads"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": seq_bytes,
+                "d2h_bytes_per_step": int(n * 8 + np.sum(ops_len))},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.config == 4:
+        run_serving(args, rank, world, local)
         return
     import torch
     import wfa2gpu as W

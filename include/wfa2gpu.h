@@ -428,7 +428,8 @@ int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const in
  * wavefront_align_batch_device(), and the work is queued on `cuda_stream`
  * (NULL: the legacy default stream).
  *
- * Limits: every pattern and text at most 2048 characters (max_sequence_length
+ * Limits: memory mode ultralow (BiWFA) is not served (WF2G_ERR_CONFIG); every
+ * pattern and text at most 2048 characters (max_sequence_length
  * above that is rejected with WF2G_ERR_ARGS and a message); a pair whose
  * back-trace needs more than 512 KiB of choice bytes reports WF_STATUS_OOM.
  * Concurrency is bounded by the array (tens of warps), so throughput is far
@@ -456,6 +457,60 @@ int64_t wavefront_aligner_gpu_launches(const wavefront_aligner_t* const wf_align
 /* CUDA device the library uses (the current device at wavefront_aligner_new()),
  * or -1 when no usable GPU is present. */
 int wfa2gpu_device(void);
+
+/* ------------------------------------------------------------------ serving
+ * Continuous batching of single-pair requests on one GPU (no counterpart in
+ * the reference, whose callers loop over wavefront_align()).  Requests are
+ * queued by wavefront_server_submit() from any thread; worker lanes admit
+ * what has arrived into batches within the device-memory budget and run them
+ * concurrently on the GPU; a pair whose back-trace exceeds the per-warp
+ * budget is re-run in BiWFA mode (wavefront_memory_ultralow), and its result
+ * says so.  Each result equals what wavefront_align() returns for that pair
+ * with the aligner's configuration (memory mode high) or, for BiWFA re-runs,
+ * with memory mode ultralow. */
+typedef struct wavefront_server_t wavefront_server_t;
+
+typedef struct {
+  int64_t hbm_budget_bytes; /* device memory the server may use; 0: 80 GiB */
+  int64_t backtrace_budget_bytes; /* back-trace bytes of one pair before it is
+                                     re-run in BiWFA mode; 0: 64 MiB */
+  int lanes;                /* batches in flight on the GPU; 0: 2 */
+  int max_batch_pairs;      /* pairs per batch; 0: 65536 */
+  int batch_window_us;      /* wait for more requests before a batch; <0: 200 */
+  int biwfa_min_length;     /* admission: pairs this long (pattern or text) are
+                               predicted over budget and aligned in BiWFA mode
+                               directly; 0: 8192, <0: never */
+} wavefront_server_attr_t;
+
+typedef struct {
+  int64_t id;             /* as returned by wavefront_server_submit() */
+  int status;             /* WF_STATUS_* */
+  int score;              /* cigar->score */
+  int memory_mode;        /* wavefront_memory_high, or _ultralow for BiWFA re-runs */
+  const char* operations; /* CIGAR operations (M/X/I/D), valid until the next poll */
+  int operations_length;
+  double latency_us;      /* submit to result */
+} wavefront_server_result_t;
+
+/* Server with the configuration of `wf_aligner` (end-to-end, heuristic none,
+ * memory mode high; score-only or full CIGAR).  NULL if that configuration is
+ * not served or no GPU is present. */
+wavefront_server_t* wavefront_server_new(const wavefront_aligner_t* const wf_aligner,
+                                         const wavefront_server_attr_t* const attributes);
+/* Queues one pair (copied); returns its id (>= 0) or a WF2G_ERR_* code. */
+int64_t wavefront_server_submit(wavefront_server_t* const server, const char* const pattern,
+                                const int pattern_length, const char* const text,
+                                const int text_length);
+/* Up to max_results finished results, waiting up to timeout_us for the first;
+ * returns their number (0 if none finished in time). */
+int wavefront_server_poll(wavefront_server_t* const server, wavefront_server_result_t* results,
+                          const int max_results, const int timeout_us);
+/* Requests submitted and not yet returned by wavefront_server_poll(). */
+int64_t wavefront_server_in_flight(wavefront_server_t* const server);
+/* Kernel launches issued by the server so far. */
+int64_t wavefront_server_gpu_launches(wavefront_server_t* const server);
+/* Finishes the queued work, stops the lanes and frees the server. */
+void wavefront_server_delete(wavefront_server_t* const server);
 
 #ifdef __cplusplus
 }

@@ -491,3 +491,47 @@ int64_t wavefront_aligner_gpu_launches(const wavefront_aligner_t* const wf_align
 }
 
 int wfa2gpu_device(void) { return wf2g_engine_device(); }
+
+/* ----------------------------------------------------------------- serving */
+wavefront_server_t* wavefront_server_new(const wavefront_aligner_t* const wf_aligner,
+                                         const wavefront_server_attr_t* const attributes) {
+  if (!wf_aligner) return NULL;
+  wf2g_cfg_t cfg;
+  if (make_cfg(wf_aligner, &cfg) != 0 || cfg.ultralow) {
+    fprintf(stderr, "[wfa2gpu] server: configuration not served (needs gap-affine or "
+                    "gap-affine-2p, end-to-end, heuristic none, memory mode high)\n");
+    return NULL;
+  }
+  wavefront_server_attr_t a = {0, 0, 0, 0, -1, 0};
+  if (attributes) a = *attributes;
+  int err = 0;
+  void* s = wf2g_server_new(&cfg, a.hbm_budget_bytes, a.backtrace_budget_bytes, a.lanes,
+                            a.max_batch_pairs, a.batch_window_us < 0 ? 200 : a.batch_window_us,
+                            a.biwfa_min_length == 0 ? 8192 : a.biwfa_min_length, &err);
+  return (wavefront_server_t*)s;
+}
+
+int64_t wavefront_server_submit(wavefront_server_t* const server, const char* const pattern,
+                                const int pattern_length, const char* const text,
+                                const int text_length) {
+  if (!server) return WF2G_ERR_ARGS;
+  return wf2g_server_submit(server, pattern, pattern_length, text, text_length);
+}
+
+int wavefront_server_poll(wavefront_server_t* const server, wavefront_server_result_t* results,
+                          const int max_results, const int timeout_us) {
+  if (!server) return WF2G_ERR_ARGS;
+  return wf2g_server_poll(server, results, max_results, timeout_us);
+}
+
+int64_t wavefront_server_in_flight(wavefront_server_t* const server) {
+  return server ? wf2g_server_in_flight(server) : 0;
+}
+
+int64_t wavefront_server_gpu_launches(wavefront_server_t* const server) {
+  return server ? wf2g_server_launches(server) : 0;
+}
+
+void wavefront_server_delete(wavefront_server_t* const server) {
+  if (server) wf2g_server_free(server);
+}

@@ -149,7 +149,9 @@ int run_breakpoints(Ctx& C, const std::vector<BiSeg>& segs, std::vector<BiOut>& 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, nt, smem);
   bps = std::max(1, bps);
   int ctas = std::min(nseg, bps * E->num_sms);
-  const int64_t budget = (int64_t)env_int("WF2G_BI_SCRATCH_GB", 32) << 30;
+  const int64_t budget = E->bi_scratch_budget >= 0
+                             ? E->bi_scratch_budget
+                             : (int64_t)env_int("WF2G_BI_SCRATCH_GB", 32) << 30;
   const int64_t cta_bytes = bp.rows_per_cta * 4;
   if ((int64_t)ctas * cta_bytes > budget) ctas = (int)std::max<int64_t>(1, budget / cta_bytes);
   if (ensure(B->rows, (size_t)ctas * cta_bytes) || ensure(B->segs, (size_t)nseg * sizeof(BiSeg)) ||

@@ -1,14 +1,15 @@
 // wfa_engine.cu -- host side of the GB300 wavefront aligner: device buffers,
 // pass planning and kernel launches behind the C interface of wfa_engine.h.
 //
-// A batch runs in two passes, both persistent kernels that pull pairs from a
-// device work queue (no host round trip between them):
-//   pass 1  every pair: 2-bit packed sequences, 1 MB of back-trace bytes per
-//           warp; pairs with non-ACGT bytes or a longer back-trace go to a
-//           retry list;
-//   pass 2  the retry list only: 8-bit sequences and a back-trace slice sized
-//           for any alignment of the batch; a remaining overflow is reported
-//           as WF_STATUS_OOM.
+// A batch runs in up to four passes, all persistent kernels that pull pairs
+// from a device work queue (no host round trip between them):
+//   pass 1    every pair: 2-bit packed sequences, 1 MB of back-trace bytes per
+//             warp; pairs with non-ACGT bytes or a longer back-trace go to a
+//             retry list;
+//   pass 2-4  the previous pass's retry list: 8-bit sequences and back-trace
+//             slices of 16 MB, 256 MB, then what any alignment of the batch
+//             may need, on ever fewer warps within the scratch budget; a
+//             remaining overflow is reported as WF_STATUS_OOM.
 // Each warp owns a global-memory slice holding its wavefront ring (every
 // diagonal the pair can reach, so rows never wrap) and back-trace bytes; the
 // slices stay L1/L2 resident.  On GB300 this measured 2x faster than a ring in
@@ -134,9 +135,19 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   const int need = (n_upper + wpc - 1) / wpc;
   int blocks = std::min(bps * E->num_sms, std::max(need, 1));
   // bound the scratch slices by the budget
-  const int64_t budget = (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
+  const int64_t budget =
+      E->scratch_budget >= 0 ? E->scratch_budget : (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
   if ((int64_t)blocks * wpc * kp.gscratch_per_warp > budget)
     blocks = std::max(1, (int)(budget / (wpc * kp.gscratch_per_warp)));
+  if ((int64_t)wpc * kp.gscratch_per_warp > budget && cigar) {
+    // even one block is over the budget: shrink its back-trace slices to fit;
+    // pairs whose back-trace needs more report WF_STATUS_OOM (final pass)
+    const int64_t fixed = (kp.ring_bytes + kp.seq_bytes + table_bytes + 255) & ~int64_t(255);
+    const int64_t bits = ((budget / wpc - fixed) & ~int64_t(255));
+    if (bits < (int64_t(1) << 20)) return WF2G_ERR_OOM_;
+    kp.bits_cap = bits;
+    kp.gscratch_per_warp = fixed + bits;
+  }
   if (ensure(scratch, (size_t)blocks * wpc * kp.gscratch_per_warp)) return WF2G_ERR_OOM_;
   kp.gscratch = (uint8_t*)scratch.p;
   void* args[] = {(void*)&kp};
@@ -156,10 +167,12 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  const int8_t* d_ce, int score_cap, cudaStream_t st) {
   const bool cigar = !cfg.score_only;
   if (max_len < 1) max_len = 1;
-  if (ensure(E->counters, 4 * sizeof(int32_t)) || ensure(E->retry, (size_t)n * sizeof(int32_t)))
+  // counters: [0..3] work queues of passes 1-4, [4..6] retry counts of passes 1-3
+  if (ensure(E->counters, 8 * sizeof(int32_t)) || ensure(E->retry, (size_t)3 * n * sizeof(int32_t)))
     return WF2G_ERR_OOM_;
   int32_t* counters = (int32_t*)E->counters.p;
-  if (cudaMemsetAsync(counters, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return WF2G_ERR_CUDA_;
+  int32_t* retry = (int32_t*)E->retry.p;
+  if (cudaMemsetAsync(counters, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return WF2G_ERR_CUDA_;
 
   KParams base;
   memset(&base, 0, sizeof(base));
@@ -172,8 +185,6 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   base.t_len = d_tlen;
   base.comp_begin = d_cb;
   base.comp_end = d_ce;
-  base.retry_items = (int32_t*)E->retry.p;
-  base.retry_count = counters + 2;
   base.scores = d_scores;
   base.status = d_status;
   base.ops = (uint8_t*)d_ops;
@@ -183,26 +194,47 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   base.table_cap = score_bound(cfg, max_len) + 1;
   if (score_cap > 0) base.table_cap = std::min(base.table_cap, score_cap + 1);
 
-  // pass 1: every pair, 2-bit sequences, 1 MB of back-trace bytes per warp
-  KParams k1 = base;
-  k1.items = nullptr;
-  k1.num_items_dev = nullptr;
-  k1.n_items = n;
-  k1.queue = counters + 0;
-  Pass p1{2, 0, int64_t(1) << 20, 8};
-  int rc = run_pass(E, cfg, k1, p1, n, E->scratch1, st);
+  // back-trace bytes one warp may need for any pair of the batch
+  int64_t need = 0;
+  if (cigar) need = (int64_t)base.table_cap * (2 * (int64_t)max_len + 1) + 4 * (int64_t)max_len + 64;
+  if (cigar && E->bits_cap > 0) need = std::min(need, E->bits_cap);
+
+  // pass 1: every pair, 2-bit sequences, 1 MB of back-trace bytes per warp;
+  // pairs with non-ACGT bytes or a longer back-trace go to the next pass
+  KParams k = base;
+  k.items = nullptr;
+  k.num_items_dev = nullptr;
+  k.n_items = n;
+  k.queue = counters + 0;
+  k.retry_items = retry;
+  k.retry_count = counters + 4;
+  Pass p{2, 0, int64_t(1) << 20, 8};
+  if (cigar) p.bits_cap = std::min(p.bits_cap, need);
+  int rc = run_pass(E, cfg, k, p, n, E->scratch1, st);
   if (rc) return rc;
-  // pass 2: the retry list (non-ACGT bytes, back-trace overflow), 8-bit
-  // sequences and a back-trace slice sized for any alignment of the batch
-  KParams k2 = base;
-  k2.items = (const int32_t*)E->retry.p;
-  k2.num_items_dev = counters + 2;
-  k2.n_items = 0;
-  k2.queue = counters + 1;
-  int64_t bits2 = 0;
-  if (cigar) bits2 = (int64_t)base.table_cap * (2 * (int64_t)max_len + 1) + 4 * (int64_t)max_len + 64;
-  Pass p2{8, 1, bits2, 2};
-  return run_pass(E, cfg, k2, p2, std::min(n, 2 * E->num_sms * 8), E->scratch2, st);
+  // passes 2-4 over the previous pass's overflow list: 8-bit sequences and
+  // ever larger back-trace slices on ever fewer warps (16 MB on up to 8
+  // blocks per SM, 256 MB on 2, then whatever one alignment of the batch may
+  // need); the last pass that covers `need` reports a remaining overflow as
+  // WF_STATUS_OOM
+  const int64_t slices[3] = {int64_t(16) << 20, int64_t(256) << 20, need};
+  const int per_sm[3] = {8, 2, 1};
+  for (int q = 0; q < 3; ++q) {
+    const int64_t bits = cigar ? std::min(need, slices[q]) : 0;
+    const bool final_pass = !cigar || bits >= need || q == 2;
+    k = base;
+    k.items = retry + (size_t)q * n;
+    k.num_items_dev = counters + 4 + q;
+    k.n_items = 0;
+    k.queue = counters + 1 + q;
+    k.retry_items = final_pass ? nullptr : retry + (size_t)(q + 1) * n;
+    k.retry_count = final_pass ? nullptr : counters + 5 + q;
+    Pass pq{8, final_pass ? 1 : 0, bits, per_sm[q]};
+    rc = run_pass(E, cfg, k, pq, std::min(n, per_sm[q] * E->num_sms * 8), E->scratch2, st);
+    if (rc) return rc;
+    if (final_pass) break;
+  }
+  return WF2G_OK_;
 }
 
 extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int on_device,

@@ -49,6 +49,16 @@ int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int num_pairs, const char* d_seqs,
                        char* d_ops, const int64_t* d_ops_off, int32_t* d_ops_len, void* stream);
 int wf2g_engine_device(void);
 
+/* Serving loop (wfa_server.cu); the result type is wavefront_server_result_t
+ * of include/wfa2gpu.h, passed as void* to keep this header self-contained. */
+void* wf2g_server_new(const wf2g_cfg_t* cfg, int64_t hbm_budget, int64_t backtrace_budget,
+                      int lanes, int max_batch, int window_us, int biwfa_min_length, int* err);
+int64_t wf2g_server_submit(void* srv, const char* pattern, int plen, const char* text, int tlen);
+int wf2g_server_poll(void* srv, void* results, int max, int timeout_us);
+int64_t wf2g_server_in_flight(void* srv);
+int64_t wf2g_server_launches(void* srv);
+void wf2g_server_free(void* srv);
+
 #ifdef __cplusplus
 }
 #endif

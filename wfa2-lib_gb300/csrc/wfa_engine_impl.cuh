@@ -72,6 +72,13 @@ struct Engine {
   DevBuf retry;
   DevBuf scratch1, scratch2;
   BiState* bi = nullptr;
+  // device-memory limits of this engine (bytes; < 0: the WF2G_SCRATCH_GB /
+  // WF2G_BI_SCRATCH_GB defaults) and the cap of back-trace bytes per warp in
+  // both passes (0: the first pass 1 MiB, the second sized for any alignment
+  // of the batch; a pair above the cap finishes with WF_STATUS_OOM)
+  int64_t scratch_budget = -1;
+  int64_t bi_scratch_budget = -1;
+  int64_t bits_cap = 0;
 };
 
 inline int env_int(const char* name, int dflt) {

@@ -624,11 +624,13 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     const int64_t items_cap = p.bits_cap - cursor;
     int64_t n = 0;
     bool bad = false;
+    bool items_full = false;  // walk items did not fit the back-trace slice
     {
       int st = ce;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
       int ss = s, kk = k_end;
       while (true) {
-        if (n + 2 > items_cap || ss < 0) { bad = true; break; }
+        if (n + 2 > items_cap) { items_full = true; break; }
+        if (ss < 0) { bad = true; break; }
         if (st == 0) {
           if (lane == 0 && CHK(n < items_cap, 33, n)) items[n] = 'E';
           ++n;
@@ -675,6 +677,21 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
     }
     __syncwarp();
+    if (items_full) {
+      // the same overflow as a full cell table: retry with a larger slice, or
+      // WF_STATUS_OOM in the final pass
+      if (lane == 0) {
+        if (!p.final_pass) {
+          p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
+        } else {
+          p.status[pair] = kStOOM;
+          p.scores[pair] = 0;
+          p.ops_len[pair] = 0;
+        }
+      }
+      __syncwarp();
+      continue;
+    }
     int out_n = 0;
     if (!bad) {
       uint8_t* const out = p.ops + p.ops_off[pair];

@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import time
 from dataclasses import dataclass
 
 import numpy as np
@@ -148,7 +149,24 @@ EXPORTED = [
     "cigar_print_pretty", "wavefront_align_batch", "wavefront_align_batch_device",
     "wavefront_aligner_gpu_launches", "wfa2gpu_device",
     "wavefront_align_batch_device_noalloc",
+    "wavefront_server_new", "wavefront_server_submit", "wavefront_server_poll",
+    "wavefront_server_in_flight", "wavefront_server_gpu_launches", "wavefront_server_delete",
 ]
+
+
+class ServerAttr(C.Structure):
+    """wavefront_server_attr_t"""
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("backtrace_budget_bytes", C.c_int64),
+                ("lanes", C.c_int),
+                ("max_batch_pairs", C.c_int), ("batch_window_us", C.c_int),
+                ("biwfa_min_length", C.c_int)]
+
+
+class ServerResult(C.Structure):
+    """wavefront_server_result_t"""
+    _fields_ = [("id", C.c_int64), ("status", C.c_int), ("score", C.c_int),
+                ("memory_mode", C.c_int), ("operations", C.c_void_p),
+                ("operations_length", C.c_int), ("latency_us", C.c_double)]
 
 
 def build() -> None:
@@ -199,6 +217,18 @@ def lib() -> C.CDLL:
     L.cigar_check_alignment.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int,
                                         C.POINTER(Cigar), C.c_bool]
     L.cigar_check_alignment.restype = C.c_bool
+    L.wavefront_server_new.argtypes = [C.POINTER(Aligner_t), C.POINTER(ServerAttr)]
+    L.wavefront_server_new.restype = C.c_void_p
+    L.wavefront_server_submit.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
+    L.wavefront_server_submit.restype = C.c_int64
+    L.wavefront_server_poll.argtypes = [C.c_void_p, C.POINTER(ServerResult), C.c_int, C.c_int]
+    L.wavefront_server_poll.restype = C.c_int
+    L.wavefront_server_in_flight.argtypes = [C.c_void_p]
+    L.wavefront_server_in_flight.restype = C.c_int64
+    L.wavefront_server_gpu_launches.argtypes = [C.c_void_p]
+    L.wavefront_server_gpu_launches.restype = C.c_int64
+    L.wavefront_server_delete.argtypes = [C.c_void_p]
+    L.wavefront_server_delete.restype = None
     _lib = L
     return L
 
@@ -353,6 +383,68 @@ def _genlib():
                                           C.c_void_p, C.c_void_p, C.c_void_p]
         _gen = g
     return _gen
+
+
+class Server:
+    """A ``wavefront_server_t``: continuous batching of single-pair requests."""
+
+    def __init__(self, cfg: Config | None = None, hbm_budget_bytes: int = 0, lanes: int = 0,
+                 max_batch_pairs: int = 0, batch_window_us: int = -1,
+                 backtrace_budget_bytes: int = 0, biwfa_min_length: int = 0):
+        self.cfg = cfg or Config()
+        self._al = Aligner(self.cfg)
+        attr = ServerAttr(hbm_budget_bytes, backtrace_budget_bytes, lanes, max_batch_pairs,
+                          batch_window_us, biwfa_min_length)
+        self._h = lib().wavefront_server_new(self._al._h, C.byref(attr))
+        if not self._h:
+            raise RuntimeError("wavefront_server_new failed")
+        self._res = (ServerResult * 4096)()
+
+    def submit(self, pattern: bytes, text: bytes) -> int:
+        rid = int(lib().wavefront_server_submit(self._h, pattern, len(pattern), text, len(text)))
+        if rid < 0:
+            raise RuntimeError(f"wavefront_server_submit failed: {rid}")
+        return rid
+
+    def poll(self, timeout_us: int = 1000):
+        """Finished results: list of (id, status, score, memory_mode, ops, latency_us)."""
+        k = lib().wavefront_server_poll(self._h, self._res, len(self._res), timeout_us)
+        out = []
+        for r in self._res[:max(k, 0)]:
+            ops = C.string_at(r.operations, r.operations_length).decode() if r.operations_length else ""
+            out.append((r.id, r.status, r.score, r.memory_mode, ops, r.latency_us))
+        return out
+
+    def wait_all(self, ids, timeout_s: float = 600.0):
+        """Polls until every id in `ids` has returned; {id: result tuple}."""
+        want = set(ids)
+        got = {}
+        t0 = time.time()
+        while want - got.keys():
+            for r in self.poll(10_000):
+                got[r[0]] = r
+            if time.time() - t0 > timeout_s:
+                raise TimeoutError(f"{len(want - got.keys())} requests still in flight")
+        return got
+
+    @property
+    def in_flight(self) -> int:
+        return int(lib().wavefront_server_in_flight(self._h))
+
+    @property
+    def launches(self) -> int:
+        return int(lib().wavefront_server_gpu_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().wavefront_server_delete(self._h)
+            self._h = None
+        if getattr(self, "_al", None):
+            self._al.close()
+            self._al = None
+
+    def __del__(self):
+        self.close()
 
 
 @dataclass
