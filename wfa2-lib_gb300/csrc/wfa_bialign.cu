@@ -35,8 +35,8 @@ constexpr int kBiMaxWarps = kBiMaxThreads / 32;
 constexpr int kRed = 11;  // per step: (trimmed lo, hi) x 5 components + max antidiagonal
 
 struct BiShared {
-  int red[kBiMaxWarps][kRed];
-  int res[2];  // termination flag, max antidiagonal
+  int red[2][kBiMaxWarps][kRed];  // per-warp partials, alternating per step
+  int res[2][2];  // per step parity: termination flag, max antidiagonal
   int found[3];
   int seg;
 };
@@ -61,6 +61,8 @@ struct BiCtx {
   int scope, stride, kofs, kmin, kmax;
   int ext_lo, ext_hi;  // diagonals NULL-initialised in every row of this CTA
   int jfound;
+  int rsel;      // which sh.res / sh.red buffer is written next (alternates)
+  bool one_bar;  // every input of a step lies >= 2 scores back
   // segment
   int plen, tlen, k_end;
   int enc2;
@@ -87,6 +89,11 @@ struct BiCtx {
     ext_lo = 1;
     ext_hi = 0;
     jfound = 0;
+    rsel = 0;
+    const Penalties& pen = p.pen;
+    int gap = min(pen.x, pen.e1);
+    if (A2P) gap = min(gap, pen.e2);
+    one_bar = gap >= 2;
   }
 
   __device__ __forceinline__ int32_t* row(int d, int c, int slot) const {
@@ -391,57 +398,64 @@ struct BiCtx {
       th[c] = __reduce_max_sync(kFull, th[c]);
     }
     mak = __reduce_max_sync(kFull, mak);
+    // partials of this step in buffer rsel: a warp reads them after the
+    // barrier below and writes the other buffer next step, and no warp can
+    // write this buffer again before every warp passed the next barrier
+    int (*red)[kRed] = sh.red[rsel];
     if (lane == 0) {
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        sh.red[warp][2 * c] = tl[c];
-        sh.red[warp][2 * c + 1] = th[c];
+        red[warp][2 * c] = tl[c];
+        red[warp][2 * c + 1] = th[c];
       }
-      sh.red[warp][2 * NC] = mak;
+      red[warp][2 * NC] = mak;
     }
     __syncthreads();
-    if (warp == 0) {
-      int v = 0;
-      if (lane <= 2 * NC) {
-        const bool is_lo = (lane < 2 * NC) && !(lane & 1);
-        v = sh.red[0][lane];
-        for (int w = 1; w < nwarps; ++w) {
-          const int x = sh.red[w][lane];
-          v = is_lo ? min(v, x) : max(v, x);
-        }
+    // every warp reduces the partials itself (the same values everywhere)
+    int v = 0;
+    if (lane <= 2 * NC) {
+      const bool is_lo = (lane < 2 * NC) && !(lane & 1);
+      v = red[0][lane];
+      for (int w = 1; w < nwarps; ++w) {
+        const int x = red[w][lane];
+        v = is_lo ? min(v, x) : max(v, x);
       }
-      int2 nm[NC];
+    }
+    rsel ^= 1;
+    int2 nm[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const int a = __shfl_sync(kFull, v, 2 * c);
+      const int b = __shfl_sync(kFull, v, 2 * c + 1);
+      nm[c] = a > b ? E : make_int2(a, b);
+    }
+    const int mk = __shfl_sync(kFull, v, 2 * NC);
+    // warp 0 NULLs the trimmed ends and publishes the limits; the next step
+    // reads neither when every input lies two or more scores back (one_bar),
+    // otherwise a second barrier orders them
+    if (warp == 0) {
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const int a = __shfl_sync(kFull, v, 2 * c);
-        const int b = __shfl_sync(kFull, v, 2 * c + 1);
         int32_t* const r = row(d, c, slot);
-        if (a > b) {
+        if (nm[c].x > nm[c].y) {
           null_range_warp(r, lo, hi);
-          nm[c] = E;
         } else {
-          null_range_warp(r, lo, a - 1);
-          null_range_warp(r, b + 1, hi);
-          nm[c] = make_int2(a, b);
+          null_range_warp(r, lo, nm[c].x - 1);
+          null_range_warp(r, nm[c].y + 1, hi);
         }
       }
-      const int mk = __shfl_sync(kFull, v, 2 * NC);
       if (lane == 0) {
 #pragma unroll
         for (int c = 0; c < NC; ++c) mt(d, c, slot) = nm[c];
-        // wavefront/wavefront_termination.c:37-108 on the end component
-        const int ec = endc[d];
-        const int2 em = nm[ec];
-        int flag = 0;
-        if (em.x <= k_end && k_end <= em.y && row(d, ec, slot)[k_end] >= tlen) flag = 1;
-        sh.res[0] = flag;
-        sh.res[1] = mk;
       }
     }
-    __syncthreads();
-    const int flag = sh.res[0];
-    mak_out = flag ? 0 : sh.res[1];
-    __syncthreads();  // sh.res is rewritten by the next step
+    // wavefront/wavefront_termination.c:37-108 on the end component
+    const int ec = endc[d];
+    const int2 em = nm[ec];
+    const int flag =
+        (em.x <= k_end && k_end <= em.y && row(d, ec, slot)[k_end] >= tlen) ? 1 : 0;
+    if (!one_bar) __syncthreads();
+    mak_out = flag ? 0 : mk;
     return flag;
   }
 
@@ -453,13 +467,13 @@ struct BiCtx {
     if (tid == 0) {
       const int L = lcp(d, 0, 0, min(plen, tlen));
       row(d, kCompM, 0)[0] = L;
-      sh.res[0] = (endc[d] == kCompM && k_end == 0 && L >= tlen) ? 1 : 0;
-      sh.res[1] = 2 * L;
+      sh.res[rsel][0] = (endc[d] == kCompM && k_end == 0 && L >= tlen) ? 1 : 0;
+      sh.res[rsel][1] = 2 * L;
     }
     __syncthreads();
-    const int flag = sh.res[0];
-    mak_out = flag ? 0 : sh.res[1];
-    __syncthreads();
+    const int flag = sh.res[rsel][0];
+    mak_out = flag ? 0 : sh.res[rsel][1];
+    rsel ^= 1;
     return flag;
   }
 
@@ -528,6 +542,7 @@ struct BiCtx {
 
   // wavefront/wavefront_bialign.c:878-956
   __device__ void overlap(int d0, bool forward, BP& bp) {
+    __syncthreads();  // the last step's trimmed ends and limits are in place
     const Penalties& pen = p.pen;
     const int score_0 = s[d0], score_1 = s[d0 ^ 1];
     if (score_0 == 0 && beg[d0] != kCompM) return;  // no M wavefront at score 0
@@ -587,6 +602,7 @@ struct BiCtx {
       search(res, guard);
     }
     if (tid == 0) p.out[seg] = res;
+    __syncthreads();  // the last step's trimmed ends and limits are in place
     // leave every row NULL for the next segment
     for (int d = 0; d < 2; ++d)
       for (int c = 0; c < NC; ++c)
@@ -672,8 +688,10 @@ struct BiCtx {
 
 }  // namespace
 
+// gap-affine fits 64 registers (two 512-thread CTAs per SM); affine2p keeps 128
 template <bool A2P>
-__global__ void __launch_bounds__(kBiMaxThreads) wfa_bi_breakpoint_kernel(const BiParams p) {
+__global__ void __launch_bounds__(kBiMaxThreads, A2P ? 1 : 2)
+    wfa_bi_breakpoint_kernel(const __grid_constant__ BiParams p) {
   extern __shared__ __align__(16) uint8_t smem[];
   BiShared& sh = *reinterpret_cast<BiShared*>(smem);
   int2* meta = reinterpret_cast<int2*>(smem + ((sizeof(BiShared) + 15) & ~size_t(15)));
@@ -691,8 +709,8 @@ __global__ void __launch_bounds__(kBiMaxThreads) wfa_bi_breakpoint_kernel(const 
   }
 }
 
-template __global__ void wfa_bi_breakpoint_kernel<false>(const BiParams p);
-template __global__ void wfa_bi_breakpoint_kernel<true>(const BiParams p);
+template __global__ void wfa_bi_breakpoint_kernel<false>(const __grid_constant__ BiParams p);
+template __global__ void wfa_bi_breakpoint_kernel<true>(const __grid_constant__ BiParams p);
 
 // 2-bit packing of every pair (one CTA per pair); enc2[pair] = 0 when a
 // sequence holds a byte outside {A,C,G,T} (those pairs compare bytes).
