@@ -39,11 +39,14 @@ class Penalties:
     gap_opening2: int = 24
     gap_extension2: int = 1
 
-    def cfg(self, memory_mode=MEM_HIGH, score_only=False, max_steps=0):
+    def cfg(self, memory_mode=MEM_HIGH, score_only=False, max_steps=0, wfadaptive=None):
+        """wfadaptive: None, or (min_wavefront_length, max_distance_threshold,
+        steps_between_cutoffs) of the wf-adaptive heuristic."""
+        h = [1, *wfadaptive] if wfadaptive else [0, 0, 0, 0]
         return np.array(
             [self.metric, self.match, self.mismatch, self.gap_opening1, self.gap_extension1,
              self.gap_opening2, self.gap_extension2, memory_mode, int(bool(score_only)),
-             max_steps], dtype=np.int32)
+             max_steps, *h], dtype=np.int32)
 
 
 def build(ref: bool = False) -> None:
@@ -136,10 +139,10 @@ class AlignResult:
 
 
 def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=False,
-          max_steps=0, kind="port", nthreads=0) -> AlignResult:
+          max_steps=0, kind="port", nthreads=0, wfadaptive=None) -> AlignResult:
     fn = _lib(kind)
     n = batch.n
-    cfg = pen.cfg(memory_mode, score_only, max_steps)
+    cfg = pen.cfg(memory_mode, score_only, max_steps, wfadaptive)
     score = np.zeros(n, np.int32)
     status = np.zeros(n, np.int32)
     ops_off = batch.ops_offsets()

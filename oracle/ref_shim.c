@@ -46,6 +46,12 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
   attr.memory_mode = (wavefront_memory_t)cfg[7];
   attr.alignment_scope = cfg[8] ? compute_score : compute_alignment;
   attr.heuristic.strategy = wf_heuristic_none;
+  if (cfg[10] == 1) {
+    attr.heuristic.strategy = wf_heuristic_wfadaptive;
+    attr.heuristic.min_wavefront_length = cfg[11];
+    attr.heuristic.max_distance_threshold = cfg[12];
+    attr.heuristic.steps_between_cutoffs = cfg[13];
+  }
   if (cfg[9] > 0) attr.system.max_alignment_steps = cfg[9];
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();

@@ -77,6 +77,11 @@ static int setup_penalties(const int* cfg, pen_t* p) {
   p->scope = imax(indel, p->x) + 1;
   p->score_only = cfg[8] != 0;
   p->max_steps = cfg[9] > 0 ? cfg[9] : INT_MAX;
+  /* wavefront/wavefront_heuristic.c:44-55 */
+  p->heur = cfg[10] == 1;
+  p->h_min_len = cfg[11];
+  p->h_max_dist = cfg[12];
+  p->h_steps = cfg[13];
   return 0;
 }
 
@@ -492,6 +497,8 @@ void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const cha
   ua->k_end = tlen - plen;
   ua->cells = 0;
   ua->ext = 0;
+  ua->heur = p->heur;
+  ua->steps_wait = p->h_steps;
   ws_reset(ws);
   ws_ensure_rows(ws, 0);
   if (ws->modular) memset(ws->rows, 0, (size_t)ws->scope * NCOMP * sizeof(orow_t));
@@ -507,6 +514,59 @@ void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const cha
   r0->exists = 1;
   r0->lo = r0->hi = r0->ilo = r0->ihi = 0;
   r0->off[0] = 0;
+}
+
+/* wf-adaptive cut-off of M[s] after its extension
+ * (wavefront/wavefront_heuristic.c:229-289, dispatcher :506-566).  Only the
+ * limits shrink: the cut offsets stay inside the initialised window, where
+ * later compute steps (wavefront/wavefront_compute.c:498-527 pads only beyond
+ * it) and the back-trace (wavefront/wavefront_backtrace.c:63-75) still read
+ * them.  I/D rows of the same score take the intersection of limits. */
+static void wfadaptive_cutoff(oracle_ua_t* ua) {
+  oracle_ws_t* ws = ua->ws;
+  const pen_t* p = ua->p;
+  orow_t* m = row_at(ws, ua->s, C_M);
+  if (!m->exists || m->lo > m->hi) return;
+  --ua->steps_wait;
+  if (ua->steps_wait > 0) return;
+  const int lo = m->lo, hi = m->hi;
+  if (hi - lo + 1 < p->h_min_len) return;
+  const int plen = ua->plen, tlen = ua->tlen;
+  int* dist = (int*)malloc((size_t)(hi - lo + 1) * sizeof(int));
+  int min_d = imax(plen, tlen);
+  for (int k = lo; k <= hi; ++k) {
+    const int32_t off = m->off[k];
+    const int d = off >= 0 ? imax(plen - (off - k), tlen - off) : -WF_NULL;
+    dist[k - lo] = d;
+    min_d = imin(min_d, d);
+  }
+  const int k_a = tlen - plen;
+  const int top = imin(k_a, hi);
+  int nlo = lo;
+  for (int k = lo; k < top; ++k) {
+    if (dist[k - lo] - min_d <= p->h_max_dist) break;
+    ++nlo;
+  }
+  const int bot = imax(k_a, nlo);
+  int nhi = hi;
+  for (int k = hi; k > bot; --k) {
+    if (dist[k - lo] - min_d <= p->h_max_dist) break;
+    --nhi;
+  }
+  free(dist);
+  ua->steps_wait = p->h_steps;
+  if (nlo == lo && nhi == hi) return;
+  m->lo = nlo;
+  m->hi = nhi;
+  if (nlo > nhi) m->null = 1;
+  const int ncomp = p->metric == 4 ? NCOMP : 3;
+  for (int c = 1; c < ncomp; ++c) {
+    orow_t* r = row_at(ws, ua->s, c);
+    if (!r->exists) continue;
+    if (nlo > r->lo) r->lo = nlo;
+    if (nhi < r->hi) r->hi = nhi;
+    if (r->lo > r->hi) r->null = 1;
+  }
 }
 
 /* Extends M[s] and tests termination on component ce
@@ -537,6 +597,8 @@ int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
   const int k_end = ua->k_end;
   if (e->exists && e->lo <= k_end && k_end <= e->hi && e->off[k_end] >= ua->tlen)
     return ST_END_REACHED;
+  /* wavefront/wavefront_extend.c:112-119 (wf-adaptive never drops) */
+  if (ua->heur) wfadaptive_cutoff(ua);
   if (max_ak) *max_ak = mak;
   return 0;
 }

@@ -29,8 +29,11 @@ extern "C" {
  *   cfg[7] memory mode       (0 high, 1 med, 2 low, 3 ultralow)
  *   cfg[8] score only        (1 = compute_score, 0 = compute_alignment)
  *   cfg[9] max alignment steps (<= 0 means unlimited)
+ *   cfg[10] heuristic        (0 none, 1 wf-adaptive)
+ *   cfg[11..13] wf-adaptive min_wavefront_length, max_distance_threshold,
+ *           steps_between_cutoffs (wavefront/wavefront_heuristic.h:42-69)
  */
-#define ORACLE_CFG_LEN 10
+#define ORACLE_CFG_LEN 14
 
 /* Align num_pairs pairs with nthreads host threads (OpenMP, one aligner per
  * thread, as tools/align_benchmark/align_benchmark.c:504-586 does).

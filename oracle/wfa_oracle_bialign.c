@@ -207,6 +207,7 @@ static int bi_base(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce) {
   const pen_t* p = b->p;
   oracle_ua_t U;
   oracle_ua_start(&U, &b->wsb, p, b->P + pb, pe - pb, b->T + tb, te - tb, cb, ce);
+  U.heur = 0; /* the base aligner's heuristic is none (wavefront/wavefront_bialigner.c:64-66) */
   int st;
   while (1) {
     st = oracle_ua_extend(&U, NULL);

@@ -26,6 +26,8 @@ typedef struct {
   int scope; /* max_score_scope */
   int score_only;
   int max_steps;
+  /* heuristic: 0 none, 1 wf-adaptive (wavefront/wavefront_heuristic.c:254-289) */
+  int heur, h_min_len, h_max_dist, h_steps;
 } pen_t;
 
 typedef struct {
@@ -70,6 +72,7 @@ typedef struct {
   int tlen;
   int cb, ce;
   int s, null_steps, k_end;
+  int heur, steps_wait; /* wf-adaptive cut-off state (wavefront_heuristic_clear) */
   int64_t cells, ext;
 } oracle_ua_t;
 

@@ -38,6 +38,14 @@ PENALTY_SETS = {
     "affine.p3": (3, -5, 1, 2, 1, 24, 1),
     "affine.p4": (3, -2, 3, 1, 4, 24, 1),
     "affine.p5": (3, -3, 5, 3, 2, 24, 1),
+    "affine.wfapt0": (3, 0, 4, 6, 2, 24, 1),
+    "affine.wfapt1": (3, 0, 4, 6, 2, 24, 1),
+}
+# wf-adaptive heuristic of a penalty set: (min_wavefront_length,
+# max_distance_threshold, steps_between_cutoffs); tests/wfa.utest.sh:61-63
+HEURISTICS = {
+    "affine.wfapt0": (10, 50, 1),
+    "affine.wfapt1": (10, 50, 10),
 }
 # file prefix -> (memory mode, score only); tests/wfa.utest.sh:35-40
 MODES = {
@@ -67,6 +75,11 @@ SYNTHETIC = {
     "w5_affine_biwfa_ms700": (5, 40, "affine", False, 3, 3000, 300, 700),
     "w0_affine_biwfa_ms12": (0, 200, "affine", False, 3, 0, 0, 12),
     "w1_affine_biwfa_ms300_score": (1, 100, "affine", True, 3, 0, 0, 300),
+    # the wf-adaptive heuristic (the reference's default attributes)
+    "w1_wfapt0_full": (1, 300, "affine.wfapt0", False, 0, 0, 0),
+    "w4_wfapt0_full": (4, 60, "affine.wfapt0", False, 0, 0, 0),
+    "w1_wfapt1_score": (1, 300, "affine.wfapt1", True, 0, 0, 0),
+    "w5_wfapt0_biwfa_full": (5, 40, "affine.wfapt0", False, 3, 3000, 300),
 }
 
 
@@ -94,8 +107,8 @@ def main():
                     rows.append([int(score), crc(cig)])
             expected[f"{mode_prefix}.{name}"] = rows
     with open(os.path.join(HERE, "utest_expected.json"), "w") as f:
-        json.dump({"penalty_sets": PENALTY_SETS, "modes": MODES, "expected": expected}, f,
-                  separators=(",", ":"))
+        json.dump({"penalty_sets": PENALTY_SETS, "heuristics": HEURISTICS, "modes": MODES,
+                   "expected": expected}, f, separators=(",", ":"))
 
     from oracle import oracle as O
     import wfa2gpu as W
@@ -110,7 +123,8 @@ def main():
                           gap_opening2=o2, gap_extension2=e2)
         p = W.generate(wl, n, param=param, param2=param2)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-        r = O.align(b, pen, memory_mode=mm, score_only=so, kind="reference", max_steps=max_steps)
+        r = O.align(b, pen, memory_mode=mm, score_only=so, kind="reference", max_steps=max_steps,
+                    wfadaptive=HEURISTICS.get(pset))
         rows = [[int(r.score[i]), int(r.status[i]), crc(r.cigar(i))] for i in range(n)]
         synth[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
                        "penalties": pset, "score_only": so, "memory_mode": mm,

@@ -34,7 +34,8 @@ def test_oracle_matches_reference_goldens(oracle_mod, key):
     pen = _pen(O, UT["penalty_sets"][name])
     pats, txts = helpers.utest_pairs()
     b = O.PairBatch.from_lists(pats, txts)
-    r = O.align(b, pen, memory_mode=mode, score_only=score_only)
+    r = O.align(b, pen, memory_mode=mode, score_only=score_only,
+                wfadaptive=UT.get("heuristics", {}).get(name))
     exp = UT["expected"][key]
     assert len(exp) == b.n
     bad = []
@@ -61,7 +62,8 @@ def test_oracle_matches_reference_on_synthetic(oracle_mod, wfa, name):
     p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
     b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
     r = O.align(b, pen, memory_mode=fx["memory_mode"], score_only=fx["score_only"],
-                max_steps=fx.get("max_steps", 0))
+                max_steps=fx.get("max_steps", 0),
+                wfadaptive=UT.get("heuristics", {}).get(fx["penalties"]))
     for i, (score, status, c) in enumerate(fx["rows"]):
         assert int(r.score[i]) == score and int(r.status[i]) == status, (name, i)
         assert helpers.crc(r.cigar(i)) == c, (name, i)
