@@ -12,11 +12,15 @@ UT = helpers.utest_expected()
 SY = helpers.synthetic_expected()
 
 
-def cfg_of(W, spec, score_only=False, memory_mode=0, max_steps=0):
+def cfg_of(W, spec, score_only=False, memory_mode=0, max_steps=0, wfadaptive=None):
     m, match, x, o1, e1, o2, e2 = spec
     return W.Config(metric=m, match=match, mismatch=x, gap_opening1=o1, gap_extension1=e1,
                     gap_opening2=o2, gap_extension2=e2, score_only=score_only,
-                    memory_mode=memory_mode, max_steps=max_steps)
+                    memory_mode=memory_mode, max_steps=max_steps,
+                    wfadaptive=tuple(wfadaptive) if wfadaptive else None)
+
+
+HEUR = UT.get("heuristics", {})
 
 
 def pen_of(O, spec):
@@ -56,7 +60,8 @@ def test_gpu_matches_reference_goldens(gpu_available, wfa, oracle_mod, key):
     spec = UT["penalty_sets"][name]
     pats, txts = helpers.utest_pairs()
     batch = helpers.pack(pats, txts)
-    scores, status, cig = run_batch(W, cfg_of(W, spec, score_only, mode), batch)
+    scores, status, cig = run_batch(W, cfg_of(W, spec, score_only, mode, 0, HEUR.get(name)),
+                                    batch)
     assert (status == 0).all()
     exp = UT["expected"][key]
     pen = pen_of(O, spec)
@@ -80,7 +85,8 @@ def test_gpu_matches_reference_on_synthetic(gpu_available, wfa, name):
     spec = UT["penalty_sets"][fx["penalties"]]
     p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
     batch = (p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-    cfg = cfg_of(W, spec, fx["score_only"], fx["memory_mode"], fx.get("max_steps", 0))
+    cfg = cfg_of(W, spec, fx["score_only"], fx["memory_mode"], fx.get("max_steps", 0),
+                 HEUR.get(fx["penalties"]))
     scores, status, cig = run_batch(W, cfg, batch)
     for i, (score, st, c) in enumerate(fx["rows"]):
         assert int(scores[i]) == score and int(status[i]) == st, (name, i)
@@ -181,11 +187,12 @@ def test_packed2bits_entry_point(gpu_available, wfa):
 
 
 def test_unsupported_configurations_fail_loudly(gpu_available, wfa):
-    """No silent CPU or heuristic fallback: out-of-scope forms return
-    WF_STATUS_UNATTAINABLE (per pair) / WF2G_ERR_CONFIG (batch)."""
+    """No silent CPU or heuristic fallback: out-of-scope forms (here the
+    x-drop heuristic) return WF_STATUS_UNATTAINABLE (per pair) /
+    WF2G_ERR_CONFIG (batch)."""
     W = wfa
     al = W.Aligner(W.Config())
-    W.lib().wavefront_aligner_set_heuristic_wfadaptive(al._h, 10, 50, 1)
+    W.lib().wavefront_aligner_set_heuristic_xdrop(al._h, 100, 1)
     st, _, _ = al.align(b"ACGT", b"ACGA")
     assert st == W.WF_STATUS_UNATTAINABLE
     seqs, po, pl, to, tl = helpers.pack([b"ACGT"], [b"ACGA"])

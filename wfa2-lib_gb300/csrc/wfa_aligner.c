@@ -313,7 +313,10 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   const wavefront_penalties_t* p = &wf->penalties;
   if (p->distance_metric != gap_affine && p->distance_metric != gap_affine_2p) return -1;
   if (wf->alignment_form.span != alignment_end2end || wf->alignment_form.extension) return -1;
-  if (wf->heuristic.strategy != wf_heuristic_none) return -1;
+  /* exact, or the wf-adaptive cut-off (wavefront/wavefront_heuristic.c:229-289);
+   * wfmash, drops and bands are not computed on the GPU */
+  const int wfadaptive = (wf->heuristic.strategy == wf_heuristic_wfadaptive);
+  if (wf->heuristic.strategy != wf_heuristic_none && !wfadaptive) return -1;
   cfg->metric = (int)p->distance_metric;
   cfg->match = p->match;
   cfg->x = p->mismatch;
@@ -325,6 +328,10 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   cfg->max_steps = wf->system.max_alignment_steps > 0 ? wf->system.max_alignment_steps : INT_MAX;
   /* ultralow memory mode is BiWFA (wavefront/wavefront_align.c:138-146) */
   cfg->ultralow = (wf->memory_mode == wavefront_memory_ultralow);
+  cfg->heur = wfadaptive;
+  cfg->h_min_len = wfadaptive ? wf->heuristic.min_wavefront_length : 0;
+  cfg->h_max_dist = wfadaptive ? wf->heuristic.max_distance_threshold : 0;
+  cfg->h_steps = wfadaptive ? wf->heuristic.steps_between_cutoffs : 0;
   return 0;
 }
 

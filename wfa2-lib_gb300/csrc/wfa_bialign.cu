@@ -72,6 +72,8 @@ struct BiCtx {
   const uint8_t* TB;
   int pb, pe, tb, te;
   int s[2], nulls[2], beg[2], endc[2];
+  int steps_wait[2];  // wf-adaptive state per direction
+  int2* imeta;        // initialised windows (rows are NULL outside them)
 
   __device__ BiCtx(const BiParams& p_, BiShared& sh_, int2* meta_)
       : p(p_), sh(sh_), meta(meta_) {
@@ -86,6 +88,7 @@ struct BiCtx {
     kmin = -kofs;
     kmax = stride - kofs - 1;
     rows = p.rows + (int64_t)blockIdx.x * p.rows_per_cta;
+    imeta = meta + 2 * NC * p.scope;
     ext_lo = 1;
     ext_hi = 0;
     jfound = 0;
@@ -102,8 +105,14 @@ struct BiCtx {
   __device__ __forceinline__ const int32_t* null_row() const {
     return rows + (int64_t)(2 * NC * scope) * stride + kofs;
   }
+  // limits (lo,hi) of row (d,c,slot); lo > hi: null
   __device__ __forceinline__ int2& mt(int d, int c, int slot) const {
     return meta[(d * NC + c) * scope + slot];
+  }
+  // initialised window of the row: equal to the limits except after a
+  // heuristic cut-off, which narrows only the limits
+  __device__ __forceinline__ int2& wm(int d, int c, int slot) const {
+    return imeta[(d * NC + c) * scope + slot];
   }
 
   // ------------------------------------------------------------ sequences
@@ -249,7 +258,7 @@ struct BiCtx {
     const bool vI2 = A2P && eI2.x <= eI2.y, vD2 = A2P && eD2.x <= eD2.y;
     int2 old[NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) old[c] = mt(d, c, slot);
+    for (int c = 0; c < NC; ++c) old[c] = wm(d, c, slot);
     s[d] = s1;
 
     // wavefront/wavefront_compute_affine.c:236-243: all inputs null
@@ -260,7 +269,7 @@ struct BiCtx {
       __syncthreads();
       if (tid == 0) {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) mt(d, c, slot) = E;
+        for (int c = 0; c < NC; ++c) mt(d, c, slot) = wm(d, c, slot) = E;
       }
       __syncthreads();
       mak_out = 0;
@@ -446,7 +455,7 @@ struct BiCtx {
       }
       if (lane == 0) {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) mt(d, c, slot) = nm[c];
+        for (int c = 0; c < NC; ++c) mt(d, c, slot) = wm(d, c, slot) = nm[c];
       }
     }
     // wavefront/wavefront_termination.c:37-108 on the end component
@@ -454,6 +463,7 @@ struct BiCtx {
     const int2 em = nm[ec];
     const int flag =
         (em.x <= k_end && k_end <= em.y && row(d, ec, slot)[k_end] >= tlen) ? 1 : 0;
+    if (p.heur && !flag) cutoff(d, slot, nm[kCompM]);
     if (!one_bar) __syncthreads();
     mak_out = flag ? 0 : mk;
     return flag;
@@ -474,7 +484,47 @@ struct BiCtx {
     const int flag = sh.res[rsel][0];
     mak_out = flag ? 0 : sh.res[rsel][1];
     rsel ^= 1;
+    if (p.heur && !flag) cutoff(d, 0, make_int2(0, 0));
     return flag;
+  }
+
+  // wf-adaptive cut-off of M at `slot` after its extension
+  // (wavefront/wavefront_heuristic.c:229-289, :506-566); block-uniform.  Only
+  // limits shrink (M, and the I/D rows of the score intersected with M).
+  __device__ void cutoff(int d, int slot, int2 mlim) {
+    if (mlim.x > mlim.y) return;  // empty M: no step counted
+    if (--steps_wait[d] > 0) return;
+    const int mlo = mlim.x, mhi = mlim.y;
+    if (mhi - mlo + 1 < p.h_min_len) return;
+    const int32_t* const mr = row(d, kCompM, slot);
+    auto dist = [&](int k) -> int {
+      const int32_t off = mr[k];
+      return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
+    };
+    int dm = max(plen, tlen);
+    for (int k = mlo + tid; k <= mhi; k += nt) dm = min(dm, dist(k));
+    dm = block_min(dm);
+    const int top = min(k_end, mhi);
+    int first = INT_MAX;
+    for (int k = mlo + tid; k < top; k += nt)
+      if (dist(k) - dm <= p.h_max_dist) { first = k; break; }
+    first = block_min(first);
+    const int nlo = first == INT_MAX ? max(mlo, top) : first;
+    const int bot = max(k_end, nlo);
+    int neg_last = INT_MAX;  // -(last qualifying k), for a block minimum
+    for (int k = mhi - tid; k > bot; k -= nt)
+      if (dist(k) - dm <= p.h_max_dist) { neg_last = -k; break; }
+    neg_last = block_min(neg_last);
+    const int nhi = neg_last == INT_MAX ? min(mhi, bot) : -neg_last;
+    steps_wait[d] = p.h_steps;
+    if (nlo == mlo && nhi == mhi) return;
+    if (tid == 0) {
+      mt(d, kCompM, slot) = make_int2(nlo, nhi);
+      for (int c = 1; c < NC; ++c) {
+        const int2 m = mt(d, c, slot);
+        mt(d, c, slot) = make_int2(max(m.x, nlo), min(m.y, nhi));
+      }
+    }
   }
 
   // ------------------------------------------------------------ overlap
@@ -584,6 +634,7 @@ struct BiCtx {
     endc[1] = sg.cb;
     s[0] = s[1] = 0;
     nulls[0] = nulls[1] = 0;
+    steps_wait[0] = steps_wait[1] = p.h_steps;  // wavefront_heuristic_clear at each init
     BiOut res;
     res.status = kBiGuard;
     res.reached = 0;
@@ -594,9 +645,9 @@ struct BiCtx {
     if (ensure_extent(-2, 2)) {
       if (tid == 0) {
         row(0, beg[0], 0)[0] = 0;
-        mt(0, beg[0], 0) = make_int2(0, 0);
+        mt(0, beg[0], 0) = wm(0, beg[0], 0) = make_int2(0, 0);
         row(1, beg[1], 0)[0] = 0;
-        mt(1, beg[1], 0) = make_int2(0, 0);
+        mt(1, beg[1], 0) = wm(1, beg[1], 0) = make_int2(0, 0);
       }
       __syncthreads();
       search(res, guard);
@@ -607,11 +658,11 @@ struct BiCtx {
     for (int d = 0; d < 2; ++d)
       for (int c = 0; c < NC; ++c)
         for (int sl = 0; sl < scope; ++sl) {
-          const int2 m = mt(d, c, sl);
+          const int2 m = wm(d, c, sl);
           if (m.x <= m.y) null_range(row(d, c, sl), m.x, m.y);
         }
     __syncthreads();
-    for (int i = tid; i < 2 * NC * scope; i += nt) meta[i] = make_int2(1, 0);
+    for (int i = tid; i < 4 * NC * scope; i += nt) meta[i] = make_int2(1, 0);
     __syncthreads();
   }
 
@@ -696,7 +747,7 @@ __global__ void __launch_bounds__(kBiMaxThreads, A2P ? 1 : 2)
   BiShared& sh = *reinterpret_cast<BiShared*>(smem);
   int2* meta = reinterpret_cast<int2*>(smem + ((sizeof(BiShared) + 15) & ~size_t(15)));
   BiCtx<A2P> c(p, sh, meta);
-  for (int i = c.tid; i < 2 * BiCtx<A2P>::NC * c.scope; i += c.nt) meta[i] = make_int2(1, 0);
+  for (int i = c.tid; i < 4 * BiCtx<A2P>::NC * c.scope; i += c.nt) meta[i] = make_int2(1, 0);
   if (c.tid < 3) sh.found[c.tid] = INT_MAX;
   __syncthreads();
   while (true) {
@@ -766,7 +817,8 @@ extern "C" void* wf2g_bi_pack_ptr(void) { return (void*)wfa_bi_pack_kernel; }
 extern "C" void* wf2g_bi_gather_ptr(void) { return (void*)wfa_bi_gather_kernel; }
 extern "C" size_t wf2g_bi_smem_bytes(int a2p, int scope) {
   const int nc = a2p ? 5 : 3;
-  return ((sizeof(BiShared) + 15) & ~size_t(15)) + (size_t)2 * nc * scope * sizeof(int2);
+  // limits and initialised windows of every row
+  return ((sizeof(BiShared) + 15) & ~size_t(15)) + (size_t)4 * nc * scope * sizeof(int2);
 }
 
 }  // namespace wf2g

@@ -38,6 +38,8 @@ struct BiParams {
   Penalties pen;  // x, o1, e1, o2, e2 as in the unidirectional kernel
   int scope;      // max_score_scope: ring depth of every component
   int max_steps;
+  // wf-adaptive heuristic of the forward/reverse searches (0: none)
+  int heur, h_min_len, h_max_dist, h_steps;
   // sequences: caller bytes, and the 2-bit packed copy of ACGT-only pairs
   const uint8_t* seqs;
   const int64_t* p_off;

@@ -126,6 +126,12 @@ int run_breakpoints(Ctx& C, const std::vector<BiSeg>& segs, std::vector<BiOut>& 
   bp.pen = pen;
   bp.scope = scope;
   bp.max_steps = C.cfg.max_steps;
+  // the forward/reverse searches inherit the heuristic
+  // (wavefront/wavefront_bialigner.c:48-56)
+  bp.heur = C.cfg.heur;
+  bp.h_min_len = C.cfg.h_min_len;
+  bp.h_max_dist = C.cfg.h_max_dist;
+  bp.h_steps = C.cfg.h_steps;
   bp.seqs = (const uint8_t*)C.d_seqs;
   bp.p_off = C.d_poff;
   bp.t_off = C.d_toff;
@@ -418,13 +424,16 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
       // of length <= 100 (wavefront/wavefront_bialign.c:1160-1164,1105-1107)
       const int cap = std::max(score_bound(cfg, kFallbackMinLength), kRecoveryMinScore + 64);
       const int bounds[3] = {1024, 30000, INT_MAX};
+      // the base aligner runs without heuristic (wavefront/wavefront_bialigner.c:64-66)
+      wf2g_cfg_t bcfg = cfg;
+      bcfg.heur = 0;
       int j0 = 0;
       for (int b = 0; b < 3 && j0 < nl; ++b) {
         int j1 = j0;
         while (j1 < nl && std::max(lplen[j1], ltlen[j1]) <= bounds[b]) ++j1;
         if (j1 == j0) continue;
         const int ml = std::max(lplen[j1 - 1], ltlen[j1 - 1]);
-        int rc = plan_and_run(E, cfg, j1 - j0, C.d_seqs, (const int64_t*)B->lpoff.p + j0,
+        int rc = plan_and_run(E, bcfg, j1 - j0, C.d_seqs, (const int64_t*)B->lpoff.p + j0,
                               (const int32_t*)B->lplen.p + j0, (const int64_t*)B->ltoff.p + j0,
                               (const int32_t*)B->ltlen.p + j0, ml,
                               (int32_t*)B->lscore.p + j0, (int32_t*)B->lstatus.p + j0,

@@ -67,8 +67,9 @@ extern "C" void* wf2g_engine_new(int* err) {
     for (int cig = 0; cig < 2; ++cig)
       for (int enc = 2; enc <= 8; enc += 6)
         for (int ob = 2; ob <= 4; ob += 2)
-          cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob),
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+          for (int h = 0; h < 2; ++h)
+            cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (err) *err = WF2G_OK_;
   return E;
 }
@@ -114,7 +115,8 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   const int64_t seq_bytes = wf2g_seq_bytes(ps.enc, base.max_len);
   kp.seq_in_smem = seq_bytes <= 48 * 1024;
   kp.seq_bytes = kp.seq_in_smem ? 0 : ((seq_bytes + 255) & ~int64_t(255));
-  kp.smem_per_warp = (int)((((kp.seq_in_smem ? seq_bytes : 0) + (int64_t)nrows * 8) + 15) & ~int64_t(15));
+  // staged sequences + per-row limits and initialised windows (2 x int2)
+  kp.smem_per_warp = (int)((((kp.seq_in_smem ? seq_bytes : 0) + (int64_t)nrows * 16) + 15) & ~int64_t(15));
   kp.bits_cap = cigar ? ps.bits_cap : 0;
   const int64_t table_bytes = cigar ? (int64_t)kp.table_cap * 8 : 0;
   kp.gscratch_per_warp = (kp.ring_bytes + kp.seq_bytes + table_bytes + kp.bits_cap + 255) & ~int64_t(255);
@@ -122,7 +124,7 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   int wpc = (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_warp, 1));
   wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
   const size_t smem = (size_t)kp.smem_per_warp * wpc;
-  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes);
+  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur);
   // shared memory holds only the staged sequences and row limits; give the
   // rest of the SM's unified storage to L1, which caches the wavefront rows
   const int want_blocks = std::max(1, 64 / wpc);
@@ -178,6 +180,10 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   memset(&base, 0, sizeof(base));
   base.pen = make_pen(cfg);
   base.max_steps = cfg.max_steps;
+  base.heur = cfg.heur;
+  base.h_min_len = cfg.h_min_len;
+  base.h_max_dist = cfg.h_max_dist;
+  base.h_steps = cfg.h_steps;
   base.seqs = (const uint8_t*)d_seqs;
   base.p_off = d_poff;
   base.p_len = d_plen;

@@ -21,6 +21,8 @@ typedef struct {
   int score_only;
   int max_steps; /* INT32_MAX when unlimited */
   int ultralow;  /* 1: BiWFA (wavefront_memory_ultralow) */
+  /* wf-adaptive heuristic (heur = 1) and its parameters; 0: exact */
+  int heur, h_min_len, h_max_dist, h_steps;
 } wf2g_cfg_t;
 
 /* Creates an engine on the current CUDA device; NULL (and *err set to a

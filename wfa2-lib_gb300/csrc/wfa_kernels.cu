@@ -202,7 +202,8 @@ __device__ __forceinline__ bool in_bounds(int32_t off, int k, int plen, int tlen
 #define WF2G_MIN_BLOCKS 4
 #endif
 
-template <bool A2P, bool CIGAR, int ENC, typename OffT>
+// HEUR: the wf-adaptive heuristic is compiled in (exact runs do without it)
+template <bool A2P, bool CIGAR, int ENC, typename OffT, bool HEUR>
 __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const KParams p) {
   typedef typename Seq<ENC>::Word Word;
   extern __shared__ __align__(16) uint8_t smem[];
@@ -230,7 +231,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     gs += p.seq_bytes;
   }
   Word* const T = P + nwords;
-  int2* const meta = reinterpret_cast<int2*>(ws);  // [nrows] trimmed (lo,hi); lo>hi == empty
+  int2* const meta = reinterpret_cast<int2*>(ws);  // [nrows] limits (lo,hi); lo>hi == null
+  // [nrows] initialised windows: a row is NULL outside its window.  The window
+  // equals the limits except after a heuristic cut-off, which narrows only the
+  // limits; the cut offsets stay readable, as wf_elements_init_min/max keep
+  // them in the reference (wavefront/wavefront_compute.c:498-527)
+  int2* const imeta = meta + nrows;
   int2* const table = CIGAR ? reinterpret_cast<int2*>(gs) : nullptr;
   uint8_t* const bits = CIGAR ? reinterpret_cast<uint8_t*>(table + p.table_cap) : nullptr;
   auto row = [=](int r) -> OffT* { return ring + (size_t)r * stride + kofs; };
@@ -250,7 +256,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
 
   // ring starts all-NULL, every row empty
   for (int64_t i = lane; i < (int64_t)(nrows + 1) * stride; i += 32) ring[i] = null_of<OffT>();
-  for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
+  for (int r = lane; r < nrows; r += 32) meta[r] = imeta[r] = make_int2(1, 0);
   __syncwarp();
 
   const int n_items = p.num_items_dev ? *p.num_items_dev : p.n_items;
@@ -267,11 +273,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
 
     // ---- reset the rows the previous pair left non-NULL
     for (int r = 0; r < nrows; ++r) {
-      const int2 mt = meta[r];
+      const int2 mt = imeta[r];
       if (mt.x <= mt.y) null_range(row(r), mt.x, mt.y, lane, rb, g_pair);
     }
     __syncwarp();
-    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
+    for (int r = lane; r < nrows; r += 32) meta[r] = imeta[r] = make_int2(1, 0);
 
     // ---- stage sequences
     bool ok = (plen <= p.max_len) && (tlen <= p.max_len);
@@ -308,7 +314,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     if (lane == 0) {
       const int r0 = comp_row(cb, 0, 0, 0);
       RING_ST(row(r0), 0, (OffT)L0);
-      meta[r0] = make_int2(0, 0);
+      meta[r0] = imeta[r0] = make_int2(0, 0);
       if (CIGAR) table[0] = make_int2(0, 0);
     }
     __syncwarp();
@@ -316,6 +322,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int s = 0;
     int curM = 0, cur1 = 0, cur2 = 0;  // ring slots of score s
     int null_steps = 0;
+    int steps_wait = p.h_steps;  // wf-adaptive (wavefront/wavefront_heuristic.c:114-121)
     int64_t cursor = 0;  // choice bytes used
     int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable, 4 guard
     const int k_end = tlen - plen;
@@ -343,6 +350,51 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       } else if (null_steps > pen.R) {
         result = 3;
         break;
+      }
+
+      // ================= wf-adaptive cut-off of the extended M[s]
+      // (wavefront/wavefront_heuristic.c:229-289, :506-566): only the limits
+      // of M[s] (and, intersected, of its I/D rows) shrink; the cut offsets
+      // stay in the rows' initialised windows
+      if (HEUR && m_exists && mlo <= mhi) {
+        --steps_wait;
+        if (steps_wait <= 0 && mhi - mlo + 1 >= p.h_min_len) {
+          const OffT* const mr = row(curM);
+          auto dist = [&](int k) -> int {
+            const int32_t off = RING_LD(mr, k);
+            return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
+          };
+          int dmin = max(plen, tlen);
+          for (int k = mlo + lane; k <= mhi; k += 32) dmin = min(dmin, dist(k));
+          dmin = __reduce_min_sync(kFull, dmin);
+          const int top = min(k_end, mhi);
+          int first = INT32_MAX;
+          for (int k = mlo + lane; k < top; k += 32)
+            if (dist(k) - dmin <= p.h_max_dist) { first = k; break; }
+          first = __reduce_min_sync(kFull, first);
+          const int nlo = first == INT32_MAX ? max(mlo, top) : first;
+          const int bot = max(k_end, nlo);
+          int last = INT32_MIN;
+          for (int k = mhi - lane; k > bot; k -= 32)
+            if (dist(k) - dmin <= p.h_max_dist) { last = k; break; }
+          last = __reduce_max_sync(kFull, last);
+          const int nhi = last == INT32_MIN ? min(mhi, bot) : last;
+          steps_wait = p.h_steps;
+          if (nlo != mlo || nhi != mhi) {
+            mlo = nlo;
+            mhi = nhi;
+            if (lane == 0) {
+              meta[curM] = make_int2(nlo, nhi);
+              const int nr = A2P ? 4 : 2;
+              for (int j = 0; j < nr; ++j) {
+                const int r = j == 0 ? rowI1 + cur1 : j == 1 ? rowD1 + cur1 : j == 2 ? rowI2 + cur2 : rowD2 + cur2;
+                const int2 m = meta[r];
+                meta[r] = make_int2(max(m.x, nlo), min(m.y, nhi));
+              }
+            }
+            __syncwarp();
+          }
+        }
       }
 
       // ================= compute score s+1
@@ -385,9 +437,10 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       OffT* const oD1 = row(rowD1 + cur1);
       OffT* const oI2 = A2P ? row(rowI2 + cur2) : nullptr;
       OffT* const oD2 = A2P ? row(rowD2 + cur2) : nullptr;
-      const int2 oldM = meta[curM], oldI1 = meta[rowI1 + cur1], oldD1 = meta[rowD1 + cur1];
-      const int2 oldI2 = A2P ? meta[rowI2 + cur2] : kEmpty;
-      const int2 oldD2 = A2P ? meta[rowD2 + cur2] : kEmpty;
+      // what a reused slot holds: its initialised window
+      const int2 oldM = imeta[curM], oldI1 = imeta[rowI1 + cur1], oldD1 = imeta[rowD1 + cur1];
+      const int2 oldI2 = A2P ? imeta[rowI2 + cur2] : kEmpty;
+      const int2 oldD2 = A2P ? imeta[rowD2 + cur2] : kEmpty;
 
       // wavefront/wavefront_compute_affine.c:236-243: all inputs null -> null step
       if (!(vMx | vMo1 | vI1 | vD1 | vMo2 | vI2 | vD2)) {
@@ -401,12 +454,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         }
         __syncwarp();
         if (lane == 0) {
-          meta[curM] = kEmpty;
-          meta[rowI1 + cur1] = kEmpty;
-          meta[rowD1 + cur1] = kEmpty;
+          meta[curM] = imeta[curM] = kEmpty;
+          meta[rowI1 + cur1] = imeta[rowI1 + cur1] = kEmpty;
+          meta[rowD1 + cur1] = imeta[rowD1 + cur1] = kEmpty;
           if (A2P) {
-            meta[rowI2 + cur2] = kEmpty;
-            meta[rowD2 + cur2] = kEmpty;
+            meta[rowI2 + cur2] = imeta[rowI2 + cur2] = kEmpty;
+            meta[rowD2 + cur2] = imeta[rowD2 + cur2] = kEmpty;
           }
         }
         if (CIGAR) {
@@ -458,6 +511,29 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       const OffT* const rMo2 = vMo2 ? row(sMo2) : null_row;
       const OffT* const rI2 = vI2 ? row(rowI2 + sI2) : null_row;
       const OffT* const rD2 = vD2 ? row(rowD2 + sI2) : null_row;
+      // The reference's back-trace reads an input within its initialised
+      // window even when the row is null (wavefront/wavefront_backtrace.c:
+      // 63-219), while the compute step reads the all-NULL row: the two
+      // differ only for an I/D row that a cut-off left with empty limits and
+      // a non-empty window.  Choice bytes then follow the back-trace.
+      auto window_row = [&](bool valid, int r, int score_back) -> const OffT* {
+        if (valid || score_back < 0) return nullptr;
+        const int2 w = imeta[r];
+        return w.x <= w.y ? row(r) : nullptr;
+      };
+      const OffT* wI1 = nullptr;
+      const OffT* wD1 = nullptr;
+      const OffT* wI2 = nullptr;
+      const OffT* wD2 = nullptr;
+      if (CIGAR && HEUR) {
+        wI1 = window_row(vI1, rowI1 + sI1, s - pen.e1);
+        wD1 = window_row(vD1, rowD1 + sI1, s - pen.e1);
+        if (A2P) {
+          wI2 = window_row(vI2, rowI2 + sI2, s - pen.e2);
+          wD2 = window_row(vD2, rowD2 + sI2, s - pen.e2);
+        }
+      }
+      const bool ghost = wI1 || wD1 || wI2 || wD2;
       uint8_t* const brow = CIGAR ? bits + cursor - lo : nullptr;
 
       int tloM = INT32_MAX, thiM = INT32_MIN;
@@ -542,6 +618,31 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
             c |= (uint8_t)(i2_e >= mo2_m) << 5;
             c |= (uint8_t)(d2_e >= mo2_p) << 6;
           }
+          if (HEUR && ghost) {
+            // back-trace candidates with the cut rows' window values
+            const int32_t wi1e = wI1 ? RING_LD(wI1, k - 1) : i1_e;
+            const int32_t wd1e = wD1 ? RING_LD(wD1, k + 1) : d1_e;
+            const int32_t wi1 = max(mo1_m, wi1e) + 1, wd1 = max(mo1_p, wd1e);
+            int32_t wi2 = kNull, wd2 = kNull, wi2e = i2_e, wd2e = d2_e;
+            if (A2P) {
+              wi2e = wI2 ? RING_LD(wI2, k - 1) : i2_e;
+              wd2e = wD2 ? RING_LD(wD2, k + 1) : d2_e;
+              wi2 = max(mo2_m, wi2e) + 1;
+              wd2 = max(mo2_p, wd2e);
+            }
+            const int32_t wbest = max(max(wd1, wd2), max(mis, max(wi1, wi2)));
+            if (mis == wbest) c = kSrcX;
+            else if (A2P && wd2 == wbest) c = kSrcD2;
+            else if (wd1 == wbest) c = kSrcD1;
+            else if (A2P && wi2 == wbest) c = kSrcI2;
+            else c = kSrcI1;
+            c |= (uint8_t)(wi1e >= mo1_m) << 3;
+            c |= (uint8_t)(wd1e >= mo1_p) << 4;
+            if (A2P) {
+              c |= (uint8_t)(wi2e >= mo2_m) << 5;
+              c |= (uint8_t)(wd2e >= mo2_p) << 6;
+            }
+          }
           if (CHK(cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
         }
       }
@@ -567,12 +668,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
       __syncwarp();
       if (lane == 0) {
-        meta[curM] = make_int2(tloM, thiM);
-        meta[rowI1 + cur1] = make_int2(tloI1, thiI1);
-        meta[rowD1 + cur1] = make_int2(tloD1, thiD1);
+        meta[curM] = imeta[curM] = make_int2(tloM, thiM);
+        meta[rowI1 + cur1] = imeta[rowI1 + cur1] = make_int2(tloI1, thiI1);
+        meta[rowD1 + cur1] = imeta[rowD1 + cur1] = make_int2(tloD1, thiD1);
         if (A2P) {
-          meta[rowI2 + cur2] = make_int2(tloI2, thiI2);
-          meta[rowD2 + cur2] = make_int2(tloD2, thiD2);
+          meta[rowI2 + cur2] = imeta[rowI2 + cur2] = make_int2(tloI2, thiI2);
+          meta[rowD2 + cur2] = imeta[rowD2 + cur2] = make_int2(tloD2, thiD2);
         }
         if (CIGAR && CHK(s < p.table_cap, 31, s)) table[s] = make_int2((int)cursor, lo);
       }
@@ -726,33 +827,37 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
 }
 
 // -------------------------------------------------------------- launchers
-#define WF2G_INST(A2P, CIG, ENC, T) \
-  template __global__ void wfa_align_kernel<A2P, CIG, ENC, T>(const KParams p);
-#define WF2G_INST_T(T)          \
-  WF2G_INST(false, false, 2, T) \
-  WF2G_INST(false, true, 2, T)  \
-  WF2G_INST(true, false, 2, T)  \
-  WF2G_INST(true, true, 2, T)   \
-  WF2G_INST(false, false, 8, T) \
-  WF2G_INST(false, true, 8, T)  \
-  WF2G_INST(true, false, 8, T)  \
-  WF2G_INST(true, true, 8, T)
-WF2G_INST_T(int16_t)
-WF2G_INST_T(int32_t)
+#define WF2G_INST(A2P, CIG, ENC, T, H) \
+  template __global__ void wfa_align_kernel<A2P, CIG, ENC, T, H>(const KParams p);
+#define WF2G_INST_T(T, H)          \
+  WF2G_INST(false, false, 2, T, H) \
+  WF2G_INST(false, true, 2, T, H)  \
+  WF2G_INST(true, false, 2, T, H)  \
+  WF2G_INST(true, true, 2, T, H)   \
+  WF2G_INST(false, false, 8, T, H) \
+  WF2G_INST(false, true, 8, T, H)  \
+  WF2G_INST(true, false, 8, T, H)  \
+  WF2G_INST(true, true, 8, T, H)
+WF2G_INST_T(int16_t, false)
+WF2G_INST_T(int32_t, false)
+WF2G_INST_T(int16_t, true)
+WF2G_INST_T(int32_t, true)
 
-template <typename T>
+template <typename T, bool H>
 static void* pick(int a2p, int cigar, int enc) {
   if (enc == 2) {
-    if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 2, T> : (void*)wfa_align_kernel<false, false, 2, T>;
-    return cigar ? (void*)wfa_align_kernel<true, true, 2, T> : (void*)wfa_align_kernel<true, false, 2, T>;
+    if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 2, T, H> : (void*)wfa_align_kernel<false, false, 2, T, H>;
+    return cigar ? (void*)wfa_align_kernel<true, true, 2, T, H> : (void*)wfa_align_kernel<true, false, 2, T, H>;
   }
-  if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 8, T> : (void*)wfa_align_kernel<false, false, 8, T>;
-  return cigar ? (void*)wfa_align_kernel<true, true, 8, T> : (void*)wfa_align_kernel<true, false, 8, T>;
+  if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 8, T, H> : (void*)wfa_align_kernel<false, false, 8, T, H>;
+  return cigar ? (void*)wfa_align_kernel<true, true, 8, T, H> : (void*)wfa_align_kernel<true, false, 8, T, H>;
 }
 
-// Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or 4-byte offsets).
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes) {
-  return off_bytes == 2 ? pick<int16_t>(a2p, cigar, enc) : pick<int32_t>(a2p, cigar, enc);
+// Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or
+// 4-byte offsets, wf-adaptive heuristic?).
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur) {
+  if (heur) return off_bytes == 2 ? pick<int16_t, true>(a2p, cigar, enc) : pick<int32_t, true>(a2p, cigar, enc);
+  return off_bytes == 2 ? pick<int16_t, false>(a2p, cigar, enc) : pick<int32_t, false>(a2p, cigar, enc);
 }
 
 // First bounds violation seen by a checked build: {site, index, pair, count}.

@@ -44,6 +44,9 @@ struct Penalties {
 struct KParams {
   Penalties pen;
   int max_steps;
+  // wf-adaptive heuristic (0: none); min wavefront length, max distance
+  // threshold, steps between cut-offs (wavefront/wavefront_heuristic.h:42-69)
+  int heur, h_min_len, h_max_dist, h_steps;
   // inputs
   const uint8_t* seqs;
   const int64_t* p_off;

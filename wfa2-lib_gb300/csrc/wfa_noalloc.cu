@@ -21,7 +21,7 @@
 #include "wfa_kernels.cuh"
 
 namespace wf2g {
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes);
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 }  // namespace wf2g
 
@@ -109,6 +109,10 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   if (cfg->metric == 4) bound = std::max<int64_t>(bound, (int64_t)cfg->x * L + cfg->o2 + (int64_t)cfg->e2 * L);
   kp.table_cap = (int)(bound + 9);
   kp.max_steps = cfg->max_steps;
+  kp.heur = cfg->heur;
+  kp.h_min_len = cfg->h_min_len;
+  kp.h_max_dist = cfg->h_max_dist;
+  kp.h_steps = cfg->h_steps;
   kp.seqs = (const uint8_t*)d_seqs;
   kp.p_off = d_poff;
   kp.p_len = d_plen;
@@ -127,7 +131,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.ring_bytes = (((int64_t)(nrows + 1) * kp.row_stride * 2) + 255) & ~int64_t(255);
   const int seq_bytes = wf2g_seq_bytes(8, L);
   kp.seq_in_smem = 1;
-  kp.smem_per_warp = (int)(((int64_t)seq_bytes + (int64_t)nrows * 8 + 15) & ~int64_t(15));
+  kp.smem_per_warp = (int)(((int64_t)seq_bytes + (int64_t)nrows * 16 + 15) & ~int64_t(15));
   kp.bits_cap = cigar ? kNoAllocBitsPerWarp : 0;
   kp.gscratch_per_warp =
       (kp.ring_bytes + (cigar ? (int64_t)kp.table_cap * 8 + kp.bits_cap : 0) + 255) & ~int64_t(255);
@@ -152,7 +156,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.gscratch = base + 256;
   // calls share the array: clear the queue head left by the previous call
   if (cudaMemsetAsync(queue, 0, sizeof(int32_t), st) != cudaSuccess) return -4;
-  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2);
+  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur);
   void* args[] = {(void*)&kp};
   const cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args,
                                          (size_t)kp.smem_per_warp * wpc, st);

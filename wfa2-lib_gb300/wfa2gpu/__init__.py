@@ -31,6 +31,7 @@ INDEL, EDIT, GAP_LINEAR, GAP_AFFINE, GAP_AFFINE_2P = 0, 1, 2, 3, 4
 COMPUTE_SCORE, COMPUTE_ALIGNMENT = 0, 1
 MEM_HIGH, MEM_MED, MEM_LOW, MEM_ULTRALOW = 0, 1, 2, 3
 WF_HEURISTIC_NONE = 0
+WF_HEURISTIC_WFADAPTIVE = 0x4
 
 
 # ------------------------------------------------------------ ABI mirror
@@ -255,6 +256,9 @@ class Config:
     score_only: bool = False
     memory_mode: int = MEM_HIGH
     max_steps: int = 0
+    # wf-adaptive heuristic: (min_wavefront_length, max_distance_threshold,
+    # steps_between_cutoffs), or None for exact alignment
+    wfadaptive: tuple | None = None
 
     def attributes(self) -> AlignerAttr:
         a = default_attributes()
@@ -271,6 +275,10 @@ class Config:
         a.affine2p_penalties.gap_opening2 = self.gap_opening2
         a.affine2p_penalties.gap_extension2 = self.gap_extension2
         a.heuristic.strategy = WF_HEURISTIC_NONE
+        if self.wfadaptive:
+            a.heuristic.strategy = WF_HEURISTIC_WFADAPTIVE
+            (a.heuristic.min_wavefront_length, a.heuristic.max_distance_threshold,
+             a.heuristic.steps_between_cutoffs) = self.wfadaptive
         a.memory_mode = self.memory_mode
         if self.max_steps > 0:
             a.system.max_alignment_steps = self.max_steps
