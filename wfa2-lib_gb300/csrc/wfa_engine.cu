@@ -6,10 +6,14 @@
 //   pass 1    every pair: 2-bit packed sequences, 1 MB of back-trace bytes per
 //             warp; pairs with non-ACGT bytes or a longer back-trace go to a
 //             retry list;
-//   pass 2-4  the previous pass's retry list: 8-bit sequences and back-trace
-//             slices of 16 MB, 256 MB, then what any alignment of the batch
-//             may need, on ever fewer warps within the scratch budget; a
-//             remaining overflow is reported as WF_STATUS_OOM.
+//   pass 2    the retry list: 8-bit sequences, choice bytes in a shared block
+//             pool (each pair takes blocks as its back-trace grows and
+//             returns them when done), as many warps as the pool can feed;
+//             a pair that finds the pool empty goes to the next list;
+//   pass 3    the same with fewer warps;
+//   pass 4    what is left, pooled, with few enough warps that all can hold
+//             their pair's back-trace at once; a remaining overflow is
+//             reported as WF_STATUS_OOM.
 // Each warp owns a global-memory slice holding its wavefront ring (every
 // diagonal the pair can reach, so rows never wrap) and back-trace bytes; the
 // slices stay L1/L2 resident.  On GB300 this measured 2x faster than a ring in
@@ -80,7 +84,8 @@ extern "C" void wf2g_engine_free(void* engine) {
   cudaSetDevice(E->device);
   DevBuf* bufs[] = {&E->seqs,   &E->poff,     &E->plen,  &E->toff,     &E->tlen,
                     &E->scores, &E->status,   &E->ops,   &E->opsoff,   &E->opslen,
-                    &E->counters, &E->retry,  &E->scratch1, &E->scratch2};
+                    &E->counters, &E->retry,  &E->scratch1, &E->scratch2,
+                    &E->pool,   &E->poolctl};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   bi_state_free(E->bi);
@@ -96,8 +101,9 @@ extern "C" int64_t wf2g_engine_launches(const void* engine) {
 struct Pass {
   int enc;          // 2 or 8 bits per staged base
   int final_pass;   // 1: overflow -> WF_STATUS_OOM
-  int64_t bits_cap; // back-trace bytes per warp (full CIGAR)
+  int64_t bits_cap; // back-trace bytes per warp (full CIGAR); pooled: block list + walk items
   int max_blocks_per_sm;
+  int pooled;       // choice bytes in the block pool (base.pool)
 };
 
 static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const Pass& ps,
@@ -118,12 +124,13 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   // staged sequences + per-row limits and initialised windows (2 x int2)
   kp.smem_per_warp = (int)((((kp.seq_in_smem ? seq_bytes : 0) + (int64_t)nrows * 16) + 15) & ~int64_t(15));
   kp.bits_cap = cigar ? ps.bits_cap : 0;
-  const int64_t table_bytes = cigar ? (int64_t)kp.table_cap * 8 : 0;
+  const int64_t table_bytes = cigar ? (int64_t)kp.table_cap * kBtRowBytes : 0;
+  if (!ps.pooled) kp.pool = nullptr;
   kp.gscratch_per_warp = (kp.ring_bytes + kp.seq_bytes + table_bytes + kp.bits_cap + 255) & ~int64_t(255);
 
   int wpc = (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_warp, 1));
   wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
-  const size_t smem = (size_t)kp.smem_per_warp * wpc;
+  size_t smem = (size_t)kp.smem_per_warp * wpc;
   void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur);
   // shared memory holds only the staged sequences and row limits; give the
   // rest of the SM's unified storage to L1, which caches the wavefront rows
@@ -136,12 +143,21 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   bps = std::max(1, std::min(bps, ps.max_blocks_per_sm));
   const int need = (n_upper + wpc - 1) / wpc;
   int blocks = std::min(bps * E->num_sms, std::max(need, 1));
+  if (ps.pooled) {
+    // a pooled pass's warp count is a bound, not a hint: the last pass relies
+    // on all of its warps holding their largest back-trace at once
+    if (wpc > n_upper) {
+      wpc = std::max(1, n_upper);
+      smem = (size_t)kp.smem_per_warp * wpc;
+    }
+    blocks = std::max(1, std::min(blocks, n_upper / wpc));
+  }
   // bound the scratch slices by the budget
   const int64_t budget =
       E->scratch_budget >= 0 ? E->scratch_budget : (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
   if ((int64_t)blocks * wpc * kp.gscratch_per_warp > budget)
     blocks = std::max(1, (int)(budget / (wpc * kp.gscratch_per_warp)));
-  if ((int64_t)wpc * kp.gscratch_per_warp > budget && cigar) {
+  if ((int64_t)wpc * kp.gscratch_per_warp > budget && cigar && !ps.pooled) {
     // even one block is over the budget: shrink its back-trace slices to fit;
     // pairs whose back-trace needs more report WF_STATUS_OOM (final pass)
     const int64_t fixed = (kp.ring_bytes + kp.seq_bytes + table_bytes + 255) & ~int64_t(255);
@@ -170,6 +186,7 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   const bool cigar = !cfg.score_only;
   if (max_len < 1) max_len = 1;
   // counters: [0..3] work queues of passes 1-4, [4..6] retry counts of passes 1-3
+  // (retry lists: pass q writes list q-1, at retry + (q-1) * n)
   if (ensure(E->counters, 8 * sizeof(int32_t)) || ensure(E->retry, (size_t)3 * n * sizeof(int32_t)))
     return WF2G_ERR_OOM_;
   int32_t* counters = (int32_t*)E->counters.p;
@@ -218,16 +235,57 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   if (cigar) p.bits_cap = std::min(p.bits_cap, need);
   int rc = run_pass(E, cfg, k, p, n, E->scratch1, st);
   if (rc) return rc;
-  // passes 2-4 over the previous pass's overflow list: 8-bit sequences and
-  // ever larger back-trace slices on ever fewer warps (16 MB on up to 8
-  // blocks per SM, 256 MB on 2, then whatever one alignment of the batch may
-  // need); the last pass that covers `need` reports a remaining overflow as
-  // WF_STATUS_OOM
-  const int64_t slices[3] = {int64_t(16) << 20, int64_t(256) << 20, need};
-  const int per_sm[3] = {8, 2, 1};
+  if (!cigar) {
+    // score-only: the pairs with non-ACGT bytes, 8-bit sequences
+    k = base;
+    k.items = retry;
+    k.num_items_dev = counters + 4;
+    k.n_items = 0;
+    k.queue = counters + 1;
+    Pass p2{8, 1, 0, 8, 0};
+    return run_pass(E, cfg, k, p2, std::min(n, 8 * E->num_sms * 8), E->scratch2, st);
+  }
+  // passes 2 and 3: the overflow list with choice bytes in a shared block
+  // pool, so each pair holds what its back-trace needs, up to `need` bytes
+  // (blocks of at least two of the widest rows; a row never spans blocks, so a
+  // pair fills at least half of each block it holds).  Pass 2 runs as many
+  // warps as the pool can feed at about 24 MB each, pass 3 at 96 MB each; a
+  // pair that finds the pool empty goes to the next pass.  Pass 4 runs few
+  // enough warps that all of them can hold their largest back-trace at once,
+  // so every outcome depends on the pair alone; what does not fit there is
+  // reported as WF_STATUS_OOM.
+  const int64_t block_bytes =
+      std::max<int64_t>(int64_t(1) << 20, ((4 * (int64_t)max_len + 64) + 4095) & ~int64_t(4095));
+  const int64_t pool_cap =
+      E->pool_budget >= 0 ? E->pool_budget : (int64_t)env_int("WF2G_POOL_MB", 48 << 10) << 20;
+  // sized for the batch: a one-pair call takes a small pool, a large batch the budget
+  const int64_t per_pair = std::max(2 * block_bytes, std::min<int64_t>(need, int64_t(64) << 20));
+  const int64_t pool_bytes = std::max(
+      2 * block_bytes, std::min(pool_cap, (int64_t)std::min(n, 8 * E->num_sms * 8) * per_pair));
+  const int nblocks = (int)std::min<int64_t>(pool_bytes / block_bytes, INT32_MAX / 2);
+  if (ensure(E->pool, (size_t)nblocks * block_bytes) ||
+      ensure(E->poolctl, ((size_t)nblocks + 64) * sizeof(int32_t)))
+    return WF2G_ERR_OOM_;
+  int32_t* ctl = (int32_t*)E->poolctl.p;
+  int32_t* stack = ctl + 64;
+  int32_t* count = ctl;
+  int32_t* lock = ctl + 1;
+  int nb = nblocks;
+  void* iargs[] = {(void*)&stack, (void*)&count, (void*)&lock, (void*)&nb};
+  const int igrid = std::max(1, std::min((nblocks + 255) / 256, 1024));
+  if (cudaLaunchKernel(wf2g_pool_init_ptr(), dim3(igrid), dim3(256), iargs, 0, st) != cudaSuccess)
+    return WF2G_ERR_CUDA_;
+  E->launches++;
+  const int64_t items = ((4 * (int64_t)max_len + 64) + 255) & ~int64_t(255);
+  const int max_blocks =
+      (int)std::min<int64_t>(nblocks, std::min<int64_t>(2 * (need / block_bytes) + 2, 16384));
+  const int64_t pool_total = (int64_t)nblocks * block_bytes;
+  // the back-trace bytes a pass-2 warp is expected to hold (pass 3: 4x that)
+  const int64_t warp_bytes = std::max<int64_t>(1, env_int("WF2G_POOL_WARP_MB", 24)) << 20;
   for (int q = 0; q < 3; ++q) {
-    const int64_t bits = cigar ? std::min(need, slices[q]) : 0;
-    const bool final_pass = !cigar || bits >= need || q == 2;
+    const bool final_pass = (q == 2);
+    const int64_t warps = std::max<int64_t>(
+        1, final_pass ? nblocks / max_blocks : pool_total / (warp_bytes << (2 * q)));
     k = base;
     k.items = retry + (size_t)q * n;
     k.num_items_dev = counters + 4 + q;
@@ -235,10 +293,16 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
     k.queue = counters + 1 + q;
     k.retry_items = final_pass ? nullptr : retry + (size_t)(q + 1) * n;
     k.retry_count = final_pass ? nullptr : counters + 5 + q;
-    Pass pq{8, final_pass ? 1 : 0, bits, per_sm[q]};
-    rc = run_pass(E, cfg, k, pq, std::min(n, per_sm[q] * E->num_sms * 8), E->scratch2, st);
+    k.pool = (uint8_t*)E->pool.p;
+    k.block_bytes = block_bytes;
+    k.pool_stack = stack;
+    k.pool_count = count;
+    k.pool_lock = lock;
+    k.max_blocks = max_blocks;
+    k.pair_cap = need;
+    Pass pq{8, final_pass ? 1 : 0, (int64_t)max_blocks * 4 + items, 8, 1};
+    rc = run_pass(E, cfg, k, pq, (int)std::min<int64_t>(n, warps), E->scratch2, st);
     if (rc) return rc;
-    if (final_pass) break;
   }
   return WF2G_OK_;
 }

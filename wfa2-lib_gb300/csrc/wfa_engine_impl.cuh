@@ -27,6 +27,7 @@ extern "C" void* wf2g_bi_kernel_ptr(int a2p);
 extern "C" void* wf2g_bi_pack_ptr(void);
 extern "C" void* wf2g_bi_gather_ptr(void);
 extern "C" size_t wf2g_bi_smem_bytes(int a2p, int scope);
+extern "C" void* wf2g_pool_init_ptr(void);
 
 namespace eng {
 
@@ -71,6 +72,7 @@ struct Engine {
   DevBuf counters;  // [0] queue pass 1, [1] queue pass 2, [2] retry count
   DevBuf retry;
   DevBuf scratch1, scratch2;
+  DevBuf pool, poolctl;  // back-trace block pool; [count, lock, ..., stack]
   BiState* bi = nullptr;
   // device-memory limits of this engine (bytes; < 0: the WF2G_SCRATCH_GB /
   // WF2G_BI_SCRATCH_GB defaults) and the cap of back-trace bytes per warp in
@@ -78,6 +80,7 @@ struct Engine {
   // of the batch; a pair above the cap finishes with WF_STATUS_OOM)
   int64_t scratch_budget = -1;
   int64_t bi_scratch_budget = -1;
+  int64_t pool_budget = -1;  // back-trace block pool (< 0: WF2G_POOL_GB, default 32)
   int64_t bits_cap = 0;
 };
 

@@ -196,6 +196,61 @@ __device__ __forceinline__ bool in_bounds(int32_t off, int k, int plen, int tlen
   return (uint32_t)off <= (uint32_t)tlen && (uint32_t)(off - k) <= (uint32_t)plen;
 }
 
+// ---------------------------------------------------------------- block pool
+// A spin lock with a bounded number of tries guards the free stack; a caller
+// that gives up treats the pool as empty (its pair is retried in a later pass).
+constexpr int kPoolTries = 1 << 20;
+
+__device__ __forceinline__ bool pool_lock(int32_t* lock) {
+  for (int i = 0; i < kPoolTries; ++i) {
+    if (atomicCAS(lock, 0, 1) == 0) {
+      __threadfence();
+      return true;
+    }
+    __nanosleep(64);
+  }
+  return false;
+}
+__device__ __forceinline__ void pool_unlock(int32_t* lock) {
+  __threadfence();
+  atomicExch(lock, 0);
+}
+// One free block index, or -1.
+__device__ int pool_pop(const KParams& p) {
+  if (!pool_lock(p.pool_lock)) return -1;
+  volatile int32_t* const cnt = p.pool_count;
+  volatile int32_t* const stk = p.pool_stack;
+  int b = -1;
+  const int c = *cnt;
+  if (c > 0) {
+    b = stk[c - 1];
+    *cnt = c - 1;
+  }
+  pool_unlock(p.pool_lock);
+  return b;
+}
+// Returns n blocks (if the lock cannot be had they stay out of the pool until
+// the next batch re-initialises it).
+__device__ void pool_push(const KParams& p, const int32_t* blocks, int n) {
+  if (!pool_lock(p.pool_lock)) return;
+  volatile int32_t* const cnt = p.pool_count;
+  volatile int32_t* const stk = p.pool_stack;
+  const int c = *cnt;
+  for (int i = 0; i < n; ++i) stk[c + i] = blocks[i];
+  *cnt = c + n;
+  pool_unlock(p.pool_lock);
+}
+
+// Pool set-up before a pooled pass: every block free, lock released.
+__global__ void wfa_pool_init_kernel(int32_t* stack, int32_t* count, int32_t* lock, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    stack[i] = i;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *count = n;
+    *lock = 0;
+  }
+}
+
 // 4 resident 256-thread blocks per SM (64 registers per thread): the kernel
 // is latency-bound, so residency matters more than registers.
 #ifndef WF2G_MIN_BLOCKS
@@ -237,8 +292,14 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
   // limits; the cut offsets stay readable, as wf_elements_init_min/max keep
   // them in the reference (wavefront/wavefront_compute.c:498-527)
   int2* const imeta = meta + nrows;
-  int2* const table = CIGAR ? reinterpret_cast<int2*>(gs) : nullptr;
+  BtRow* const table = CIGAR ? reinterpret_cast<BtRow*>(gs) : nullptr;
   uint8_t* const bits = CIGAR ? reinterpret_cast<uint8_t*>(table + p.table_cap) : nullptr;
+  // where choice bytes live: the warp's slice, or the shared block pool, in
+  // which case the slice holds the pair's block list and then the walk items
+  const bool pooled = CIGAR && ENC == 8 && p.pool != nullptr;  // pass 1 (2-bit) never pools
+  uint8_t* const bt = pooled ? p.pool : bits;
+  int32_t* const owned = reinterpret_cast<int32_t*>(bits);
+  const int64_t owned_bytes = pooled ? (int64_t)p.max_blocks * 4 : 0;
   auto row = [=](int r) -> OffT* { return ring + (size_t)r * stride + kofs; };
   const OffT* const null_row = row(nrows);
   const RingBounds rb{ring, ring + (size_t)(nrows + 1) * stride};
@@ -315,7 +376,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       const int r0 = comp_row(cb, 0, 0, 0);
       RING_ST(row(r0), 0, (OffT)L0);
       meta[r0] = imeta[r0] = make_int2(0, 0);
-      if (CIGAR) table[0] = make_int2(0, 0);
+      if (CIGAR) table[0] = BtRow{0, 0, 0};
     }
     __syncwarp();
 
@@ -323,7 +384,9 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int curM = 0, cur1 = 0, cur2 = 0;  // ring slots of score s
     int null_steps = 0;
     int steps_wait = p.h_steps;  // wf-adaptive (wavefront/wavefront_heuristic.c:114-121)
-    int64_t cursor = 0;  // choice bytes used
+    int64_t cursor = 0;  // choice bytes used (slice)
+    int nblk = 0, cur_blk = -1;  // pool: blocks held, block being filled
+    int64_t blk_off = 0, pool_used = 0;
     int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable, 4 guard
     const int k_end = tlen - plen;
     int mlo = cb == 0 ? 0 : 1, mhi = 0;  // trimmed limits of M[s]
@@ -467,7 +530,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
             result = -1;
             break;
           }
-          if (lane == 0 && CHK(s < p.table_cap, 32, s)) table[s] = make_int2(-1, 0);
+          if (lane == 0 && CHK(s < p.table_cap, 32, s)) table[s] = BtRow{-1, 0, -1};
         }
         __syncwarp();
         m_exists = false;
@@ -491,9 +554,31 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
       }
       const int width = hi - lo + 1;
-      if (CIGAR && (s >= p.table_cap || cursor + width > p.bits_cap)) {
+      if (CIGAR && (s >= p.table_cap || (!pooled && cursor + width > p.bits_cap))) {
         result = -1;
         break;
+      }
+      int64_t bpos = cursor;  // this row's first choice byte in the store
+      if (pooled) {
+        if (pool_used + width > p.pair_cap) {  // over the pair's back-trace budget
+          result = -1;
+          break;
+        }
+        pool_used += width;
+        if (cur_blk < 0 || blk_off + width > p.block_bytes) {
+          int b = -1;
+          if (nblk < p.max_blocks && lane == 0) b = pool_pop(p);
+          b = __shfl_sync(kFull, b, 0);
+          if (b < 0) {  // pool empty: a later pass retries the pair
+            result = -1;
+            break;
+          }
+          if (lane == 0) owned[nblk] = b;
+          ++nblk;
+          cur_blk = b;
+          blk_off = 0;
+        }
+        bpos = (int64_t)cur_blk * p.block_bytes + blk_off;
       }
       clear_outside(oM, oldM, lo, hi, lane, rb, g_pair);
       clear_outside(oI1, oldI1, lo, hi, lane, rb, g_pair);
@@ -534,7 +619,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         }
       }
       const bool ghost = wI1 || wD1 || wI2 || wD2;
-      uint8_t* const brow = CIGAR ? bits + cursor - lo : nullptr;
+      uint8_t* const brow = CIGAR ? bt + bpos - lo : nullptr;
 
       int tloM = INT32_MAX, thiM = INT32_MIN;
       int tloI1 = INT32_MAX, thiI1 = INT32_MIN, tloD1 = INT32_MAX, thiD1 = INT32_MIN;
@@ -643,7 +728,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
               c |= (uint8_t)(wd2e >= mo2_p) << 6;
             }
           }
-          if (CHK(cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
+          if (CHK(pooled || cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
         }
       }
       __syncwarp();
@@ -675,9 +760,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           meta[rowI2 + cur2] = imeta[rowI2 + cur2] = make_int2(tloI2, thiI2);
           meta[rowD2 + cur2] = imeta[rowD2 + cur2] = make_int2(tloD2, thiD2);
         }
-        if (CIGAR && CHK(s < p.table_cap, 31, s)) table[s] = make_int2((int)cursor, lo);
+        if (CIGAR && CHK(s < p.table_cap, 31, s)) table[s] = BtRow{bpos, lo, width};
       }
-      if (CIGAR) cursor += width;
+      if (CIGAR) {
+        if (pooled) blk_off += width;
+        else cursor += width;
+      }
       mlo = tloM;
       mhi = thiM;
       m_exists = true;
@@ -689,8 +777,19 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
     }
 
+    // pool blocks go back when the pair is finished (every path below)
+    auto release_blocks = [&]() {
+      if (pooled && nblk > 0) {
+        __syncwarp();
+        if (lane == 0) pool_push(p, owned, nblk);
+        nblk = 0;
+        __syncwarp();
+      }
+    };
+
     // ================= finish the pair (warp-uniform from here on)
     if (result != 1) {
+      release_blocks();
       if (lane == 0) {
         if (result == -1 && !p.final_pass) {
           p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
@@ -721,8 +820,8 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
 
     // ================= back-trace over choice bytes (uniform walk), then a
     // forward replay that re-extends the matches of every M visit
-    uint8_t* const items = bits + cursor;
-    const int64_t items_cap = p.bits_cap - cursor;
+    uint8_t* const items = pooled ? bits + owned_bytes : bits + cursor;
+    const int64_t items_cap = pooled ? p.bits_cap - owned_bytes : p.bits_cap - cursor;
     int64_t n = 0;
     bool bad = false;
     bool items_full = false;  // walk items did not fit the back-trace slice
@@ -745,11 +844,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           break;
         }
         if (!CHK(ss < p.table_cap, 34, ss)) { bad = true; break; }
-        const int2 te = table[ss];
-        const int64_t bi = (int64_t)te.x + (kk - te.y);
-        if (te.x < 0 || kk < te.y || bi >= cursor) { bad = true; break; }
-        if (!CHK(bi >= 0 && bi < p.bits_cap, 35, bi)) { bad = true; break; }
-        const uint8_t c = bits[bi];
+        const BtRow te = table[ss];
+        if (te.width <= 0 || kk < te.lo || kk - te.lo >= te.width) { bad = true; break; }
+        const int64_t bi = te.pos + (kk - te.lo);
+        if (!CHK(pooled || (bi >= 0 && bi < p.bits_cap), 35, bi)) { bad = true; break; }
+        const uint8_t c = bt[bi];
         char op = 0;
         if (st == 0) {
           const int src = c & 7;
@@ -778,6 +877,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
     }
     __syncwarp();
+    release_blocks();  // the walk has read every choice byte it needs
     if (items_full) {
       // the same overflow as a full cell table: retry with a larger slice, or
       // WF_STATUS_OOM in the final pass
@@ -859,6 +959,8 @@ extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int
   if (heur) return off_bytes == 2 ? pick<int16_t, true>(a2p, cigar, enc) : pick<int32_t, true>(a2p, cigar, enc);
   return off_bytes == 2 ? pick<int16_t, false>(a2p, cigar, enc) : pick<int32_t, false>(a2p, cigar, enc);
 }
+
+extern "C" void* wf2g_pool_init_ptr(void) { return (void*)wfa_pool_init_kernel; }
 
 // First bounds violation seen by a checked build: {site, index, pair, count}.
 extern "C" int wf2g_fault_info(unsigned long long* out) {

@@ -33,6 +33,15 @@ constexpr int kStUnattainable = -300;
 //   bit 5     I2 extends                 bit 6  D2 extends
 enum : uint8_t { kSrcX = 0, kSrcD1 = 1, kSrcI1 = 2, kSrcD2 = 3, kSrcI2 = 4 };
 
+// Back-trace row table entry, one per score: choice bytes of the row's cells
+// [lo, lo+width) start at byte `pos` of the back-trace store (the warp's slice,
+// or the block pool); width < 0 marks a score without wavefront.
+struct BtRow {
+  int64_t pos;
+  int32_t lo, width;
+};
+constexpr int kBtRowBytes = (int)sizeof(BtRow);
+
 struct Penalties {
   int match;  // user match (<= 0)
   int x, o1, e1, o2, e2;  // internal (possibly Eizenga-transformed) penalties
@@ -84,7 +93,17 @@ struct KParams {
   int64_t ring_bytes;
   int64_t seq_bytes;
   int table_cap;      // back-trace row table entries (scores); also the score bound
-  int64_t bits_cap;   // back-trace choice bytes per warp
+  int64_t bits_cap;   // back-trace choice bytes per warp (pooled: owned-block list + walk items)
+  // Back-trace block pool (nullptr: choice bytes in the warp's slice).  A pair
+  // takes blocks from a shared free stack as its rows need room and returns
+  // them when it finishes, so each pair uses what its alignment needs.
+  uint8_t* pool;
+  int64_t block_bytes;  // >= the widest row
+  int32_t* pool_stack;  // free block indices
+  int32_t* pool_count;  // entries on the stack
+  int32_t* pool_lock;   // 0 free, 1 held
+  int max_blocks;       // blocks one pair may hold
+  int64_t pair_cap;     // choice bytes one pair may use (its back-trace budget)
 };
 
 }  // namespace wf2g

@@ -134,7 +134,8 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.smem_per_warp = (int)(((int64_t)seq_bytes + (int64_t)nrows * 16 + 15) & ~int64_t(15));
   kp.bits_cap = cigar ? kNoAllocBitsPerWarp : 0;
   kp.gscratch_per_warp =
-      (kp.ring_bytes + (cigar ? (int64_t)kp.table_cap * 8 + kp.bits_cap : 0) + 255) & ~int64_t(255);
+      (kp.ring_bytes + (cigar ? (int64_t)kp.table_cap * kBtRowBytes + kp.bits_cap : 0) + 255) &
+      ~int64_t(255);
 
   // the array: [control: 256 bytes][per-warp slices]
   const int64_t avail = (int64_t)kNoAllocBytes - 256;

@@ -324,7 +324,8 @@ extern "C" void* wf2g_server_new(const wf2g_cfg_t* cfg, int64_t hbm_budget,
     }
     Engine* en = (Engine*)E;
     en->scratch_budget = share / 2;
-    en->bi_scratch_budget = share / 2;
+    en->bi_scratch_budget = share / 4;
+    en->pool_budget = share / 4;
     // back-trace bytes a pair may use: pairs needing more are over budget
     // and go to BiWFA
     en->bits_cap = backtrace_budget > 0 ? backtrace_budget : 64ll << 20;
