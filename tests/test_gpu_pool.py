@@ -64,8 +64,8 @@ def test_pool_results_do_not_depend_on_pool_size(gpu_available, wfa, oracle_mod,
 
     # default pool: everything fits
     assert _run(W, cfg, pats, txts, {}) == want
-    # 96 MB pool fed to 12 warps of 8 MB: pass 2 runs dry, later passes finish
-    assert _run(W, cfg, pats, txts, {"WF2G_POOL_MB": 96, "WF2G_POOL_WARP_MB": 8}) == want
+    # 96 MB pool fed to 12 pairs of 8 MB: pass 2 runs dry, later passes finish
+    assert _run(W, cfg, pats, txts, {"WF2G_POOL_MB": 96, "WF2G_POOL_PAIR_MB": 8}) == want
     # a pool of two 1 MB blocks: the large pairs report WF_STATUS_OOM, the
     # small ones (first pass, no pool) are exact
     tiny = _run(W, cfg, pats, txts, {"WF2G_POOL_MB": 2})

@@ -6,14 +6,18 @@
 //   pass 1    every pair: 2-bit packed sequences, 1 MB of back-trace bytes per
 //             warp; pairs with non-ACGT bytes or a longer back-trace go to a
 //             retry list;
-//   pass 2    the retry list: 8-bit sequences, choice bytes in a shared block
-//             pool (each pair takes blocks as its back-trace grows and
-//             returns them when done), as many warps as the pool can feed;
-//             a pair that finds the pool empty goes to the next list;
-//   pass 3    the same with fewer warps;
-//   pass 4    what is left, pooled, with few enough warps that all can hold
-//             their pair's back-trace at once; a remaining overflow is
-//             reported as WF_STATUS_OOM.
+//   pass 2    the retry list, a 256-thread CTA per pair (long pairs have rows
+//             of thousands of diagonals), 2-bit sequences, choice bytes in a
+//             shared block pool (each pair takes blocks as its back-trace
+//             grows and returns them when done), as many CTAs as the pool
+//             can feed; a pair that finds the pool empty, or holds non-ACGT
+//             bytes, goes to the next list;
+//   pass 3    the same with 8-bit sequences and fewer CTAs;
+//   pass 4    what is left, with few enough CTAs that all can hold their
+//             pair's back-trace at once; a remaining overflow is reported as
+//             WF_STATUS_OOM.
+// Score-only runs have no back-trace: pass 2 takes the non-ACGT pairs with
+// 8-bit sequences and is the last.
 // Each warp owns a global-memory slice holding its wavefront ring (every
 // diagonal the pair can reach, so rows never wrap) and back-trace bytes; the
 // slices stay L1/L2 resident.  On GB300 this measured 2x faster than a ring in
@@ -72,8 +76,9 @@ extern "C" void* wf2g_engine_new(int* err) {
       for (int enc = 2; enc <= 8; enc += 6)
         for (int ob = 2; ob <= 4; ob += 2)
           for (int h = 0; h < 2; ++h)
-            cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            for (int w = 0; w <= cig; ++w)
+              cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h, w),
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (err) *err = WF2G_OK_;
   return E;
 }
@@ -104,6 +109,7 @@ struct Pass {
   int64_t bits_cap; // back-trace bytes per warp (full CIGAR); pooled: block list + walk items
   int max_blocks_per_sm;
   int pooled;       // choice bytes in the block pool (base.pool)
+  int wide;         // a 256-thread CTA per pair (pooled passes only)
 };
 
 static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const Pass& ps,
@@ -122,24 +128,29 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   kp.seq_in_smem = seq_bytes <= 48 * 1024;
   kp.seq_bytes = kp.seq_in_smem ? 0 : ((seq_bytes + 255) & ~int64_t(255));
   // staged sequences + per-row limits and initialised windows (2 x int2)
-  kp.smem_per_warp = (int)((((kp.seq_in_smem ? seq_bytes : 0) + (int64_t)nrows * 16) + 15) & ~int64_t(15));
+  // (+ the CTA's reduction partials and broadcast slot when a CTA is a group)
+  kp.smem_per_group = (int)((((kp.seq_in_smem ? seq_bytes : 0) + (int64_t)nrows * 16 +
+                              (ps.wide ? kGroupRedBytes : 0)) + 15) & ~int64_t(15));
   kp.bits_cap = cigar ? ps.bits_cap : 0;
   const int64_t table_bytes = cigar ? (int64_t)kp.table_cap * kBtRowBytes : 0;
   if (!ps.pooled) kp.pool = nullptr;
-  kp.gscratch_per_warp = (kp.ring_bytes + kp.seq_bytes + table_bytes + kp.bits_cap + 255) & ~int64_t(255);
+  kp.gscratch_per_group = (kp.ring_bytes + kp.seq_bytes + table_bytes + kp.bits_cap + 255) & ~int64_t(255);
 
-  int wpc = (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_warp, 1));
-  wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
-  size_t smem = (size_t)kp.smem_per_warp * wpc;
-  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur);
+  // groups per CTA: warps of one CTA (a warp per pair), or one CTA per pair
+  const int tpg = ps.wide ? 256 : 32;
+  int wpc = ps.wide ? 1 : (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_group, 1));
+  if (!ps.wide) wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
+  size_t smem = (size_t)kp.smem_per_group * wpc;
+  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur, ps.wide);
+  if (!fn) return WF2G_ERR_CUDA_;
   // shared memory holds only the staged sequences and row limits; give the
   // rest of the SM's unified storage to L1, which caches the wavefront rows
-  const int want_blocks = std::max(1, 64 / wpc);
+  const int want_blocks = ps.wide ? 8 : std::max(1, 64 / wpc);
   int carve = (int)((smem * want_blocks * 100 + 228 * 1024 - 1) / (228 * 1024)) + 1;
   carve = std::max(1, std::min(carve, 100));
   cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
   int bps = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32 * wpc, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, tpg * wpc, smem);
   bps = std::max(1, std::min(bps, ps.max_blocks_per_sm));
   const int need = (n_upper + wpc - 1) / wpc;
   int blocks = std::min(bps * E->num_sms, std::max(need, 1));
@@ -148,28 +159,28 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
     // on all of its warps holding their largest back-trace at once
     if (wpc > n_upper) {
       wpc = std::max(1, n_upper);
-      smem = (size_t)kp.smem_per_warp * wpc;
+      smem = (size_t)kp.smem_per_group * wpc;
     }
     blocks = std::max(1, std::min(blocks, n_upper / wpc));
   }
   // bound the scratch slices by the budget
   const int64_t budget =
       E->scratch_budget >= 0 ? E->scratch_budget : (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
-  if ((int64_t)blocks * wpc * kp.gscratch_per_warp > budget)
-    blocks = std::max(1, (int)(budget / (wpc * kp.gscratch_per_warp)));
-  if ((int64_t)wpc * kp.gscratch_per_warp > budget && cigar && !ps.pooled) {
+  if ((int64_t)blocks * wpc * kp.gscratch_per_group > budget)
+    blocks = std::max(1, (int)(budget / (wpc * kp.gscratch_per_group)));
+  if ((int64_t)wpc * kp.gscratch_per_group > budget && cigar && !ps.pooled) {
     // even one block is over the budget: shrink its back-trace slices to fit;
     // pairs whose back-trace needs more report WF_STATUS_OOM (final pass)
     const int64_t fixed = (kp.ring_bytes + kp.seq_bytes + table_bytes + 255) & ~int64_t(255);
     const int64_t bits = ((budget / wpc - fixed) & ~int64_t(255));
     if (bits < (int64_t(1) << 20)) return WF2G_ERR_OOM_;
     kp.bits_cap = bits;
-    kp.gscratch_per_warp = fixed + bits;
+    kp.gscratch_per_group = fixed + bits;
   }
-  if (ensure(scratch, (size_t)blocks * wpc * kp.gscratch_per_warp)) return WF2G_ERR_OOM_;
+  if (ensure(scratch, (size_t)blocks * wpc * kp.gscratch_per_group)) return WF2G_ERR_OOM_;
   kp.gscratch = (uint8_t*)scratch.p;
   void* args[] = {(void*)&kp};
-  cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args, smem, st);
+  cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(tpg * wpc), args, smem, st);
   if (e != cudaSuccess) {
     fprintf(stderr, "[wfa2gpu] kernel launch failed: %s\n", cudaGetErrorString(e));
     return WF2G_ERR_CUDA_;
@@ -231,7 +242,7 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   k.queue = counters + 0;
   k.retry_items = retry;
   k.retry_count = counters + 4;
-  Pass p{2, 0, int64_t(1) << 20, 8};
+  Pass p{2, 0, int64_t(1) << 20, 8, 0, 0};
   if (cigar) p.bits_cap = std::min(p.bits_cap, need);
   int rc = run_pass(E, cfg, k, p, n, E->scratch1, st);
   if (rc) return rc;
@@ -242,18 +253,18 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
     k.num_items_dev = counters + 4;
     k.n_items = 0;
     k.queue = counters + 1;
-    Pass p2{8, 1, 0, 8, 0};
+    Pass p2{8, 1, 0, 8, 0, 0};
     return run_pass(E, cfg, k, p2, std::min(n, 8 * E->num_sms * 8), E->scratch2, st);
   }
-  // passes 2 and 3: the overflow list with choice bytes in a shared block
-  // pool, so each pair holds what its back-trace needs, up to `need` bytes
-  // (blocks of at least two of the widest rows; a row never spans blocks, so a
-  // pair fills at least half of each block it holds).  Pass 2 runs as many
-  // warps as the pool can feed at about 24 MB each, pass 3 at 96 MB each; a
-  // pair that finds the pool empty goes to the next pass.  Pass 4 runs few
-  // enough warps that all of them can hold their largest back-trace at once,
-  // so every outcome depends on the pair alone; what does not fit there is
-  // reported as WF_STATUS_OOM.
+  // passes 2-4: the overflow list, a 256-thread CTA per pair, choice bytes in
+  // a shared block pool, so each pair holds what its back-trace needs, up to
+  // `need` bytes (blocks of at least two of the widest rows; a row never spans
+  // blocks, so a pair fills at least half of each block it holds).  Pass 2
+  // (2-bit sequences) runs as many CTAs as the pool can feed at about 24 MB
+  // each; pairs with non-ACGT bytes, or that find the pool empty, go to pass 3
+  // (8-bit sequences, 96 MB each).  Pass 4 runs few enough CTAs that all of
+  // them can hold their largest back-trace at once, so every outcome depends
+  // on the pair alone; what does not fit there is reported as WF_STATUS_OOM.
   const int64_t block_bytes =
       std::max<int64_t>(int64_t(1) << 20, ((4 * (int64_t)max_len + 64) + 4095) & ~int64_t(4095));
   const int64_t pool_cap =
@@ -280,12 +291,12 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   const int max_blocks =
       (int)std::min<int64_t>(nblocks, std::min<int64_t>(2 * (need / block_bytes) + 2, 16384));
   const int64_t pool_total = (int64_t)nblocks * block_bytes;
-  // the back-trace bytes a pass-2 warp is expected to hold (pass 3: 4x that)
-  const int64_t warp_bytes = std::max<int64_t>(1, env_int("WF2G_POOL_WARP_MB", 24)) << 20;
+  // the back-trace bytes a pass-2 pair is expected to hold (pass 3: 4x that)
+  const int64_t pair_bytes = std::max<int64_t>(1, env_int("WF2G_POOL_PAIR_MB", 24)) << 20;
   for (int q = 0; q < 3; ++q) {
     const bool final_pass = (q == 2);
-    const int64_t warps = std::max<int64_t>(
-        1, final_pass ? nblocks / max_blocks : pool_total / (warp_bytes << (2 * q)));
+    const int64_t groups = std::max<int64_t>(
+        1, final_pass ? nblocks / max_blocks : pool_total / (pair_bytes << (2 * q)));
     k = base;
     k.items = retry + (size_t)q * n;
     k.num_items_dev = counters + 4 + q;
@@ -300,8 +311,8 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
     k.pool_lock = lock;
     k.max_blocks = max_blocks;
     k.pair_cap = need;
-    Pass pq{8, final_pass ? 1 : 0, (int64_t)max_blocks * 4 + items, 8, 1};
-    rc = run_pass(E, cfg, k, pq, (int)std::min<int64_t>(n, warps), E->scratch2, st);
+    Pass pq{q == 0 ? 2 : 8, final_pass ? 1 : 0, (int64_t)max_blocks * 4 + items, 8, 1, 1};
+    rc = run_pass(E, cfg, k, pq, (int)std::min<int64_t>(n, groups), E->scratch2, st);
     if (rc) return rc;
   }
   return WF2G_OK_;

@@ -21,7 +21,7 @@
 #define WF2G_ERR_OOM_ -5
 
 namespace wf2g {
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur);
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 extern "C" void* wf2g_bi_kernel_ptr(int a2p);
 extern "C" void* wf2g_bi_pack_ptr(void);

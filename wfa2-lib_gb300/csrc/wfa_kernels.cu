@@ -1,245 +1,11 @@
-// wfa_kernels.cu -- sm_103a kernels of the GB300 wavefront aligner.
-//
-// Semantics follow smarco/WFA2-lib's exact unidirectional WFA (end-to-end):
-//   compute   wavefront/wavefront_compute_affine.c:44-86,
-//             wavefront/wavefront_compute_affine2p.c:45-106
-//   limits    wavefront/wavefront_compute.c:40-87 (output range = union of inputs)
-//   trim      wavefront/wavefront_compute.c:579-613 (ends only; interior kept)
-//   extend    wavefront/wavefront_extend.c:86-121 (exact LCP per diagonal)
-//   terminate wavefront/wavefront_termination.c:37-60
-//   loop      wavefront/wavefront_unialign.c:242-273, limits :98-143
-//   backtrace wavefront/wavefront_backtrace.c:320-529 -- reproduced from
-//             per-cell choice bits: ties resolve exactly as the reference's
-//             (offset<<4|type) maximum does: mismatch > D2 > D1 > I2 > I1,
-//             extension > opening (wavefront/wavefront_backtrace.c:49-59).
-//
-// GPU design: one warp per pair, lanes striped over diagonals k.  Every
-// wavefront row is NULL outside its trimmed range (the reference's NULL
-// padding, wavefront/wavefront_compute.c:498-575), so the cell loop reads its
-// inputs without bounds checks; empty inputs read an all-NULL row.
-#include <cuda_runtime.h>
-
-#include <cstdint>
-
-#include "wfa_kernels.cuh"
+// wfa_kernels.cu -- sm_103a kernels of the GB300 wavefront aligner: the
+// warp-per-pair exact variants, the block-pool set-up and the kernel table.
+// The alignment kernel itself is the template of wfa_align.cuh; its
+// wf-adaptive and CTA-per-pair variants are built by wfa_kernels_heur.cu and
+// wfa_kernels_wide.cu, in parallel with this unit.
+#include "wfa_align.cuh"
 
 namespace wf2g {
-
-// NULL as stored in a row of OffT (int16 rows serve sequences < 32000).
-template <typename OffT>
-__device__ __forceinline__ OffT null_of() {
-  return sizeof(OffT) == 2 ? (OffT)(-32768) : (OffT)kNull;
-}
-
-// ---------------------------------------------------------------- checking
-// Built with -DWF2G_CHECKED every ring, sequence, back-trace and output access
-// is bounds-checked: a violation is recorded (first one wins) and the access
-// is skipped, so a faulty index is reported instead of faulting the GPU.
-#ifdef WF2G_CHECKED
-__device__ unsigned long long g_fault[4];  // site, index, pair, count
-__device__ __forceinline__ bool wf2g_ok(bool ok, int site, long long idx, int pair) {
-  if (!ok) {
-    if (atomicCAS(&g_fault[0], 0ull, (unsigned long long)site) == 0ull) {
-      g_fault[1] = (unsigned long long)idx;
-      g_fault[2] = (unsigned long long)pair;
-    }
-    atomicAdd(&g_fault[3], 1ull);
-  }
-  return ok;
-}
-#define CHK(cond, site, idx) wf2g_ok((cond), (site), (long long)(idx), g_pair)
-#else
-#define CHK(cond, site, idx) true
-#endif
-
-__device__ __forceinline__ int ring_back(int cur, int d, int R) {
-  // slot of score (s-d) when the slot of s is cur, 0 <= d < R
-  const int t = cur - d;
-  return t < 0 ? t + R : t;
-}
-
-// ---------------------------------------------------------------- sequences
-// ENC==2: base i at bits [31-2(i%16), 30-2(i%16)] of 32-bit word i/16.
-// ENC==8: byte i at bits [63-8(i%8), 56-8(i%8)] of 64-bit word i/8.
-template <int ENC>
-struct Seq;
-
-template <>
-struct Seq<2> {
-  typedef uint32_t Word;
-  static constexpr int kPer = 16;
-  static __device__ __forceinline__ uint32_t window(const uint32_t* W, int pos) {
-    const int w = pos >> 4;
-    return __funnelshift_l(W[w + 1], W[w], (pos & 15) << 1);
-  }
-  static __device__ __forceinline__ int equal_prefix(uint32_t d) { return __clz(d) >> 1; }
-  static __host__ __device__ int words(int len) { return ((len + 15) >> 4) + 2; }
-};
-
-template <>
-struct Seq<8> {
-  typedef uint64_t Word;
-  static constexpr int kPer = 8;
-  static __device__ __forceinline__ uint64_t window(const uint64_t* W, int pos) {
-    const int w = pos >> 3;
-    const int sh = (pos & 7) << 3;
-    uint64_t x = W[w];
-    if (sh) x = (x << sh) | (W[w + 1] >> (64 - sh));
-    return x;
-  }
-  static __device__ __forceinline__ int equal_prefix(uint64_t d) { return __clzll(d) >> 3; }
-  static __host__ __device__ int words(int len) { return ((len + 7) >> 3) + 2; }
-};
-
-// Longest common prefix of P[v..] and T[h..], at most lim characters:
-// word-wide XOR + count-leading-zeros (wavefront/wavefront_extend_kernels.c:68-92).
-template <int ENC>
-__device__ __forceinline__ int lcp(const typename Seq<ENC>::Word* P,
-                                   const typename Seq<ENC>::Word* T, int v, int h, int lim,
-                                   int nw = 0, int g_pair = 0) {
-  int L = 0;
-  while (L < lim) {
-    const int wp = (v + L) / Seq<ENC>::kPer, wt = (h + L) / Seq<ENC>::kPer;
-    if (!CHK(v + L >= 0 && wp + 1 < nw, 20, v + L) || !CHK(h + L >= 0 && wt + 1 < nw, 21, h + L))
-      return 0;
-    const auto d = Seq<ENC>::window(P, v + L) ^ Seq<ENC>::window(T, h + L);
-    if (d) {
-      L += Seq<ENC>::equal_prefix(d);
-      break;
-    }
-    L += Seq<ENC>::kPer;
-  }
-  return L < lim ? L : lim;
-}
-
-// Stages one sequence into W (warp-cooperative).  Returns false if ENC==2
-// and the sequence holds a byte outside {A,C,G,T}.
-template <int ENC>
-__device__ bool stage_sequence(const uint8_t* __restrict__ src, int len,
-                               typename Seq<ENC>::Word* W, int lane) {
-  const int nwords = Seq<ENC>::words(len);
-  bool ok = true;
-  if (ENC == 2) {
-    const int nblk = (len + 31) >> 5;  // 32 bases -> 2 words
-    for (int b = 0; b < nblk; ++b) {
-      const int i = (b << 5) + lane;
-      uint32_t code = 0;
-      if (i < len) {
-        const uint8_t c = src[i];
-        ok &= (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
-        code = (c >> 1) & 3u;  // A0 C1 T2 G3: a bijection on ACGT
-      }
-      const int sh = 30 - 2 * (lane & 15);
-      const uint32_t w0 = __reduce_or_sync(kFull, lane < 16 ? code << sh : 0u);
-      const uint32_t w1 = __reduce_or_sync(kFull, lane >= 16 ? code << sh : 0u);
-      if (lane == 0) {
-        W[2 * b] = w0;
-        if (2 * b + 1 < nwords) W[2 * b + 1] = w1;
-      }
-    }
-    for (int b = 2 * nblk + lane; b < nwords; b += 32) W[b] = 0;
-    ok = __all_sync(kFull, ok);
-  } else {
-    uint8_t* B = reinterpret_cast<uint8_t*>(W);
-    const int nbytes = nwords * 8;
-    for (int i = lane; i < nbytes; i += 32) {
-      const uint8_t c = i < len ? src[i] : 0;
-      B[(i & ~7) | (7 - (i & 7))] = c;  // big-endian inside each word
-    }
-  }
-  __syncwarp();
-  return ok;
-}
-
-// Ring bounds of the calling warp (checked builds only).
-struct RingBounds {
-  const void* lo;
-  const void* hi;
-};
-
-// NULL-fill row elements of diagonals [a,b].
-template <typename OffT>
-__device__ __forceinline__ void null_range(OffT* row, int a, int b, int lane,
-                                           RingBounds rb = RingBounds{nullptr, nullptr},
-                                           int g_pair = 0) {
-  if (a > b) return;  // also keeps a + lane from overflowing on empty ranges
-  for (int k = a + lane; k <= b; k += 32) {
-    if (CHK(rb.lo == nullptr || ((const void*)(row + k) >= rb.lo && (const void*)(row + k) < rb.hi), 1, k))
-      row[k] = null_of<OffT>();
-  }
-}
-
-// After computing [lo,hi] and finding the trimmed range [tlo,thi]: NULL the
-// trimmed-away ends (wavefront/wavefront_compute.c:579-613).
-template <typename OffT>
-__device__ __forceinline__ void trim_fill(OffT* row, int lo, int hi, int tlo, int thi, int lane,
-                                          RingBounds rb, int g_pair) {
-  if (tlo > thi) {
-    null_range(row, lo, hi, lane, rb, g_pair);
-  } else {
-    null_range(row, lo, tlo - 1, lane, rb, g_pair);
-    null_range(row, thi + 1, hi, lane, rb, g_pair);
-  }
-}
-
-// Clears what a reused slot holds outside the new range [lo,hi].
-template <typename OffT>
-__device__ __forceinline__ void clear_outside(OffT* row, int2 old, int lo, int hi, int lane,
-                                              RingBounds rb, int g_pair) {
-  if (old.x <= old.y) {
-    null_range(row, old.x, min(old.y, lo - 1), lane, rb, g_pair);
-    null_range(row, max(old.x, hi + 1), old.y, lane, rb, g_pair);
-  }
-}
-
-__device__ __forceinline__ bool in_bounds(int32_t off, int k, int plen, int tlen) {
-  return (uint32_t)off <= (uint32_t)tlen && (uint32_t)(off - k) <= (uint32_t)plen;
-}
-
-// ---------------------------------------------------------------- block pool
-// A spin lock with a bounded number of tries guards the free stack; a caller
-// that gives up treats the pool as empty (its pair is retried in a later pass).
-constexpr int kPoolTries = 1 << 20;
-
-__device__ __forceinline__ bool pool_lock(int32_t* lock) {
-  for (int i = 0; i < kPoolTries; ++i) {
-    if (atomicCAS(lock, 0, 1) == 0) {
-      __threadfence();
-      return true;
-    }
-    __nanosleep(64);
-  }
-  return false;
-}
-__device__ __forceinline__ void pool_unlock(int32_t* lock) {
-  __threadfence();
-  atomicExch(lock, 0);
-}
-// One free block index, or -1.
-__device__ int pool_pop(const KParams& p) {
-  if (!pool_lock(p.pool_lock)) return -1;
-  volatile int32_t* const cnt = p.pool_count;
-  volatile int32_t* const stk = p.pool_stack;
-  int b = -1;
-  const int c = *cnt;
-  if (c > 0) {
-    b = stk[c - 1];
-    *cnt = c - 1;
-  }
-  pool_unlock(p.pool_lock);
-  return b;
-}
-// Returns n blocks (if the lock cannot be had they stay out of the pool until
-// the next batch re-initialises it).
-__device__ void pool_push(const KParams& p, const int32_t* blocks, int n) {
-  if (!pool_lock(p.pool_lock)) return;
-  volatile int32_t* const cnt = p.pool_count;
-  volatile int32_t* const stk = p.pool_stack;
-  const int c = *cnt;
-  for (int i = 0; i < n; ++i) stk[c + i] = blocks[i];
-  *cnt = c + n;
-  pool_unlock(p.pool_lock);
-}
 
 // Pool set-up before a pooled pass: every block free, lock released.
 __global__ void wfa_pool_init_kernel(int32_t* stack, int32_t* count, int32_t* lock, int n) {
@@ -251,730 +17,72 @@ __global__ void wfa_pool_init_kernel(int32_t* stack, int32_t* count, int32_t* lo
   }
 }
 
-// 4 resident 256-thread blocks per SM (64 registers per thread): the kernel
-// is latency-bound, so residency matters more than registers.
-#ifndef WF2G_MIN_BLOCKS
-#define WF2G_MIN_BLOCKS 4
-#endif
+#define WF2G_INST(A2P, CIG, ENC, T) \
+  template __global__ void wfa_align_kernel<A2P, CIG, ENC, T, false, 32>(const KParams p);
+#define WF2G_INST_T(T)          \
+  WF2G_INST(false, false, 2, T) \
+  WF2G_INST(false, true, 2, T)  \
+  WF2G_INST(true, false, 2, T)  \
+  WF2G_INST(true, true, 2, T)   \
+  WF2G_INST(false, false, 8, T) \
+  WF2G_INST(false, true, 8, T)  \
+  WF2G_INST(true, false, 8, T)  \
+  WF2G_INST(true, true, 8, T)
+WF2G_INST_T(int16_t)
+WF2G_INST_T(int32_t)
 
-// HEUR: the wf-adaptive heuristic is compiled in (exact runs do without it)
-template <bool A2P, bool CIGAR, int ENC, typename OffT, bool HEUR>
-__global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const KParams p) {
-  typedef typename Seq<ENC>::Word Word;
-  extern __shared__ __align__(16) uint8_t smem[];
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int wpc = blockDim.x >> 5;
-  const int64_t gwarp = (int64_t)blockIdx.x * wpc + warp;
-  const Penalties pen = p.pen;
-  const int nrows = A2P ? pen.R + 2 * pen.RI1 + 2 * pen.RI2 : pen.R + 2 * pen.RI1;
-  const int stride = p.row_stride;
-  const int kofs = p.kofs;
-  const int nwords = Seq<ENC>::words(p.max_len);
-
-  // ---- carve per-warp memory
-  uint8_t* ws = smem + (size_t)warp * p.smem_per_warp;
-  uint8_t* gs = p.gscratch + gwarp * p.gscratch_per_warp;
-  OffT* const ring = reinterpret_cast<OffT*>(gs);  // (nrows+1) rows; row nrows is all-NULL
-  gs += p.ring_bytes;
-  Word* P;
-  if (p.seq_in_smem) {
-    P = reinterpret_cast<Word*>(ws);
-    ws += (size_t)2 * nwords * sizeof(Word);
-  } else {
-    P = reinterpret_cast<Word*>(gs);
-    gs += p.seq_bytes;
-  }
-  Word* const T = P + nwords;
-  int2* const meta = reinterpret_cast<int2*>(ws);  // [nrows] limits (lo,hi); lo>hi == null
-  // [nrows] initialised windows: a row is NULL outside its window.  The window
-  // equals the limits except after a heuristic cut-off, which narrows only the
-  // limits; the cut offsets stay readable, as wf_elements_init_min/max keep
-  // them in the reference (wavefront/wavefront_compute.c:498-527)
-  int2* const imeta = meta + nrows;
-  BtRow* const table = CIGAR ? reinterpret_cast<BtRow*>(gs) : nullptr;
-  uint8_t* const bits = CIGAR ? reinterpret_cast<uint8_t*>(table + p.table_cap) : nullptr;
-  // where choice bytes live: the warp's slice, or the shared block pool, in
-  // which case the slice holds the pair's block list and then the walk items
-  const bool pooled = CIGAR && ENC == 8 && p.pool != nullptr;  // pass 1 (2-bit) never pools
-  uint8_t* const bt = pooled ? p.pool : bits;
-  int32_t* const owned = reinterpret_cast<int32_t*>(bits);
-  const int64_t owned_bytes = pooled ? (int64_t)p.max_blocks * 4 : 0;
-  auto row = [=](int r) -> OffT* { return ring + (size_t)r * stride + kofs; };
-  const OffT* const null_row = row(nrows);
-  const RingBounds rb{ring, ring + (size_t)(nrows + 1) * stride};
-  int g_pair = -1;
-  (void)rb;
-  (void)g_pair;
-#ifdef WF2G_CHECKED
-#define RING_OK(ptr) CHK((const void*)(ptr) >= rb.lo && (const void*)(ptr) < rb.hi, 2, (const OffT*)(ptr) - ring)
-#define RING_LD(r, k) (RING_OK((r) + (k)) ? (int32_t)(r)[k] : (int32_t)null_of<OffT>())
-#define RING_ST(r, k, v) do { if (RING_OK((r) + (k))) (r)[k] = (v); } while (0)
-#else
-#define RING_LD(r, k) ((int32_t)(r)[k])
-#define RING_ST(r, k, v) ((r)[k] = (v))
-#endif
-
-  // ring starts all-NULL, every row empty
-  for (int64_t i = lane; i < (int64_t)(nrows + 1) * stride; i += 32) ring[i] = null_of<OffT>();
-  for (int r = lane; r < nrows; r += 32) meta[r] = imeta[r] = make_int2(1, 0);
-  __syncwarp();
-
-  const int n_items = p.num_items_dev ? *p.num_items_dev : p.n_items;
-
-  while (true) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(p.queue, 1);
-    item = __shfl_sync(kFull, item, 0);
-    if (item >= n_items) break;
-    const int pair = p.items ? p.items[item] : item;
-    g_pair = pair;
-    const int plen = p.p_len[pair];
-    const int tlen = p.t_len[pair];
-
-    // ---- reset the rows the previous pair left non-NULL
-    for (int r = 0; r < nrows; ++r) {
-      const int2 mt = imeta[r];
-      if (mt.x <= mt.y) null_range(row(r), mt.x, mt.y, lane, rb, g_pair);
-    }
-    __syncwarp();
-    for (int r = lane; r < nrows; r += 32) meta[r] = imeta[r] = make_int2(1, 0);
-
-    // ---- stage sequences
-    bool ok = (plen <= p.max_len) && (tlen <= p.max_len);
-    if (ok) {
-      ok &= stage_sequence<ENC>(p.seqs + p.p_off[pair], plen, P, lane);
-      ok &= stage_sequence<ENC>(p.seqs + p.t_off[pair], tlen, T, lane);
-    }
-    if (!ok) {
-      if (lane == 0) {
-        if (p.final_pass) {
-          p.status[pair] = kStOOM;
-          p.scores[pair] = 0;
-          if (CIGAR) p.ops_len[pair] = 0;
-        } else {
-          p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
-        }
-      }
-      __syncwarp();
-      continue;
-    }
-
-    // ---- score 0 (wavefront/wavefront_aligner.c:311-382): M[0][0] = 0, slot
-    // 0, extended at once (every later M cell is extended as it is computed);
-    // an alignment that begins in a gap component has offset 0 there and no M
-    const int cb = p.comp_begin ? p.comp_begin[pair] : 0;
-    const int ce = p.comp_end ? p.comp_end[pair] : 0;
-    const int rowI1 = pen.R, rowD1 = pen.R + pen.RI1;
-    const int rowI2 = pen.R + 2 * pen.RI1, rowD2 = rowI2 + pen.RI2;
-    // ring row of component c for the current slots (cur1: I1/D1, cur2: I2/D2)
-    auto comp_row = [&](int c, int cM, int c1, int c2) -> int {
-      return c == 0 ? cM : c == 1 ? rowI1 + c1 : c == 2 ? rowD1 + c1 : c == 3 ? rowI2 + c2 : rowD2 + c2;
-    };
-    const int L0 = cb == 0 ? lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair) : 0;
-    if (lane == 0) {
-      const int r0 = comp_row(cb, 0, 0, 0);
-      RING_ST(row(r0), 0, (OffT)L0);
-      meta[r0] = imeta[r0] = make_int2(0, 0);
-      if (CIGAR) table[0] = BtRow{0, 0, 0};
-    }
-    __syncwarp();
-
-    int s = 0;
-    int curM = 0, cur1 = 0, cur2 = 0;  // ring slots of score s
-    int null_steps = 0;
-    int steps_wait = p.h_steps;  // wf-adaptive (wavefront/wavefront_heuristic.c:114-121)
-    int64_t cursor = 0;  // choice bytes used (slice)
-    int nblk = 0, cur_blk = -1;  // pool: blocks held, block being filled
-    int64_t blk_off = 0, pool_used = 0;
-    int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable, 4 guard
-    const int k_end = tlen - plen;
-    int mlo = cb == 0 ? 0 : 1, mhi = 0;  // trimmed limits of M[s]
-    bool m_exists = (cb == 0);
-
-    while (true) {
-      // ================= termination on the extended M[s], or on the end
-      // component (wavefront/wavefront_termination.c:37-108); checked only
-      // where M[s] exists (wavefront/wavefront_extend.c:93-106)
-      if (m_exists) {
-        if (ce == 0) {
-          if (mlo <= k_end && k_end <= mhi && RING_LD(row(curM), k_end) >= tlen) {
-            result = 1;
-            break;
-          }
-        } else {
-          const int re = comp_row(ce, curM, cur1, cur2);
-          const int2 em = meta[re];
-          if (em.x <= k_end && k_end <= em.y && RING_LD(row(re), k_end) >= tlen) {
-            result = 1;
-            break;
-          }
-        }
-      } else if (null_steps > pen.R) {
-        result = 3;
-        break;
-      }
-
-      // ================= wf-adaptive cut-off of the extended M[s]
-      // (wavefront/wavefront_heuristic.c:229-289, :506-566): only the limits
-      // of M[s] (and, intersected, of its I/D rows) shrink; the cut offsets
-      // stay in the rows' initialised windows
-      if (HEUR && m_exists && mlo <= mhi) {
-        --steps_wait;
-        if (steps_wait <= 0 && mhi - mlo + 1 >= p.h_min_len) {
-          const OffT* const mr = row(curM);
-          auto dist = [&](int k) -> int {
-            const int32_t off = RING_LD(mr, k);
-            return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
-          };
-          int dmin = max(plen, tlen);
-          for (int k = mlo + lane; k <= mhi; k += 32) dmin = min(dmin, dist(k));
-          dmin = __reduce_min_sync(kFull, dmin);
-          const int top = min(k_end, mhi);
-          int first = INT32_MAX;
-          for (int k = mlo + lane; k < top; k += 32)
-            if (dist(k) - dmin <= p.h_max_dist) { first = k; break; }
-          first = __reduce_min_sync(kFull, first);
-          const int nlo = first == INT32_MAX ? max(mlo, top) : first;
-          const int bot = max(k_end, nlo);
-          int last = INT32_MIN;
-          for (int k = mhi - lane; k > bot; k -= 32)
-            if (dist(k) - dmin <= p.h_max_dist) { last = k; break; }
-          last = __reduce_max_sync(kFull, last);
-          const int nhi = last == INT32_MIN ? min(mhi, bot) : last;
-          steps_wait = p.h_steps;
-          if (nlo != mlo || nhi != mhi) {
-            mlo = nlo;
-            mhi = nhi;
-            if (lane == 0) {
-              meta[curM] = make_int2(nlo, nhi);
-              const int nr = A2P ? 4 : 2;
-              for (int j = 0; j < nr; ++j) {
-                const int r = j == 0 ? rowI1 + cur1 : j == 1 ? rowD1 + cur1 : j == 2 ? rowI2 + cur2 : rowD2 + cur2;
-                const int2 m = meta[r];
-                meta[r] = make_int2(max(m.x, nlo), min(m.y, nhi));
-              }
-            }
-            __syncwarp();
-          }
-        }
-      }
-
-      // ================= compute score s+1
-      ++s;
-      if (s > p.table_cap) {  // above the reference's score bound: a guard, never hit
-        result = 4;
-        break;
-      }
-      curM = (curM + 1 == pen.R) ? 0 : curM + 1;
-      cur1 = (cur1 + 1 == pen.RI1) ? 0 : cur1 + 1;
-      if (A2P) cur2 = (cur2 + 1 == pen.RI2) ? 0 : cur2 + 1;
-
-      // inputs (wavefront/wavefront_compute.c:306-352); score < 0 -> empty
-      const int sMx = ring_back(curM, pen.x, pen.R);
-      const int sMo1 = ring_back(curM, pen.o1 + pen.e1, pen.R);
-      const int sI1 = ring_back(cur1, pen.e1, pen.RI1);
-      const int2 kEmpty = make_int2(1, 0);
-      const int2 eMx = (s - pen.x >= 0) ? meta[sMx] : kEmpty;
-      const int2 eMo1 = (s - pen.o1 - pen.e1 >= 0) ? meta[sMo1] : kEmpty;
-      const int2 eI1 = (s - pen.e1 >= 0) ? meta[rowI1 + sI1] : kEmpty;
-      const int2 eD1 = (s - pen.e1 >= 0) ? meta[rowD1 + sI1] : kEmpty;
-      int sMo2 = 0, sI2 = 0;
-      int2 eMo2 = kEmpty, eI2 = kEmpty, eD2 = kEmpty;
-      if (A2P) {
-        sMo2 = ring_back(curM, pen.o2 + pen.e2, pen.R);
-        sI2 = ring_back(cur2, pen.e2, pen.RI2);
-        if (s - pen.o2 - pen.e2 >= 0) eMo2 = meta[sMo2];
-        if (s - pen.e2 >= 0) {
-          eI2 = meta[rowI2 + sI2];
-          eD2 = meta[rowD2 + sI2];
-        }
-      }
-      const bool vMx = eMx.x <= eMx.y, vMo1 = eMo1.x <= eMo1.y;
-      const bool vI1 = eI1.x <= eI1.y, vD1 = eD1.x <= eD1.y;
-      const bool vMo2 = A2P && eMo2.x <= eMo2.y;
-      const bool vI2 = A2P && eI2.x <= eI2.y, vD2 = A2P && eD2.x <= eD2.y;
-
-      OffT* const oM = row(curM);
-      OffT* const oI1 = row(rowI1 + cur1);
-      OffT* const oD1 = row(rowD1 + cur1);
-      OffT* const oI2 = A2P ? row(rowI2 + cur2) : nullptr;
-      OffT* const oD2 = A2P ? row(rowD2 + cur2) : nullptr;
-      // what a reused slot holds: its initialised window
-      const int2 oldM = imeta[curM], oldI1 = imeta[rowI1 + cur1], oldD1 = imeta[rowD1 + cur1];
-      const int2 oldI2 = A2P ? imeta[rowI2 + cur2] : kEmpty;
-      const int2 oldD2 = A2P ? imeta[rowD2 + cur2] : kEmpty;
-
-      // wavefront/wavefront_compute_affine.c:236-243: all inputs null -> null step
-      if (!(vMx | vMo1 | vI1 | vD1 | vMo2 | vI2 | vD2)) {
-        ++null_steps;
-        clear_outside(oM, oldM, 1, 0, lane, rb, g_pair);
-        clear_outside(oI1, oldI1, 1, 0, lane, rb, g_pair);
-        clear_outside(oD1, oldD1, 1, 0, lane, rb, g_pair);
-        if (A2P) {
-          clear_outside(oI2, oldI2, 1, 0, lane, rb, g_pair);
-          clear_outside(oD2, oldD2, 1, 0, lane, rb, g_pair);
-        }
-        __syncwarp();
-        if (lane == 0) {
-          meta[curM] = imeta[curM] = kEmpty;
-          meta[rowI1 + cur1] = imeta[rowI1 + cur1] = kEmpty;
-          meta[rowD1 + cur1] = imeta[rowD1 + cur1] = kEmpty;
-          if (A2P) {
-            meta[rowI2 + cur2] = imeta[rowI2 + cur2] = kEmpty;
-            meta[rowD2 + cur2] = imeta[rowD2 + cur2] = kEmpty;
-          }
-        }
-        if (CIGAR) {
-          if (s >= p.table_cap) {
-            result = -1;
-            break;
-          }
-          if (lane == 0 && CHK(s < p.table_cap, 32, s)) table[s] = BtRow{-1, 0, -1};
-        }
-        __syncwarp();
-        m_exists = false;
-        if (s >= p.max_steps) {
-          result = 2;
-          break;
-        }
-        continue;
-      }
-      null_steps = 0;
-
-      // wavefront/wavefront_compute.c:40-87: output range
-      int lo = INT32_MAX, hi = INT32_MIN;
-      if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
-      if (vMo1) { lo = min(lo, eMo1.x - 1); hi = max(hi, eMo1.y + 1); }
-      if (vI1) { lo = min(lo, eI1.x + 1); hi = max(hi, eI1.y + 1); }
-      if (vD1) { lo = min(lo, eD1.x - 1); hi = max(hi, eD1.y - 1); }
-      if (A2P) {
-        if (vMo2) { lo = min(lo, eMo2.x - 1); hi = max(hi, eMo2.y + 1); }
-        if (vI2) { lo = min(lo, eI2.x + 1); hi = max(hi, eI2.y + 1); }
-        if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
-      }
-      const int width = hi - lo + 1;
-      if (CIGAR && (s >= p.table_cap || (!pooled && cursor + width > p.bits_cap))) {
-        result = -1;
-        break;
-      }
-      int64_t bpos = cursor;  // this row's first choice byte in the store
-      if (pooled) {
-        if (pool_used + width > p.pair_cap) {  // over the pair's back-trace budget
-          result = -1;
-          break;
-        }
-        pool_used += width;
-        if (cur_blk < 0 || blk_off + width > p.block_bytes) {
-          int b = -1;
-          if (nblk < p.max_blocks && lane == 0) b = pool_pop(p);
-          b = __shfl_sync(kFull, b, 0);
-          if (b < 0) {  // pool empty: a later pass retries the pair
-            result = -1;
-            break;
-          }
-          if (lane == 0) owned[nblk] = b;
-          ++nblk;
-          cur_blk = b;
-          blk_off = 0;
-        }
-        bpos = (int64_t)cur_blk * p.block_bytes + blk_off;
-      }
-      clear_outside(oM, oldM, lo, hi, lane, rb, g_pair);
-      clear_outside(oI1, oldI1, lo, hi, lane, rb, g_pair);
-      clear_outside(oD1, oldD1, lo, hi, lane, rb, g_pair);
-      if (A2P) {
-        clear_outside(oI2, oldI2, lo, hi, lane, rb, g_pair);
-        clear_outside(oD2, oldD2, lo, hi, lane, rb, g_pair);
-      }
-      __syncwarp();
-
-      const OffT* const rMx = vMx ? row(sMx) : null_row;
-      const OffT* const rMo1 = vMo1 ? row(sMo1) : null_row;
-      const OffT* const rI1 = vI1 ? row(rowI1 + sI1) : null_row;
-      const OffT* const rD1 = vD1 ? row(rowD1 + sI1) : null_row;
-      const OffT* const rMo2 = vMo2 ? row(sMo2) : null_row;
-      const OffT* const rI2 = vI2 ? row(rowI2 + sI2) : null_row;
-      const OffT* const rD2 = vD2 ? row(rowD2 + sI2) : null_row;
-      // The reference's back-trace reads an input within its initialised
-      // window even when the row is null (wavefront/wavefront_backtrace.c:
-      // 63-219), while the compute step reads the all-NULL row: the two
-      // differ only for an I/D row that a cut-off left with empty limits and
-      // a non-empty window.  Choice bytes then follow the back-trace.
-      auto window_row = [&](bool valid, int r, int score_back) -> const OffT* {
-        if (valid || score_back < 0) return nullptr;
-        const int2 w = imeta[r];
-        return w.x <= w.y ? row(r) : nullptr;
-      };
-      const OffT* wI1 = nullptr;
-      const OffT* wD1 = nullptr;
-      const OffT* wI2 = nullptr;
-      const OffT* wD2 = nullptr;
-      if (CIGAR && HEUR) {
-        wI1 = window_row(vI1, rowI1 + sI1, s - pen.e1);
-        wD1 = window_row(vD1, rowD1 + sI1, s - pen.e1);
-        if (A2P) {
-          wI2 = window_row(vI2, rowI2 + sI2, s - pen.e2);
-          wD2 = window_row(vD2, rowD2 + sI2, s - pen.e2);
-        }
-      }
-      const bool ghost = wI1 || wD1 || wI2 || wD2;
-      uint8_t* const brow = CIGAR ? bt + bpos - lo : nullptr;
-
-      int tloM = INT32_MAX, thiM = INT32_MIN;
-      int tloI1 = INT32_MAX, thiI1 = INT32_MIN, tloD1 = INT32_MAX, thiD1 = INT32_MIN;
-      int tloI2 = INT32_MAX, thiI2 = INT32_MIN, tloD2 = INT32_MAX, thiD2 = INT32_MIN;
-      // Software-pipelined: the next cell's inputs are loaded before the
-      // current cell is computed, so one load latency overlaps the work.
-      int32_t n_mo1_m = 0, n_mo1_p = 0, n_i1_e = 0, n_d1_e = 0, n_mx = 0;
-      int32_t n_mo2_m = 0, n_mo2_p = 0, n_i2_e = 0, n_d2_e = 0;
-      auto load_inputs = [&](int kk) {
-        n_mo1_m = RING_LD(rMo1, kk - 1);
-        n_mo1_p = RING_LD(rMo1, kk + 1);
-        n_i1_e = RING_LD(rI1, kk - 1);
-        n_d1_e = RING_LD(rD1, kk + 1);
-        n_mx = RING_LD(rMx, kk);
-        if (A2P) {
-          n_mo2_m = RING_LD(rMo2, kk - 1);
-          n_mo2_p = RING_LD(rMo2, kk + 1);
-          n_i2_e = RING_LD(rI2, kk - 1);
-          n_d2_e = RING_LD(rD2, kk + 1);
-        }
-      };
-      if (lo + lane <= hi) load_inputs(lo + lane);
-      for (int k = lo + lane; k <= hi; k += 32) {
-        const int32_t mo1_m = n_mo1_m, mo1_p = n_mo1_p, i1_e = n_i1_e, d1_e = n_d1_e, mx = n_mx;
-        const int32_t mo2_m = n_mo2_m, mo2_p = n_mo2_p, i2_e = n_i2_e, d2_e = n_d2_e;
-        if (k + 32 <= hi) load_inputs(k + 32);
-        // wavefront/wavefront_compute_affine.c:66-84
-        int32_t i1 = max(mo1_m, i1_e) + 1;
-        const int32_t d1 = max(mo1_p, d1_e);
-        const int32_t mis = mx + 1;
-        int32_t ins = i1, del = d1;
-        int32_t i2 = kNull, d2 = kNull;
-        if (A2P) {
-          // wavefront/wavefront_compute_affine2p.c:78-95
-          i2 = max(mo2_m, i2_e) + 1;
-          d2 = max(mo2_p, d2_e);
-          ins = max(i1, i2);
-          del = max(d1, d2);
-        }
-        const int32_t best = max(del, max(mis, ins));
-        const bool okM = in_bounds(best, k, plen, tlen);
-        // Trim tests (wavefront/wavefront_compute.c:579-613), simplified: a
-        // non-NULL insertion keeps its source's v <= plen, a deletion its h <= tlen
-        const bool okI1 = (uint32_t)i1 <= (uint32_t)tlen;
-        const bool okD1 = (uint32_t)(d1 - k) <= (uint32_t)plen;
-        // insertion values drift upwards from NULL: keep narrow NULLs canonical
-        if (sizeof(OffT) == 2 && i1 < 0) i1 = null_of<OffT>();
-        // extend the new M cell now (wavefront/wavefront_extend.c:86-121): the
-        // reference extends M[s] right after computing it, before score s+1
-        int32_t mext = null_of<OffT>();
-        if (okM) {
-          const int v = best - k;
-          mext = best + lcp<ENC>(P, T, v, best, min(plen - v, tlen - best), nwords, g_pair);
-        }
-        RING_ST(oM, k, (OffT)mext);
-        RING_ST(oI1, k, (OffT)i1);
-        RING_ST(oD1, k, (OffT)d1);
-        if (okM) { tloM = min(tloM, k); thiM = k; }
-        if (okI1) { tloI1 = min(tloI1, k); thiI1 = k; }
-        if (okD1) { tloD1 = min(tloD1, k); thiD1 = k; }
-        if (A2P) {
-          const bool okI2 = (uint32_t)i2 <= (uint32_t)tlen;
-          const bool okD2 = (uint32_t)(d2 - k) <= (uint32_t)plen;
-          if (sizeof(OffT) == 2 && i2 < 0) i2 = null_of<OffT>();
-          RING_ST(oI2, k, (OffT)i2);
-          RING_ST(oD2, k, (OffT)d2);
-          if (okI2) { tloI2 = min(tloI2, k); thiI2 = k; }
-          if (okD2) { tloD2 = min(tloD2, k); thiD2 = k; }
-        }
-        if (CIGAR) {
-          // M source with the reference's tie order: mismatch > D2 > D1 > I2 > I1
-          uint8_t c;
-          if (mis == best) c = kSrcX;
-          else if (A2P && d2 == best) c = kSrcD2;
-          else if (d1 == best) c = kSrcD1;
-          else if (A2P && i2 == best) c = kSrcI2;
-          else c = kSrcI1;
-          c |= (uint8_t)(i1_e >= mo1_m) << 3;
-          c |= (uint8_t)(d1_e >= mo1_p) << 4;
-          if (A2P) {
-            c |= (uint8_t)(i2_e >= mo2_m) << 5;
-            c |= (uint8_t)(d2_e >= mo2_p) << 6;
-          }
-          if (HEUR && ghost) {
-            // back-trace candidates with the cut rows' window values
-            const int32_t wi1e = wI1 ? RING_LD(wI1, k - 1) : i1_e;
-            const int32_t wd1e = wD1 ? RING_LD(wD1, k + 1) : d1_e;
-            const int32_t wi1 = max(mo1_m, wi1e) + 1, wd1 = max(mo1_p, wd1e);
-            int32_t wi2 = kNull, wd2 = kNull, wi2e = i2_e, wd2e = d2_e;
-            if (A2P) {
-              wi2e = wI2 ? RING_LD(wI2, k - 1) : i2_e;
-              wd2e = wD2 ? RING_LD(wD2, k + 1) : d2_e;
-              wi2 = max(mo2_m, wi2e) + 1;
-              wd2 = max(mo2_p, wd2e);
-            }
-            const int32_t wbest = max(max(wd1, wd2), max(mis, max(wi1, wi2)));
-            if (mis == wbest) c = kSrcX;
-            else if (A2P && wd2 == wbest) c = kSrcD2;
-            else if (wd1 == wbest) c = kSrcD1;
-            else if (A2P && wi2 == wbest) c = kSrcI2;
-            else c = kSrcI1;
-            c |= (uint8_t)(wi1e >= mo1_m) << 3;
-            c |= (uint8_t)(wd1e >= mo1_p) << 4;
-            if (A2P) {
-              c |= (uint8_t)(wi2e >= mo2_m) << 5;
-              c |= (uint8_t)(wd2e >= mo2_p) << 6;
-            }
-          }
-          if (CHK(pooled || cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
-        }
-      }
-      __syncwarp();
-      tloM = __reduce_min_sync(kFull, tloM);
-      thiM = __reduce_max_sync(kFull, thiM);
-      tloI1 = __reduce_min_sync(kFull, tloI1);
-      thiI1 = __reduce_max_sync(kFull, thiI1);
-      tloD1 = __reduce_min_sync(kFull, tloD1);
-      thiD1 = __reduce_max_sync(kFull, thiD1);
-      if (A2P) {
-        tloI2 = __reduce_min_sync(kFull, tloI2);
-        thiI2 = __reduce_max_sync(kFull, thiI2);
-        tloD2 = __reduce_min_sync(kFull, tloD2);
-        thiD2 = __reduce_max_sync(kFull, thiD2);
-      }
-      trim_fill(oM, lo, hi, tloM, thiM, lane, rb, g_pair);
-      trim_fill(oI1, lo, hi, tloI1, thiI1, lane, rb, g_pair);
-      trim_fill(oD1, lo, hi, tloD1, thiD1, lane, rb, g_pair);
-      if (A2P) {
-        trim_fill(oI2, lo, hi, tloI2, thiI2, lane, rb, g_pair);
-        trim_fill(oD2, lo, hi, tloD2, thiD2, lane, rb, g_pair);
-      }
-      __syncwarp();
-      if (lane == 0) {
-        meta[curM] = imeta[curM] = make_int2(tloM, thiM);
-        meta[rowI1 + cur1] = imeta[rowI1 + cur1] = make_int2(tloI1, thiI1);
-        meta[rowD1 + cur1] = imeta[rowD1 + cur1] = make_int2(tloD1, thiD1);
-        if (A2P) {
-          meta[rowI2 + cur2] = imeta[rowI2 + cur2] = make_int2(tloI2, thiI2);
-          meta[rowD2 + cur2] = imeta[rowD2 + cur2] = make_int2(tloD2, thiD2);
-        }
-        if (CIGAR && CHK(s < p.table_cap, 31, s)) table[s] = BtRow{bpos, lo, width};
-      }
-      if (CIGAR) {
-        if (pooled) blk_off += width;
-        else cursor += width;
-      }
-      mlo = tloM;
-      mhi = thiM;
-      m_exists = true;
-      __syncwarp();
-      // wavefront/wavefront_unialign.c:102-107
-      if (s >= p.max_steps) {
-        result = 2;
-        break;
-      }
-    }
-
-    // pool blocks go back when the pair is finished (every path below)
-    auto release_blocks = [&]() {
-      if (pooled && nblk > 0) {
-        __syncwarp();
-        if (lane == 0) pool_push(p, owned, nblk);
-        nblk = 0;
-        __syncwarp();
-      }
-    };
-
-    // ================= finish the pair (warp-uniform from here on)
-    if (result != 1) {
-      release_blocks();
-      if (lane == 0) {
-        if (result == -1 && !p.final_pass) {
-          p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
-        } else {
-          int st, sc;
-          if (result == -1) { st = kStOOM; sc = 0; }
-          else if (result == 2) { st = kStMaxSteps; sc = -p.max_steps; }
-          else if (result == 3) { st = kStPartial; sc = -s; }
-          else { st = kStUnattainable; sc = 0; }
-          p.status[pair] = st;
-          p.scores[pair] = sc;
-          if (CIGAR) p.ops_len[pair] = 0;
-        }
-      }
-      __syncwarp();
-      continue;
-    }
-    // classic score (wavefront/wavefront_compute.c:108-120)
-    const int score = (pen.match == 0) ? -s : ((-pen.match) * (plen + tlen) - s) / 2;
-    if (!CIGAR) {
-      if (lane == 0) {
-        p.scores[pair] = score;
-        p.status[pair] = kStCompleted;
-      }
-      __syncwarp();
-      continue;
-    }
-
-    // ================= back-trace over choice bytes (uniform walk), then a
-    // forward replay that re-extends the matches of every M visit
-    uint8_t* const items = pooled ? bits + owned_bytes : bits + cursor;
-    const int64_t items_cap = pooled ? p.bits_cap - owned_bytes : p.bits_cap - cursor;
-    int64_t n = 0;
-    bool bad = false;
-    bool items_full = false;  // walk items did not fit the back-trace slice
-    {
-      int st = ce;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
-      int ss = s, kk = k_end;
-      while (true) {
-        if (n + 2 > items_cap) { items_full = true; break; }
-        if (ss < 0) { bad = true; break; }
-        if (st == 0) {
-          if (lane == 0 && CHK(n < items_cap, 33, n)) items[n] = 'E';
-          ++n;
-          if (ss == 0) {
-            bad = (kk != 0) || (cb != 0);
-            break;
-          }
-        } else if (ss == 0) {
-          // the score-0 cell of an alignment that begins in a gap component
-          bad = (kk != 0) || (st != cb);
-          break;
-        }
-        if (!CHK(ss < p.table_cap, 34, ss)) { bad = true; break; }
-        const BtRow te = table[ss];
-        if (te.width <= 0 || kk < te.lo || kk - te.lo >= te.width) { bad = true; break; }
-        const int64_t bi = te.pos + (kk - te.lo);
-        if (!CHK(pooled || (bi >= 0 && bi < p.bits_cap), 35, bi)) { bad = true; break; }
-        const uint8_t c = bt[bi];
-        char op = 0;
-        if (st == 0) {
-          const int src = c & 7;
-          if (src == kSrcX) { op = 'X'; ss -= pen.x; }
-          else if (src == kSrcD1) st = 2;
-          else if (src == kSrcI1) st = 1;
-          else if (src == kSrcD2) st = 4;
-          else st = 3;
-        } else if (st == 1) {
-          op = 'I'; kk -= 1;
-          if (c & 8) ss -= pen.e1; else { ss -= pen.o1 + pen.e1; st = 0; }
-        } else if (st == 2) {
-          op = 'D'; kk += 1;
-          if (c & 16) ss -= pen.e1; else { ss -= pen.o1 + pen.e1; st = 0; }
-        } else if (st == 3) {
-          op = 'I'; kk -= 1;
-          if (c & 32) ss -= pen.e2; else { ss -= pen.o2 + pen.e2; st = 0; }
-        } else {
-          op = 'D'; kk += 1;
-          if (c & 64) ss -= pen.e2; else { ss -= pen.o2 + pen.e2; st = 0; }
-        }
-        if (op) {
-          if (lane == 0 && CHK(n < items_cap, 36, n)) items[n] = (uint8_t)op;
-          ++n;
-        }
-      }
-    }
-    __syncwarp();
-    release_blocks();  // the walk has read every choice byte it needs
-    if (items_full) {
-      // the same overflow as a full cell table: retry with a larger slice, or
-      // WF_STATUS_OOM in the final pass
-      if (lane == 0) {
-        if (!p.final_pass) {
-          p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
-        } else {
-          p.status[pair] = kStOOM;
-          p.scores[pair] = 0;
-          p.ops_len[pair] = 0;
-        }
-      }
-      __syncwarp();
-      continue;
-    }
-    int out_n = 0;
-    if (!bad) {
-      uint8_t* const out = p.ops + p.ops_off[pair];
-      int v = 0, h = 0;
-      for (int64_t i = n - 1; i >= 0; --i) {
-        const uint8_t it = items[i];
-        if (it == 'E') {
-          const int L = lcp<ENC>(P, T, v, h, min(plen - v, tlen - h), nwords, g_pair);
-          for (int j = lane; j < L; j += 32)
-            if (CHK(out_n + j < plen + tlen, 37, out_n + j)) out[out_n + j] = 'M';
-          out_n += L;
-          v += L;
-          h += L;
-        } else {
-          if (it == 'X') { bad = (v >= plen || h >= tlen); ++v; ++h; }
-          else if (it == 'I') { bad = (h >= tlen); ++h; }
-          else { bad = (v >= plen); ++v; }
-          if (bad) break;
-          if (lane == 0 && CHK(out_n < plen + tlen, 38, out_n)) out[out_n] = it;
-          ++out_n;
-        }
-      }
-      if (v != plen || h != tlen) bad = true;
-    }
-    if (lane == 0) {
-      p.status[pair] = bad ? kStUnattainable : kStCompleted;
-      p.scores[pair] = score;
-      p.ops_len[pair] = bad ? 0 : out_n;
-    }
-    __syncwarp();
-  }
-}
-
-// -------------------------------------------------------------- launchers
-#define WF2G_INST(A2P, CIG, ENC, T, H) \
-  template __global__ void wfa_align_kernel<A2P, CIG, ENC, T, H>(const KParams p);
-#define WF2G_INST_T(T, H)          \
-  WF2G_INST(false, false, 2, T, H) \
-  WF2G_INST(false, true, 2, T, H)  \
-  WF2G_INST(true, false, 2, T, H)  \
-  WF2G_INST(true, true, 2, T, H)   \
-  WF2G_INST(false, false, 8, T, H) \
-  WF2G_INST(false, true, 8, T, H)  \
-  WF2G_INST(true, false, 8, T, H)  \
-  WF2G_INST(true, true, 8, T, H)
-WF2G_INST_T(int16_t, false)
-WF2G_INST_T(int32_t, false)
-WF2G_INST_T(int16_t, true)
-WF2G_INST_T(int32_t, true)
-
-template <typename T, bool H>
+template <typename T>
 static void* pick(int a2p, int cigar, int enc) {
   if (enc == 2) {
-    if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 2, T, H> : (void*)wfa_align_kernel<false, false, 2, T, H>;
-    return cigar ? (void*)wfa_align_kernel<true, true, 2, T, H> : (void*)wfa_align_kernel<true, false, 2, T, H>;
+    if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 2, T, false, 32> : (void*)wfa_align_kernel<false, false, 2, T, false, 32>;
+    return cigar ? (void*)wfa_align_kernel<true, true, 2, T, false, 32> : (void*)wfa_align_kernel<true, false, 2, T, false, 32>;
   }
-  if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 8, T, H> : (void*)wfa_align_kernel<false, false, 8, T, H>;
-  return cigar ? (void*)wfa_align_kernel<true, true, 8, T, H> : (void*)wfa_align_kernel<true, false, 8, T, H>;
+  if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 8, T, false, 32> : (void*)wfa_align_kernel<false, false, 8, T, false, 32>;
+  return cigar ? (void*)wfa_align_kernel<true, true, 8, T, false, 32> : (void*)wfa_align_kernel<true, false, 8, T, false, 32>;
 }
 
-// Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or
-// 4-byte offsets, wf-adaptive heuristic?).
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur) {
-  if (heur) return off_bytes == 2 ? pick<int16_t, true>(a2p, cigar, enc) : pick<int32_t, true>(a2p, cigar, enc);
-  return off_bytes == 2 ? pick<int16_t, false>(a2p, cigar, enc) : pick<int32_t, false>(a2p, cigar, enc);
-}
-
-extern "C" void* wf2g_pool_init_ptr(void) { return (void*)wfa_pool_init_kernel; }
-
-// First bounds violation seen by a checked build: {site, index, pair, count}.
-extern "C" int wf2g_fault_info(unsigned long long* out) {
-#ifdef WF2G_CHECKED
-  return (int)cudaMemcpyFromSymbol(out, g_fault, 4 * sizeof(unsigned long long));
-#else
-  for (int i = 0; i < 4; ++i) out[i] = 0;
-  return 0;
-#endif
-}
-
-// Bytes of both staged sequences of one warp for an encoding and length bound.
-extern "C" int wf2g_seq_bytes(int enc, int max_len) {
-  return enc == 2 ? 2 * Seq<2>::words(max_len) * 4 : 2 * Seq<8>::words(max_len) * 8;
-}
+WF2G_FAULT_READER(wf2g_fault_info_exact)
 
 }  // namespace wf2g
+
+extern "C" void* wf2g_kernel_ptr_heur(int a2p, int cigar, int enc, int off_bytes);
+extern "C" void* wf2g_kernel_ptr_wide(int a2p, int enc, int off_bytes, int heur);
+extern "C" int wf2g_fault_info_exact(unsigned long long* out);
+extern "C" int wf2g_fault_info_heur(unsigned long long* out);
+extern "C" int wf2g_fault_info_wide(unsigned long long* out);
+
+// Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or
+// 4-byte offsets, wf-adaptive heuristic?, a CTA per pair?).  The CTA-per-pair
+// variants exist for full-CIGAR runs only.
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide) {
+  if (wide) return cigar ? wf2g_kernel_ptr_wide(a2p, enc, off_bytes, heur) : nullptr;
+  if (heur) return wf2g_kernel_ptr_heur(a2p, cigar, enc, off_bytes);
+  return off_bytes == 2 ? wf2g::pick<int16_t>(a2p, cigar, enc) : wf2g::pick<int32_t>(a2p, cigar, enc);
+}
+
+extern "C" void* wf2g_pool_init_ptr(void) { return (void*)wf2g::wfa_pool_init_kernel; }
+
+// First bounds violation seen by a checked build: {site, index, pair, count}
+// (the first unit that recorded one; counts add up).
+extern "C" int wf2g_fault_info(unsigned long long* out) {
+  int (*const readers[3])(unsigned long long*) = {wf2g_fault_info_exact, wf2g_fault_info_heur,
+                                                  wf2g_fault_info_wide};
+  for (int i = 0; i < 4; ++i) out[i] = 0;
+  for (int r = 0; r < 3; ++r) {
+    unsigned long long f[4];
+    const int rc = readers[r](f);
+    if (rc) return rc;
+    if (out[0] == 0 && f[0] != 0) {
+      out[0] = f[0];
+      out[1] = f[1];
+      out[2] = f[2];
+    }
+    out[3] += f[3];
+  }
+  return 0;
+}
+
+// Bytes of both staged sequences of one group for an encoding and length bound.
+extern "C" int wf2g_seq_bytes(int enc, int max_len) {
+  return enc == 2 ? 2 * wf2g::Seq<2>::words(max_len) * 4 : 2 * wf2g::Seq<8>::words(max_len) * 8;
+}

@@ -42,6 +42,9 @@ struct BtRow {
 };
 constexpr int kBtRowBytes = (int)sizeof(BtRow);
 
+// Shared memory a CTA-per-pair group adds for its cross-warp reductions.
+constexpr int kGroupRedBytes = 1024;
+
 struct Penalties {
   int match;  // user match (<= 0)
   int x, o1, e1, o2, e2;  // internal (possibly Eizenga-transformed) penalties
@@ -86,9 +89,9 @@ struct KParams {
   int row_stride;     // ring row length (elements), >= 2*max_len+6
   int kofs;           // diagonal k lives at element k+kofs of a row
   int seq_in_smem;    // 1: staged sequences in shared memory, 0: in gscratch
-  int smem_per_warp;  // bytes
+  int smem_per_group;  // bytes
   uint8_t* gscratch;  // per-warp global slices
-  int64_t gscratch_per_warp;
+  int64_t gscratch_per_group;
   // per-warp slice: [ring: (nrows+1) rows][sequences if !seq_in_smem][table][bits]
   int64_t ring_bytes;
   int64_t seq_bytes;

@@ -21,7 +21,7 @@
 #include "wfa_kernels.cuh"
 
 namespace wf2g {
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur);
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 }  // namespace wf2g
 
@@ -131,25 +131,25 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.ring_bytes = (((int64_t)(nrows + 1) * kp.row_stride * 2) + 255) & ~int64_t(255);
   const int seq_bytes = wf2g_seq_bytes(8, L);
   kp.seq_in_smem = 1;
-  kp.smem_per_warp = (int)(((int64_t)seq_bytes + (int64_t)nrows * 16 + 15) & ~int64_t(15));
+  kp.smem_per_group = (int)(((int64_t)seq_bytes + (int64_t)nrows * 16 + 15) & ~int64_t(15));
   kp.bits_cap = cigar ? kNoAllocBitsPerWarp : 0;
-  kp.gscratch_per_warp =
+  kp.gscratch_per_group =
       (kp.ring_bytes + (cigar ? (int64_t)kp.table_cap * kBtRowBytes + kp.bits_cap : 0) + 255) &
       ~int64_t(255);
 
   // the array: [control: 256 bytes][per-warp slices]
   const int64_t avail = (int64_t)kNoAllocBytes - 256;
-  const int64_t warps_fit = avail / kp.gscratch_per_warp;
+  const int64_t warps_fit = avail / kp.gscratch_per_group;
   if (warps_fit < 1) {
     fprintf(stderr,
             "[wfa2gpu] wavefront_align_batch_device_noalloc: one warp's scratch (%lld bytes) "
             "exceeds the fixed %zu-byte array for these penalties\n",
-            (long long)kp.gscratch_per_warp, kNoAllocBytes);
+            (long long)kp.gscratch_per_group, kNoAllocBytes);
     return -3;  // WF2G_ERR_ARGS
   }
   int wpc = (int)std::min<int64_t>(8, warps_fit);
-  const size_t smem = (size_t)kp.smem_per_warp * wpc;
-  if (smem > 48 * 1024) wpc = std::max(1, (int)((48 * 1024) / kp.smem_per_warp));
+  const size_t smem = (size_t)kp.smem_per_group * wpc;
+  if (smem > 48 * 1024) wpc = std::max(1, (int)((48 * 1024) / kp.smem_per_group));
   int blocks = (int)std::min<int64_t>(warps_fit / wpc, ((int64_t)n + wpc - 1) / wpc);
   blocks = std::max(blocks, 1);
   int32_t* const queue = (int32_t*)base;  // the only value that must start at zero
@@ -157,10 +157,10 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.gscratch = base + 256;
   // calls share the array: clear the queue head left by the previous call
   if (cudaMemsetAsync(queue, 0, sizeof(int32_t), st) != cudaSuccess) return -4;
-  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur);
+  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur, 0);
   void* args[] = {(void*)&kp};
   const cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args,
-                                         (size_t)kp.smem_per_warp * wpc, st);
+                                         (size_t)kp.smem_per_group * wpc, st);
   if (e != cudaSuccess) {
     fprintf(stderr, "[wfa2gpu] no-alloc launch failed: %s\n", cudaGetErrorString(e));
     return -4;  // WF2G_ERR_CUDA
