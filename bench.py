@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "wfa2-lib_gb300"))
 
 METRIC = "pairs/s bit-exact score+CIGAR, batched vs per-pair on 1 GB300; p50/p99 latency"
-INT_OPS_PER_CELL = {3: 20, 4: 32}  # int32 ops per WFA cell: gap-affine, gap-affine-2p
+INT_OPS_PER_CELL = {3: 20, 4: 25}  # int32 ops per WFA cell: gap-affine, gap-affine-2p
 INT_OPS_PER_EXT_WORD = 8   # per additional 32-base extend word
 MEM_HIGH, MEM_ULTRALOW = 0, 3
 
@@ -69,9 +69,16 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="target wall time of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--fixed", default="",
+                    help="L:D -- instead of the config's pairs, pairs of fixed length L with "
+                         "D per-mille uniform edits (generator workload 5; small profiling cases)")
     a = ap.parse_args()
     c = CONFIGS[a.config]
     a.workload = c["workload"]
+    a.param = a.param2 = 0
+    if a.fixed:
+        a.workload = 5
+        a.param, a.param2 = (int(x) for x in a.fixed.split(":"))
     a.metric = c["metric"]
     a.memory = c["memory"]
     a.pairs = a.pairs or c["pairs"]
@@ -140,11 +147,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def gen_pinned(W, torch, workload, n, first):
+def gen_pinned(W, torch, workload, n, first, param=0, param2=0):
     """Seeded pairs in pinned host memory."""
     def alloc(nbytes):
         return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
-    p = W.generate(workload, n, first=first, alloc=alloc)
+    p = W.generate(workload, n, first=first, param=param, param2=param2, alloc=alloc)
 
     def pin(a):
         t = torch.empty(a.shape, dtype={np.int64: torch.int64, np.int32: torch.int32}[a.dtype.type],
@@ -160,7 +167,7 @@ def cpu_sample(O, W, args, target_s, first, kind):
     pen = O.Penalties(metric=args.metric)
     n = CONFIGS[args.config]["cpu_n"]
     while True:
-        p = W.generate(args.workload, n, first=first)
+        p = W.generate(args.workload, n, first=first, param=args.param, param2=args.param2)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
         t0 = time.perf_counter()
         r = O.align(b, pen, memory_mode=args.memory, score_only=args.score_only, kind=kind,
@@ -206,9 +213,12 @@ def workload_config(args):
     c = CONFIGS[args.config]
     pen = "gap-affine-2p(0,4,6,2,24,1)" if args.metric == 4 else "gap-affine(0,4,6,2)"
     mem = "ultralow (BiWFA)" if args.memory == MEM_ULTRALOW else "high"
+    name = c["name"]
+    if args.fixed:
+        name = f"fixed length {args.param}, {args.param2 / 10:g}% uniform edits"
     return {"workload": f"config {args.config}: batched {pen} end-to-end "
                         f"{'score-only' if args.score_only else 'full CIGAR'}, memory {mem}, "
-                        f"{args.pairs} pairs/GPU of workload {args.workload} ({c['name']})",
+                        f"{args.pairs} pairs/GPU of workload {args.workload} ({name})",
             "pairs_per_gpu": args.pairs, "seq": "uint8 ASCII ACGT",
             "l2": "inputs larger than L2 (126 MB) at the default sizes; no flush needed",
             "parallelism": f"replicas x{args.gpus} (pairs sharded, no collective)"}
@@ -357,7 +367,7 @@ def main():
     # ------------------------------------------------------------ data
     n = args.pairs
     first = rank * n
-    p = gen_pinned(W, torch, args.workload, n, first)
+    p = gen_pinned(W, torch, args.workload, n, first, args.param, args.param2)
     max_len = p.max_len
     cigar = not args.score_only
     cap = p.p_len.astype(np.int64) + p.t_len.astype(np.int64)

@@ -394,6 +394,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     g_pair = pair;
     const int plen = p.p_len[pair];
     const int tlen = p.t_len[pair];
+    if (p.wide_min_len > 0 && max(plen, tlen) >= p.wide_min_len) {
+      if (t == 0) p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
+      group_sync<G>();
+      continue;
+    }
 
     // ---- reset the rows the previous pair left non-NULL
     for (int r = 0; r < nrows; ++r) {

@@ -244,6 +244,9 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   k.retry_count = counters + 4;
   Pass p{2, 0, int64_t(1) << 20, 8, 0, 0};
   if (cigar) p.bits_cap = std::min(p.bits_cap, need);
+  // long pairs would overflow the 1 MB slice after computing that much: they
+  // go straight to the CTA-per-pair passes
+  if (cigar) k.wide_min_len = env_int("WF2G_WIDE_MIN_LEN", 4096);
   int rc = run_pass(E, cfg, k, p, n, E->scratch1, st);
   if (rc) return rc;
   if (!cigar) {

@@ -107,6 +107,9 @@ struct KParams {
   int32_t* pool_lock;   // 0 free, 1 held
   int max_blocks;       // blocks one pair may hold
   int64_t pair_cap;     // choice bytes one pair may use (its back-trace budget)
+  // a pass with a retry list sends pairs this long or longer (either
+  // sequence) straight to it: the CTA-per-pair passes take them (0: off)
+  int wide_min_len;
 };
 
 }  // namespace wf2g
