@@ -8,6 +8,9 @@ calling convention:
                    reference algorithm (wfa_oracle.c); builds on any host.
 * ``reference`` -- oracle/_ref/libwfa_ref.so, the unmodified reference library
                    compiled from its sources (only where they are present).
+* ``reference_scalar`` -- the same built without host tuning, so its portable
+                   extension kernels run (the aarch64 behaviour; the x86 AVX
+                   kernels resolve ends-free termination ties differently).
 """
 from __future__ import annotations
 
@@ -21,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libwfa_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libwfa_ref.so")
+REF_SCALAR_LIB = os.path.join(HERE, "_ref", "libwfa_ref_scalar.so")
 
 GAP_AFFINE = 3
 GAP_AFFINE_2P = 4
@@ -39,14 +43,23 @@ class Penalties:
     gap_opening2: int = 24
     gap_extension2: int = 1
 
-    def cfg(self, memory_mode=MEM_HIGH, score_only=False, max_steps=0, wfadaptive=None):
+    def cfg(self, memory_mode=MEM_HIGH, score_only=False, max_steps=0, wfadaptive=None,
+            form=None):
         """wfadaptive: None, or (min_wavefront_length, max_distance_threshold,
-        steps_between_cutoffs) of the wf-adaptive heuristic."""
+        steps_between_cutoffs) of the wf-adaptive heuristic.
+        form: None (end-to-end), "extension", or the ends-free lengths
+        (pattern_begin_free, pattern_end_free, text_begin_free, text_end_free)."""
         h = [1, *wfadaptive] if wfadaptive else [0, 0, 0, 0]
+        if form is None:
+            f = [0, 0, 0, 0, 0, 0]
+        elif form == "extension":
+            f = [1, 0, 0, 0, 0, 1]
+        else:
+            f = [1, *form, 0]
         return np.array(
             [self.metric, self.match, self.mismatch, self.gap_opening1, self.gap_extension1,
              self.gap_opening2, self.gap_extension2, memory_mode, int(bool(score_only)),
-             max_steps, *h], dtype=np.int32)
+             max_steps, *h, *f], dtype=np.int32)
 
 
 def build(ref: bool = False) -> None:
@@ -60,13 +73,13 @@ _LIBS = {}
 def _lib(kind: str):
     if kind in _LIBS:
         return _LIBS[kind]
-    path = PORT_LIB if kind == "port" else REF_LIB
+    path = {"port": PORT_LIB, "reference": REF_LIB, "reference_scalar": REF_SCALAR_LIB}[kind]
     if not os.path.exists(path):
-        build(ref=(kind == "reference"))
+        build(ref=(kind != "port"))
     lib = ctypes.CDLL(path)
     fn = lib.oracle_align_batch if kind == "port" else lib.ref_align_batch
     P = ctypes.c_void_p
-    fn.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+    fn.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
     fn.restype = ctypes.c_int
     _LIBS[kind] = fn
     return fn
@@ -132,6 +145,7 @@ class AlignResult:
     ops_len: np.ndarray
     cells: np.ndarray
     ext: np.ndarray
+    end: np.ndarray = None  # (n, 2) int32: cigar->end_v, cigar->end_h
 
     def cigar(self, i) -> str:
         o = int(self.ops_off[i])
@@ -139,10 +153,10 @@ class AlignResult:
 
 
 def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=False,
-          max_steps=0, kind="port", nthreads=0, wfadaptive=None) -> AlignResult:
+          max_steps=0, kind="port", nthreads=0, wfadaptive=None, form=None) -> AlignResult:
     fn = _lib(kind)
     n = batch.n
-    cfg = pen.cfg(memory_mode, score_only, max_steps, wfadaptive)
+    cfg = pen.cfg(memory_mode, score_only, max_steps, wfadaptive, form)
     score = np.zeros(n, np.int32)
     status = np.zeros(n, np.int32)
     ops_off = batch.ops_offsets()
@@ -150,16 +164,17 @@ def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=Fal
     ops_len = np.zeros(n, np.int32)
     cells = np.zeros(n, np.int64)
     ext = np.zeros(n, np.int64)
+    end = np.zeros((n, 2), np.int32)
 
     def ptr(a):
         return a.ctypes.data_as(ctypes.c_void_p)
 
     rc = fn(ptr(cfg), n, ptr(batch.seqs), ptr(batch.p_off), ptr(batch.p_len), ptr(batch.t_off),
             ptr(batch.t_len), ptr(score), ptr(status), ptr(ops), ptr(ops_off), ptr(ops_len),
-            ptr(cells), ptr(ext), int(nthreads))
+            ptr(cells), ptr(ext), ptr(end), int(nthreads))
     if rc != 0:
         raise ValueError("invalid configuration for the CPU checker")
-    return AlignResult(score, status, ops, ops_off, ops_len, cells, ext)
+    return AlignResult(score, status, ops, ops_off, ops_len, cells, ext, end)
 
 
 # ---------------------------------------------------------------- formats

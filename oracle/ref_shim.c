@@ -23,7 +23,7 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
                     const int32_t* p_len, const int64_t* t_off, const int32_t* t_len,
                     int32_t* out_score, int32_t* out_status, char* out_ops,
                     const int64_t* ops_off, int32_t* out_ops_len, int64_t* out_cells,
-                    int64_t* out_ext, int nthreads) {
+                    int64_t* out_ext, int32_t* out_end, int nthreads) {
   (void)out_cells;
   (void)out_ext;
   wavefront_aligner_attr_t attr = wavefront_aligner_attr_default;
@@ -53,6 +53,16 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
     attr.heuristic.steps_between_cutoffs = cfg[13];
   }
   if (cfg[9] > 0) attr.system.max_alignment_steps = cfg[9];
+  if (cfg[14] == 1) {
+    attr.alignment_form.span = alignment_endsfree;
+    attr.alignment_form.pattern_begin_free = cfg[15];
+    attr.alignment_form.pattern_end_free = cfg[16];
+    attr.alignment_form.text_begin_free = cfg[17];
+    attr.alignment_form.text_end_free = cfg[18];
+    attr.alignment_form.extension = cfg[19] != 0;
+    /* the reference exits on ends-free values longer than a sequence
+     * (wavefront/wavefront_align.c:90-101): such pairs are not handed to it */
+  }
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel num_threads(nthreads)
@@ -64,11 +74,24 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
 #pragma omp for schedule(dynamic, 16)
 #endif
     for (int i = 0; i < num_pairs; ++i) {
+      if (cfg[14] == 1 && !cfg[19] &&
+          (cfg[15] > p_len[i] || cfg[16] > p_len[i] || cfg[17] > t_len[i] || cfg[18] > t_len[i])) {
+        out_status[i] = -400; /* ORACLE_STATUS_INVALID_FORM */
+        out_score[i] = 0;
+        out_ops_len[i] = 0;
+        if (out_end) out_end[2 * i] = out_end[2 * i + 1] = -1;
+        continue;
+      }
       wavefront_align(wf, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i]);
       out_status[i] = wf->align_status.status;
       cigar_t* const cg = wf->cigar;
       out_score[i] = cg->score;
-      if (!cfg[8] && out_ops != NULL && wf->align_status.status == 0) {
+      if (out_end) {
+        out_end[2 * i] = cg->end_v;
+        out_end[2 * i + 1] = cg->end_h;
+      }
+      if (!cfg[8] && out_ops != NULL &&
+          (wf->align_status.status == 0 || wf->align_status.status == 1)) {
         const int n = cg->end_offset - cg->begin_offset;
         memcpy(out_ops + ops_off[i], cg->operations + cg->begin_offset, (size_t)n);
         out_ops_len[i] = n;

@@ -49,6 +49,12 @@ static int imax(int a, int b) { return a > b ? a : b; }
 static int setup_penalties(const int* cfg, pen_t* p) {
   p->metric = cfg[0];
   const int m = cfg[1], x = cfg[2], o1 = cfg[3], e1 = cfg[4], o2 = cfg[5], e2 = cfg[6];
+  p->um = m;
+  p->ux = x;
+  p->uo1 = o1;
+  p->ue1 = e1;
+  p->uo2 = o2;
+  p->ue2 = e2;
   if (p->metric != 3 && p->metric != 4) return -1;
   if (m > 0 || x <= 0 || o1 < 0 || e1 <= 0) return -1;
   if (p->metric == 4 && (o2 < 0 || e2 <= 0)) return -1;
@@ -82,6 +88,17 @@ static int setup_penalties(const int* cfg, pen_t* p) {
   p->h_min_len = cfg[11];
   p->h_max_dist = cfg[12];
   p->h_steps = cfg[13];
+  /* alignment form (wavefront/wavefront_attributes.h:55-69) */
+  p->endsfree = cfg[14] == 1;
+  p->pbf = cfg[15];
+  p->pef = cfg[16];
+  p->tbf = cfg[17];
+  p->tef = cfg[18];
+  p->extension = p->endsfree && cfg[19] != 0;
+  if (p->endsfree && (p->pbf < 0 || p->pef < 0 || p->tbf < 0 || p->tef < 0)) return -1;
+  /* with match < 0 a begin-free run also re-enters at every score that is a
+   * multiple of -match (wavefront/wavefront_compute.c:124-262): not restated */
+  if (p->endsfree && !p->extension && p->match != 0 && (p->pbf > 0 || p->tbf > 0)) return -1;
   return 0;
 }
 
@@ -381,7 +398,12 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
   int32_t offset = off_end;
   int h = offset, v = offset - k;
   const int a2p = (p->metric == 4);
-  /* end-to-end: v==plen, h==tlen, so no trailing gaps (wavefront/wavefront_backtrace.c:356-365) */
+  /* ending deletions, then insertions: the free end of an ends-free alignment
+   * (wavefront/wavefront_backtrace.c:346-356); none end-to-end (v==plen, h==tlen) */
+  if (comp_end == C_M) {
+    for (int i = plen - v; i > 0; --i) rev[n++] = 'D';
+    for (int i = tlen - h; i > 0; --i) rev[n++] = 'I';
+  }
   while (v > 0 && h > 0 && s > 0) {
     const int sx = s - p->x, so1 = s - p->o1 - p->e1, so2 = s - p->o2 - p->e2;
     const int se1 = s - p->e1, se2 = s - p->e2;
@@ -499,6 +521,10 @@ void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const cha
   ua->ext = 0;
   ua->heur = p->heur;
   ua->steps_wait = p->h_steps;
+  ua->endsfree = 0;
+  ua->pbf = ua->pef = ua->tbf = ua->tef = 0;
+  ua->end_k = tlen - plen;
+  ua->end_off = tlen;
   ws_reset(ws);
   ws_ensure_rows(ws, 0);
   if (ws->modular) memset(ws->rows, 0, (size_t)ws->scope * NCOMP * sizeof(orow_t));
@@ -514,6 +540,38 @@ void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const cha
   r0->exists = 1;
   r0->lo = r0->hi = r0->ilo = r0->ihi = 0;
   r0->off[0] = 0;
+}
+
+/* Ends-free start (wavefront/wavefront_aligner.c:250-305): with match 0 the
+ * score-0 M wavefront spans [-pattern_begin_free, text_begin_free], diagonal
+ * k > 0 starting at (v,h) = (0,k) and k < 0 at (-k,0).  Its initialised window
+ * stays [0,0]: compute steps NULL-pad only beyond max(window, limits)
+ * (wavefront/wavefront_compute.c:498-527), so the oracle keeps the limits as
+ * its window, which reads the same. */
+void oracle_ua_start_endsfree(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const char* P,
+                              int plen, const char* T, int tlen, int pbf, int pef, int tbf,
+                              int tef) {
+  oracle_ua_start(ua, ws, p, P, plen, T, tlen, C_M, C_M);
+  ua->endsfree = 1;
+  ua->pbf = pbf;
+  ua->pef = pef;
+  ua->tbf = tbf;
+  ua->tef = tef;
+  const int lo = p->match == 0 ? -pbf : 0;
+  const int hi = p->match == 0 ? tbf : 0;
+  if (lo == 0 && hi == 0) return;
+  ws_reset(ws);
+  ws->hlo = lo - (p->scope + 1);
+  ws->hhi = hi + p->scope + 1;
+  kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
+  kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
+  orow_t* r0 = row_at(ws, 0, C_M);
+  r0->off = row_storage(ws, 0, C_M, ws->hlo, ws->hhi);
+  r0->exists = 1;
+  r0->null = 0;
+  r0->lo = r0->ilo = lo;
+  r0->hi = r0->ihi = hi;
+  for (int k = lo; k <= hi; ++k) r0->off[k] = k > 0 ? k : 0;
 }
 
 /* wf-adaptive cut-off of M[s] after its extension
@@ -592,6 +650,23 @@ int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
     ua->ext += L;
     const int ak = 2 * (off + L) - k;
     if (mak < ak) mak = ak;
+    /* ends-free: the first diagonal, in extension order, that reaches the end
+     * of one sequence with the other's rest within its end-free length
+     * (wavefront/wavefront_extend_kernels.c:154-194,
+     * wavefront/wavefront_termination.c:115-162) */
+    if (ua->endsfree) {
+      const int h = off + L, v = off + L - k;
+      if ((h >= ua->tlen && ua->plen - v <= ua->pef) || (v >= ua->plen && ua->tlen - h <= ua->tef)) {
+        ua->end_k = k;
+        ua->end_off = off + L;
+        return ST_END_REACHED;
+      }
+    }
+  }
+  if (ua->endsfree) {
+    if (ua->heur) wfadaptive_cutoff(ua);
+    if (max_ak) *max_ak = mak;
+    return 0;
   }
   const orow_t* e = row_at(ws, ua->s, ua->ce);
   const int k_end = ua->k_end;
@@ -613,7 +688,7 @@ void oracle_ua_compute(oracle_ua_t* ua) {
  * number of operations or -1. */
 int oracle_ua_backtrace(oracle_ua_t* ua, char* ops) {
   char* rev = (char*)malloc((size_t)(ua->plen + ua->tlen + 8));
-  const int n = backtrace(ua->ws, ua->p, ua->plen, ua->tlen, ua->s, ua->k_end, ua->tlen, ua->ce,
+  const int n = backtrace(ua->ws, ua->p, ua->plen, ua->tlen, ua->s, ua->end_k, ua->end_off, ua->ce,
                           rev);
   if (n >= 0)
     for (int i = 0; i < n; ++i) ops[i] = rev[n - 1 - i];
@@ -625,12 +700,118 @@ int oracle_classic_score(const pen_t* p, int plen, int tlen, int s) {
   return classic_score(p, plen, tlen, s);
 }
 
+/* Score of an operation run under the user's penalties, as maximal-score
+ * trimming counts it (alignment/cigar_utils.c:112-318: a match earns -match,
+ * or 1 when match is 0). */
+static int run_score_affine2p(const pen_t* p, char op, int len, int* ev, int* eh) {
+  switch (op) {
+    case 'M': *ev += len; *eh += len; return (p->um != 0 ? p->um : -1) * len;
+    case 'X': *ev += len; *eh += len; return p->ux * len;
+    case 'D': {
+      *ev += len;
+      const int a = p->uo1 + p->ue1 * len, b = p->uo2 + p->ue2 * len;
+      return a < b ? a : b;
+    }
+    default: {
+      *eh += len;
+      const int a = p->uo1 + p->ue1 * len, b = p->uo2 + p->ue2 * len;
+      return a < b ? a : b;
+    }
+  }
+}
+
+/* Maximal-score trimming of ops[0..*n) (alignment/cigar_utils.c:112-318,
+ * dispatch wavefront/wavefront_aligner.c:664-676).  On return *n, *score and
+ * *ev/*eh describe the kept prefix (an empty prefix: *n = 0, score INT32_MIN,
+ * end (-1,-1), as cigar_clear leaves them); returns 1 if the CIGAR was trimmed. */
+static int maxtrim(const pen_t* p, const char* ops, int* n, int* score, int* ev, int* eh) {
+  const int len = *n;
+  int max_score = 0, max_off = 0, max_v = 0, max_h = 0;
+  int sc = 0, v = 0, h = 0;
+  if (p->metric == 4) {
+    if (len <= 0) return 0;
+    char last = 0;
+    int run = 0;
+    for (int i = 0; i < len; ++i) {
+      if (ops[i] != last && last != 0) {
+        sc -= run_score_affine2p(p, last, run, &v, &h);
+        run = 0;
+        if (max_score < sc) {
+          max_score = sc;
+          max_off = i - 1;
+          max_v = v;
+          max_h = h;
+        }
+      }
+      last = ops[i];
+      ++run;
+    }
+    sc -= run_score_affine2p(p, last, run, &v, &h);
+    if (max_score < sc) {
+      max_score = sc;
+      max_off = len - 1;
+      max_v = v;
+      max_h = h;
+    }
+  } else {
+    const int mscore = p->um != 0 ? p->um : -1;
+    char last = 0;
+    for (int i = 0; i < len; ++i) {
+      switch (ops[i]) {
+        case 'M': sc -= mscore; ++v; ++h; break;
+        case 'X': sc -= p->ux; ++v; ++h; break;
+        case 'I': sc -= p->ue1 + (last == 'I' ? 0 : p->uo1); ++h; break;
+        default: sc -= p->ue1 + (last == 'D' ? 0 : p->uo1); ++v; break;
+      }
+      last = ops[i];
+      if (max_score < sc) {
+        max_score = sc;
+        max_off = i;
+        max_v = v;
+        max_h = h;
+      }
+    }
+  }
+  const int trimmed = (max_off != len - 1);
+  if (max_score == 0) {
+    *n = 0;
+    *score = INT32_MIN;
+    *ev = -1;
+    *eh = -1;
+  } else {
+    *n = max_off + 1;
+    *score = max_score;
+    *ev = max_v;
+    *eh = max_h;
+  }
+  return trimmed;
+}
+
 /* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273). */
 void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
                       int tlen, int32_t* out_score, int32_t* out_status, char* ops,
-                      int32_t* ops_len, int64_t* cells, int64_t* ext) {
+                      int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end) {
+  int32_t end_dummy[2];
+  if (!end) end = end_dummy;
+  end[0] = end[1] = -1;
   oracle_ua_t ua;
-  oracle_ua_start(&ua, ws, p, P, plen, T, tlen, C_M, C_M);
+  if (p->endsfree) {
+    /* extension presets (wavefront/wavefront_align.c:57-63), then the bounds
+     * check of :90-101 (the reference exits there) */
+    const int pbf = p->extension ? 0 : p->pbf, pef = p->extension ? plen : p->pef;
+    const int tbf = p->extension ? 0 : p->tbf, tef = p->extension ? tlen : p->tef;
+    if (pbf > plen || pef > plen || tbf > tlen || tef > tlen) {
+      if (cells) *cells = 0;
+      if (ext) *ext = 0;
+      *out_score = 0;
+      *out_status = ST_INVALID_FORM;
+      *ops_len = 0;
+      return;
+    }
+    oracle_ua_start_endsfree(&ua, ws, p, P, plen, T, tlen, pbf, pef, tbf, tef);
+  } else {
+    oracle_ua_start(&ua, ws, p, P, plen, T, tlen, C_M, C_M);
+  }
   int status;
   while (1) {
     status = oracle_ua_extend(&ua, NULL);
@@ -658,26 +839,49 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
   *out_score = classic_score(p, plen, tlen, ua.s);
   *out_status = ST_COMPLETED;
   if (p->score_only || ops == NULL) {
+    end[0] = plen;
+    end[1] = tlen;
     *ops_len = 0;
     return;
   }
-  const int n = oracle_ua_backtrace(&ua, ops);
+  int n = oracle_ua_backtrace(&ua, ops);
   if (n < 0) {
     *out_status = ST_UNATTAINABLE;
     *ops_len = 0;
-  } else {
-    *ops_len = n;
+    end[0] = end[1] = -1;
+    return;
   }
+  *ops_len = n;
+  if (p->extension) {
+    int sc = 0, ev = 0, eh = 0;
+    *out_status = maxtrim(p, ops, &n, &sc, &ev, &eh) ? 1 /* WF_STATUS_ALG_PARTIAL */ : ST_COMPLETED;
+    if (p->metric == 4 && *ops_len == 0) {
+      /* an empty affine2p CIGAR is left as the back-trace wrote it
+       * (alignment/cigar_utils.c:281): the WFA score, no end position */
+      *out_score = ua.s;
+      return;
+    }
+    *ops_len = n;
+    *out_score = sc;
+    end[0] = ev;
+    end[1] = eh;
+    return;
+  }
+  end[0] = ua.end_off - ua.end_k;
+  end[1] = ua.end_off;
+  if (ua.endsfree) *out_score = classic_score(p, end[0], end[1], ua.s);
 }
 
 int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, const int64_t* p_off,
                        const int32_t* p_len, const int64_t* t_off, const int32_t* t_len,
                        int32_t* out_score, int32_t* out_status, char* out_ops,
                        const int64_t* ops_off, int32_t* out_ops_len, int64_t* out_cells,
-                       int64_t* out_ext, int nthreads) {
+                       int64_t* out_ext, int32_t* out_end, int nthreads) {
   pen_t p;
   if (setup_penalties(cfg, &p) != 0) return -1;
   const int ultralow = (cfg[7] == 3);
+  /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82) */
+  if (ultralow && p.endsfree) return -1;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel num_threads(nthreads)
@@ -692,12 +896,17 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
       char* ops = (out_ops && !p.score_only) ? out_ops + ops_off[i] : NULL;
       int64_t* cells = out_cells ? &out_cells[i] : NULL;
       int64_t* ext = out_ext ? &out_ext[i] : NULL;
+      int32_t* end = out_end ? &out_end[2 * i] : NULL;
       if (ultralow) {
         oracle_bialign(&p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i], &ws,
                        &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext);
+        if (end) {
+          end[0] = out_status[i] == ST_COMPLETED ? p_len[i] : -1;
+          end[1] = out_status[i] == ST_COMPLETED ? t_len[i] : -1;
+        }
       } else {
         oracle_align_one(&ws, &p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i],
-                  &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext);
+                  &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext, end);
       }
     }
     ws_free(&ws);

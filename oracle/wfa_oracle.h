@@ -32,8 +32,13 @@ extern "C" {
  *   cfg[10] heuristic        (0 none, 1 wf-adaptive)
  *   cfg[11..13] wf-adaptive min_wavefront_length, max_distance_threshold,
  *           steps_between_cutoffs (wavefront/wavefront_heuristic.h:42-69)
+ *   cfg[14] span             (0 end-to-end, 1 ends-free; wavefront/wavefront_attributes.h:55-69)
+ *   cfg[15..18] pattern_begin_free, pattern_end_free, text_begin_free,
+ *           text_end_free
+ *   cfg[19] extension        (1: ends-free with the extension presets and
+ *           maximal-score trimming, wavefront/wavefront_align.c:57-63)
  */
-#define ORACLE_CFG_LEN 14
+#define ORACLE_CFG_LEN 20
 
 /* Align num_pairs pairs with nthreads host threads (OpenMP, one aligner per
  * thread, as tools/align_benchmark/align_benchmark.c:504-586 does).
@@ -49,7 +54,12 @@ extern "C" {
  *                   (sum over scores of hi-lo+1 of the compute loop)
  *   out_ext         optional (may be NULL): characters matched by extend
  *                   (sum of offset increments over all extended diagonals)
- * Returns 0, or -1 on an invalid configuration. */
+ *   out_end         optional (may be NULL): cigar->end_v, cigar->end_h of
+ *                   pair i at out_end[2i], out_end[2i+1]
+ * Returns 0, or -1 on an invalid configuration.  A pair whose ends-free
+ * parameters exceed its lengths (the reference prints an error and exits,
+ * wavefront/wavefront_align.c:90-101) gets status ORACLE_STATUS_INVALID_FORM. */
+#define ORACLE_STATUS_INVALID_FORM (-400)
 int oracle_align_batch(
     const int* cfg, int num_pairs,
     const char* sequences,
@@ -57,7 +67,7 @@ int oracle_align_batch(
     const int64_t* t_off, const int32_t* t_len,
     int32_t* out_score, int32_t* out_status,
     char* out_ops, const int64_t* ops_off, int32_t* out_ops_len,
-    int64_t* out_cells, int64_t* out_ext, int nthreads);
+    int64_t* out_cells, int64_t* out_ext, int32_t* out_end, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -17,6 +17,7 @@
 #define ST_UNATTAINABLE -300
 #define ST_END_REACHED -2
 #define ST_END_UNREACHABLE -3
+#define ST_INVALID_FORM -400
 
 enum { C_M = 0, C_I1 = 1, C_D1 = 2, C_I2 = 3, C_D2 = 4, NCOMP = 5 };
 
@@ -28,6 +29,11 @@ typedef struct {
   int max_steps;
   /* heuristic: 0 none, 1 wf-adaptive (wavefront/wavefront_heuristic.c:254-289) */
   int heur, h_min_len, h_max_dist, h_steps;
+  /* the user's penalties, as maximal-score trimming reads them
+   * (wavefront/wavefront_aligner.c:664-676) */
+  int um, ux, uo1, ue1, uo2, ue2;
+  /* alignment form (wavefront/wavefront_attributes.h:55-69) */
+  int endsfree, extension, pbf, pef, tbf, tef;
 } pen_t;
 
 typedef struct {
@@ -74,10 +80,20 @@ typedef struct {
   int s, null_steps, k_end;
   int heur, steps_wait; /* wf-adaptive cut-off state (wavefront_heuristic_clear) */
   int64_t cells, ext;
+  /* ends-free form of this alignment (0: end-to-end) and the free lengths after
+   * the per-pair presets; the end position found by termination
+   * (wf_aligner->alignment_end_pos) */
+  int endsfree, pbf, pef, tbf, tef;
+  int end_k;
+  int32_t end_off;
 } oracle_ua_t;
 
 void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const char* P, int plen,
                      const char* T, int tlen, int cb, int ce);
+/* Ends-free variant of oracle_ua_start (component M at both ends). */
+void oracle_ua_start_endsfree(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const char* P,
+                              int plen, const char* T, int tlen, int pbf, int pef, int tbf,
+                              int tef);
 int oracle_ua_extend(oracle_ua_t* ua, int* max_ak);
 void oracle_ua_compute(oracle_ua_t* ua);
 int oracle_ua_backtrace(oracle_ua_t* ua, char* ops);
@@ -90,7 +106,7 @@ void oracle_ws_free(oracle_ws_t* ws);
 /* One unidirectional end-to-end alignment (high-memory semantics). */
 void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
                       int tlen, int32_t* out_score, int32_t* out_status, char* ops,
-                      int32_t* ops_len, int64_t* cells, int64_t* ext);
+                      int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end);
 
 /* BiWFA (ultralow memory mode). */
 void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int tlen,

@@ -14,6 +14,10 @@ sources are available; the fixtures themselves travel with the repo).
    oracle/Makefile) on seeded synthetic pairs of each workload shape
    (wfa2-lib_gb300/csrc/wfa_datagen.c): cigar->score and CRC32 of the
    operations string per pair.
+4. ``endsfree_expected.json`` -- the same for the ends-free and extension
+   forms (wavefront/wavefront_attributes.h:55-69), from the reference built
+   without host tuning (oracle/_ref/libwfa_ref_scalar.so: its portable
+   extension kernels, as on aarch64), with cigar->end_v / end_h per pair.
 
 Usage:  python tests/golden/make_golden.py [/path/to/WFA2-lib]
 """
@@ -82,6 +86,24 @@ SYNTHETIC = {
     "w5_wfapt0_biwfa_full": (5, 40, "affine.wfapt0", False, 3, 3000, 300),
 }
 
+# name: (workload, n, penalties, score_only, param, param2, form, wf-adaptive)
+# form: (pattern_begin_free, pattern_end_free, text_begin_free, text_end_free)
+# or "extension"
+ENDSFREE = {
+    "w1_affine_ef5": (1, 300, "affine", False, 0, 0, (5, 5, 5, 5), None),
+    "w1_affine_ef_text": (1, 300, "affine", False, 0, 0, (0, 0, 200, 200), None),
+    "w1_affine_ef_pattern": (1, 300, "affine", False, 0, 0, (150, 150, 0, 0), None),
+    "w1_affine_ef_score": (1, 300, "affine", True, 0, 0, (50, 50, 50, 50), None),
+    "w1_affine_ext": (1, 300, "affine", False, 0, 0, "extension", None),
+    "w1_affine2p_ext": (1, 200, "affine2p", False, 0, 0, "extension", None),
+    "w5_affine2p_ef": (5, 100, "affine2p", False, 300, 150, (30, 0, 0, 30), None),
+    "w5_affine2p_ext_div": (5, 100, "affine2p", False, 120, 300, "extension", None),
+    "w5_affine_p3_ext": (5, 100, "affine.p3", False, 300, 150, "extension", None),
+    "w5_affine_p3_endonly": (5, 100, "affine.p3", False, 300, 150, (0, 40, 0, 40), None),
+    "w1_wfapt0_ef": (1, 200, "affine.wfapt0", False, 0, 0, (10, 10, 10, 10), (10, 50, 1)),
+    "w0_affine_ef_bounds": (0, 100, "affine", False, 0, 0, (99, 99, 99, 99), None),
+}
+
 
 def crc(s: str) -> int:
     return zlib.crc32(s.encode()) & 0xFFFFFFFF
@@ -91,8 +113,9 @@ def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     with open(os.path.join(ref, "tests", "wfa.utest.seq"), "rb") as f:
         raw = f.read()
-    with gzip.open(os.path.join(HERE, "utest.seq.gz"), "wb", compresslevel=9) as f:
-        f.write(raw)
+    with open(os.path.join(HERE, "utest.seq.gz"), "wb") as fo:
+        with gzip.GzipFile(fileobj=fo, mode="wb", compresslevel=9, mtime=0) as f:
+            f.write(raw)
     expected = {}
     for mode_prefix in MODES:
         for name in PENALTY_SETS:
@@ -132,6 +155,23 @@ def main():
         print(name, "done")
     with open(os.path.join(HERE, "synthetic_expected.json"), "w") as f:
         json.dump(synth, f, separators=(",", ":"))
+
+    ends = {}
+    for name, (wl, n, pset, so, param, param2, form, heur) in ENDSFREE.items():
+        m, mi, mm_, o1, e1, o2, e2 = PENALTY_SETS[pset]
+        pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
+                          gap_opening2=o2, gap_extension2=e2)
+        p = W.generate(wl, n, param=param, param2=param2)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        r = O.align(b, pen, score_only=so, kind="reference_scalar", form=form, wfadaptive=heur)
+        rows = [[int(r.score[i]), int(r.status[i]), crc(r.cigar(i)), int(r.end[i][0]),
+                 int(r.end[i][1])] for i in range(n)]
+        ends[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
+                      "penalties": pset, "score_only": so, "form": form, "wfadaptive": heur,
+                      "rows": rows}
+        print(name, "done")
+    with open(os.path.join(HERE, "endsfree_expected.json"), "w") as f:
+        json.dump(ends, f, separators=(",", ":"))
 
 
 if __name__ == "__main__":

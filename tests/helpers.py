@@ -33,6 +33,19 @@ def synthetic_expected():
         return json.load(f)
 
 
+def endsfree_expected():
+    """Reference outputs for the ends-free and extension forms; a fixture's
+    "form" is a list of the four free lengths or the string "extension"."""
+    with open(os.path.join(GOLDEN, "endsfree_expected.json")) as f:
+        d = json.load(f)
+    for fx in d.values():
+        if isinstance(fx["form"], list):
+            fx["form"] = tuple(fx["form"])
+        if fx["wfadaptive"] is not None:
+            fx["wfadaptive"] = tuple(fx["wfadaptive"])
+    return d
+
+
 def pack(patterns, texts):
     """Concatenated ASCII batch: (seqs, p_off, p_len, t_off, t_len)."""
     parts, p_off, t_off, pos = [], [], [], 0

@@ -4,7 +4,10 @@ Pins the C restatement (oracle/wfa_oracle.c) to
   * every in-scope golden file of the reference test-suite
     (tests/wfa.utest.check/*.alg via tests/golden/utest_expected.json), and
   * outputs of the reference library itself on seeded synthetic pairs
-    (tests/golden/synthetic_expected.json).
+    (tests/golden/synthetic_expected.json), and in the ends-free and
+    extension forms (tests/golden/endsfree_expected.json: score, status,
+    CIGAR and end position; the reference built with its portable extension
+    kernels).
 """
 import numpy as np
 import pytest
@@ -67,6 +70,46 @@ def test_oracle_matches_reference_on_synthetic(oracle_mod, wfa, name):
     for i, (score, status, c) in enumerate(fx["rows"]):
         assert int(r.score[i]) == score and int(r.status[i]) == status, (name, i)
         assert helpers.crc(r.cigar(i)) == c, (name, i)
+
+
+EF = helpers.endsfree_expected()
+
+
+@pytest.mark.parametrize("name", sorted(EF.keys()))
+def test_oracle_matches_reference_endsfree(oracle_mod, wfa, name):
+    O, W = oracle_mod, wfa
+    fx = EF[name]
+    pen = _pen(O, UT["penalty_sets"][fx["penalties"]])
+    p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    r = O.align(b, pen, score_only=fx["score_only"], form=fx["form"], wfadaptive=fx["wfadaptive"])
+    for i, (score, status, c, ev, eh) in enumerate(fx["rows"]):
+        got = (int(r.score[i]), int(r.status[i]), helpers.crc(r.cigar(i)), int(r.end[i][0]),
+               int(r.end[i][1]))
+        assert got == (score, status, c, ev, eh), (name, i)
+        if status in (0, 1) and not fx["score_only"] and r.cigar(i):
+            # an ends-free CIGAR still spans both sequences (free ends as I/D);
+            # a trimmed extension CIGAR spans the prefixes up to its end
+            if fx["form"] == "extension":
+                assert O.check_cigar(r.cigar(i), b.pattern(i)[:ev], b.text(i)[:eh]), (name, i)
+            else:
+                assert O.check_cigar(r.cigar(i), b.pattern(i), b.text(i)), (name, i)
+
+
+def test_oracle_endsfree_rejections(oracle_mod, wfa):
+    """Forms the restatement does not serve fail loudly: BiWFA with any
+    ends-free form (the reference exits, wavefront/wavefront_align.c:67-82) and
+    match < 0 with begin-free lengths (re-entry at multiples of -match,
+    wavefront/wavefront_compute.c:124-262)."""
+    O, W = oracle_mod, wfa
+    p = W.generate(1, 4, first=3)
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    with pytest.raises(ValueError):
+        O.align(b, O.Penalties(), memory_mode=O.MEM_ULTRALOW, form=(5, 5, 5, 5))
+    with pytest.raises(ValueError):
+        O.align(b, O.Penalties(match=-1), form=(5, 0, 0, 0))
+    O.align(b, O.Penalties(match=-1), form=(0, 5, 0, 5))
+    O.align(b, O.Penalties(match=-1), form="extension")
 
 
 def test_oracle_rescoring_and_replay(oracle_mod, wfa):
