@@ -282,9 +282,11 @@ wavefront_aligner_t* wavefront_aligner_new(wavefront_aligner_attr_t* attributes)
 void wavefront_aligner_reap(wavefront_aligner_t* const wf_aligner);
 void wavefront_aligner_delete(wavefront_aligner_t* const wf_aligner);
 
-/* wavefront/wfa.h:135-145 (wavefront/wavefront_aligner.c:508-530).  Only
- * end-to-end alignment is computed on the GPU; the ends-free and extension
- * forms are stored and make wavefront_align() return WF_STATUS_UNATTAINABLE. */
+/* wavefront/wfa.h:135-145 (wavefront/wavefront_aligner.c:508-530).  End-to-end,
+ * ends-free and extension forms are computed on the GPU, except two the GPU
+ * path does not serve (wavefront_align() then returns WF_STATUS_UNATTAINABLE):
+ * ends-free with memory mode ultralow (the reference exits there), and
+ * begin-free lengths with match < 0. */
 void wavefront_aligner_set_alignment_end_to_end(wavefront_aligner_t* const wf_aligner);
 void wavefront_aligner_set_alignment_free_ends(wavefront_aligner_t* const wf_aligner,
     const int pattern_begin_free, const int pattern_end_free,
@@ -391,6 +393,10 @@ void cigar_print_pretty(FILE* const stream, cigar_t* const cigar,
 #define WF2G_ERR_ARGS          -3
 #define WF2G_ERR_CUDA          -4
 #define WF2G_ERR_OOM           -5
+/* Per-pair status with no reference counterpart: ends-free lengths longer
+ * than the pair's sequences (wavefront_align() prints the reference's
+ * message and exits, as wavefront/wavefront_align.c:90-101 does). */
+#define WF2G_STATUS_INVALID_FORM -400
 
 int wavefront_align_batch(wavefront_aligner_t* const wf_aligner, const int num_pairs,
     const char* seqs,
@@ -398,6 +404,19 @@ int wavefront_align_batch(wavefront_aligner_t* const wf_aligner, const int num_p
     const int64_t* text_offsets, const int32_t* text_lengths,
     int32_t* scores, int32_t* status,
     char* cigar_ops, const int64_t* cigar_offsets, int32_t* cigar_lengths);
+
+/* Same, plus each pair's end position and WFA score: end_info[3i] =
+ * cigar->end_v, end_info[3i+1] = cigar->end_h, end_info[3i+2] =
+ * align_status.score.  Ends-free alignments end before the sequences' ends;
+ * a trimmed extension ends where its CIGAR does ((-1,-1) when it is empty).
+ * Not for memory mode ultralow (WF2G_ERR_CONFIG). */
+int wavefront_align_batch_ends(wavefront_aligner_t* const wf_aligner, const int num_pairs,
+    const char* seqs,
+    const int64_t* pattern_offsets, const int32_t* pattern_lengths,
+    const int64_t* text_offsets, const int32_t* text_lengths,
+    int32_t* scores, int32_t* status,
+    char* cigar_ops, const int64_t* cigar_offsets, int32_t* cigar_lengths,
+    int32_t* end_info);
 
 /* Same, with every pointer in device memory of the aligner's GPU and the work
  * queued on `cuda_stream` (a cudaStream_t, or NULL for the aligner's own

@@ -272,6 +272,70 @@ __device__ __forceinline__ void pool_push(const KParams& p, const int32_t* block
 }
 
 
+// ---------------------------------------------------------------- extension
+// Score of an operation run under the user's penalties as maximal-score
+// trimming counts it: a match earns -match, or 1 when match is 0
+// (alignment/cigar_utils.c:208-235).
+__device__ __forceinline__ int run_score_2p(const KParams& p, uint8_t op, int len, int* ev, int* eh) {
+  if (op == 'M') { *ev += len; *eh += len; return (p.um != 0 ? p.um : -1) * len; }
+  if (op == 'X') { *ev += len; *eh += len; return p.ux * len; }
+  if (op == 'D') *ev += len; else *eh += len;
+  return min(p.uo1 + p.ue1 * len, p.uo2 + p.ue2 * len);
+}
+
+// Maximal-score trimming of ops[0..*n) (alignment/cigar_utils.c:112-318):
+// keeps the highest-scoring prefix; *n, *score, *ev, *eh describe it (an empty
+// prefix: 0 ops, INT32_MIN, end (-1,-1), as cigar_clear leaves them).
+// Returns whether the CIGAR was trimmed.  Affine2p leaves an empty CIGAR
+// untouched and returns false.  One thread, sequential.
+template <bool A2P>
+__device__ bool maxtrim(const KParams& p, const uint8_t* ops, int* n, int* score, int* ev, int* eh) {
+  const int len = *n;
+  int max_score = 0, max_off = 0, max_v = 0, max_h = 0, sc = 0, v = 0, h = 0;
+  if (A2P) {
+    if (len <= 0) return false;
+    uint8_t last = 0;
+    int run = 0;
+    for (int i = 0; i < len; ++i) {
+      const uint8_t op = ops[i];
+      if (op != last && last != 0) {
+        sc -= run_score_2p(p, last, run, &v, &h);
+        run = 0;
+        if (max_score < sc) { max_score = sc; max_off = i - 1; max_v = v; max_h = h; }
+      }
+      last = op;
+      ++run;
+    }
+    sc -= run_score_2p(p, last, run, &v, &h);
+    if (max_score < sc) { max_score = sc; max_off = len - 1; max_v = v; max_h = h; }
+  } else {
+    const int msc = p.um != 0 ? p.um : -1;
+    uint8_t last = 0;
+    for (int i = 0; i < len; ++i) {
+      const uint8_t op = ops[i];
+      if (op == 'M') { sc -= msc; ++v; ++h; }
+      else if (op == 'X') { sc -= p.ux; ++v; ++h; }
+      else if (op == 'I') { sc -= p.ue1 + (last == 'I' ? 0 : p.uo1); ++h; }
+      else { sc -= p.ue1 + (last == 'D' ? 0 : p.uo1); ++v; }
+      last = op;
+      if (max_score < sc) { max_score = sc; max_off = i; max_v = v; max_h = h; }
+    }
+  }
+  const bool trimmed = (max_off != len - 1);
+  if (max_score == 0) {
+    *n = 0;
+    *score = INT32_MIN;
+    *ev = -1;
+    *eh = -1;
+  } else {
+    *n = max_off + 1;
+    *score = max_score;
+    *ev = max_v;
+    *eh = max_h;
+  }
+  return trimmed;
+}
+
 // 4 resident 256-thread blocks per SM (64 registers per thread): the kernel
 // is latency-bound, so residency matters more than registers.
 #ifndef WF2G_MIN_BLOCKS
@@ -283,7 +347,8 @@ __device__ __forceinline__ void pool_push(const KParams& p, const int32_t* block
 // (the whole CTA per pair, for long pairs whose rows span thousands of
 // diagonals).  For G > 32 the back-trace walk and replay run on the group's
 // first warp while the others wait.
-template <bool A2P, bool CIGAR, int ENC, typename OffT, bool HEUR, int G>
+// EF: the ends-free form (and its extension variant) is compiled in.
+template <bool A2P, bool CIGAR, int ENC, typename OffT, bool HEUR, int G, bool EF = false>
 __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const KParams p) {
   static_assert(G == 32 || G == 256, "a pair is aligned by a warp or a 256-thread CTA");
   typedef typename Seq<ENC>::Word Word;
@@ -321,7 +386,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
   int2* const imeta = meta + nrows;
   // G > 32: per-warp partial reductions [G/32][kRedVals] and a broadcast slot
   int32_t* const gred = reinterpret_cast<int32_t*>(imeta + nrows);
-  constexpr int kRedVals = 10, kBc = (G / 32) * kRedVals;
+  constexpr int kRedVals = EF ? 11 : 10, kBc = (G / 32) * kRedVals;
   (void)gred;
   BtRow* const table = CIGAR ? reinterpret_cast<BtRow*>(gs) : nullptr;
   uint8_t* const bits = CIGAR ? reinterpret_cast<uint8_t*>(table + p.table_cap) : nullptr;
@@ -399,6 +464,29 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       group_sync<G>();
       continue;
     }
+    // ends-free lengths of this pair: the extension presets
+    // (wavefront/wavefront_align.c:57-63), checked as :90-101 checks them
+    int pbf = 0, pef = 0, tbf = 0, tef = 0;
+    if (EF) {
+      pbf = p.extension ? 0 : p.pbf;
+      pef = p.extension ? plen : p.pef;
+      tbf = p.extension ? 0 : p.tbf;
+      tef = p.extension ? tlen : p.tef;
+      if (pbf > plen || pef > plen || tbf > tlen || tef > tlen) {
+        if (t == 0) {
+          p.status[pair] = kStInvalidForm;
+          p.scores[pair] = 0;
+          if (CIGAR) p.ops_len[pair] = 0;
+          if (p.end_info) {
+            p.end_info[3 * (int64_t)pair] = -1;
+            p.end_info[3 * (int64_t)pair + 1] = -1;
+            p.end_info[3 * (int64_t)pair + 2] = 0;
+          }
+        }
+        group_sync<G>();
+        continue;
+      }
+    }
 
     // ---- reset the rows the previous pair left non-NULL
     for (int r = 0; r < nrows; ++r) {
@@ -439,12 +527,39 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     auto comp_row = [&](int c, int cM, int c1, int c2) -> int {
       return c == 0 ? cM : c == 1 ? rowI1 + c1 : c == 2 ? rowD1 + c1 : c == 3 ? rowI2 + c2 : rowD2 + c2;
     };
-    const int L0 = cb == 0 ? lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair) : 0;
-    if (t == 0) {
-      const int r0 = comp_row(cb, 0, 0, 0);
-      RING_ST(row(r0), 0, (OffT)L0);
-      meta[r0] = imeta[r0] = make_int2(0, 0);
-      if (CIGAR) table[0] = BtRow{0, 0, 0};
+    // ends-free with match 0: M[0] spans [-pattern_begin_free,
+    // text_begin_free], diagonal k starting at (v,h) = (max(0,-k), max(0,k))
+    // (wavefront/wavefront_aligner.c:250-305)
+    const int e_lo = (EF && cb == 0 && pen.match == 0) ? -pbf : 0;
+    const int e_hi = (EF && cb == 0 && pen.match == 0) ? tbf : 0;
+    // ends-free: the first diagonal of the last extended M wavefront that
+    // reaches an end within the free lengths (INT32_MAX: none)
+    int ef_k = INT32_MAX;
+    auto ef_done = [&](int off, int k) -> bool {
+      const int vv = off - k;
+      return (off >= tlen && plen - vv <= pef) || (vv >= plen && tlen - off <= tef);
+    };
+    if (EF && cb == 0) {
+      int qk = INT32_MAX;
+      for (int k = e_lo + t; k <= e_hi; k += G) {
+        const int v0 = max(0, -k), h0 = max(0, k);
+        const int off = h0 + lcp<ENC>(P, T, v0, h0, min(plen - v0, tlen - h0), nwords, g_pair);
+        RING_ST(row(0), k, (OffT)off);
+        if (ef_done(off, k)) qk = min(qk, k);
+      }
+      ef_k = gmin(qk);
+      if (t == 0) {
+        meta[0] = imeta[0] = make_int2(e_lo, e_hi);
+        if (CIGAR) table[0] = BtRow{0, 0, 0};
+      }
+    } else {
+      const int L0 = cb == 0 ? lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair) : 0;
+      if (t == 0) {
+        const int r0 = comp_row(cb, 0, 0, 0);
+        RING_ST(row(r0), 0, (OffT)L0);
+        meta[r0] = imeta[r0] = make_int2(0, 0);
+        if (CIGAR) table[0] = BtRow{0, 0, 0};
+      }
     }
     group_sync<G>();
 
@@ -457,7 +572,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int64_t blk_off = 0, pool_used = 0;
     int result = 0;      // 1 done, -1 overflow, 2 max steps, 3 unreachable, 4 guard
     const int k_end = tlen - plen;
-    int mlo = cb == 0 ? 0 : 1, mhi = 0;  // trimmed limits of M[s]
+    int mlo = cb == 0 ? e_lo : 1, mhi = cb == 0 ? e_hi : 0;  // trimmed limits of M[s]
     bool m_exists = (cb == 0);
 
     while (true) {
@@ -465,7 +580,13 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       // component (wavefront/wavefront_termination.c:37-108); checked only
       // where M[s] exists (wavefront/wavefront_extend.c:93-106)
       if (m_exists) {
-        if (ce == 0) {
+        if (EF) {
+          // wavefront/wavefront_termination.c:115-162, in extension order
+          if (ef_k != INT32_MAX) {
+            result = 1;
+            break;
+          }
+        } else if (ce == 0) {
           if (mlo <= k_end && k_end <= mhi && RING_LD(row(curM), k_end) >= tlen) {
             result = 1;
             break;
@@ -693,6 +814,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       int tloM = INT32_MAX, thiM = INT32_MIN;
       int tloI1 = INT32_MAX, thiI1 = INT32_MIN, tloD1 = INT32_MAX, thiD1 = INT32_MIN;
       int tloI2 = INT32_MAX, thiI2 = INT32_MIN, tloD2 = INT32_MAX, thiD2 = INT32_MIN;
+      int qk = INT32_MAX;  // ends-free: first terminating diagonal of this thread
       // Software-pipelined: the next cell's inputs are loaded before the
       // current cell is computed, so one load latency overlaps the work.
       int32_t n_mo1_m = 0, n_mo1_p = 0, n_i1_e = 0, n_d1_e = 0, n_mx = 0;
@@ -742,6 +864,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (okM) {
           const int v = best - k;
           mext = best + lcp<ENC>(P, T, v, best, min(plen - v, tlen - best), nwords, g_pair);
+          if (EF && ef_done(mext, k)) qk = min(qk, k);
         }
         RING_ST(oM, k, (OffT)mext);
         RING_ST(oI1, k, (OffT)i1);
@@ -813,6 +936,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         tloD2 = __reduce_min_sync(kFull, tloD2);
         thiD2 = __reduce_max_sync(kFull, thiD2);
       }
+      if (EF) qk = __reduce_min_sync(kFull, qk);
       if (G > 32) {
         // across the group's warps: one barrier; the partials are next
         // written after the end-of-step barrier, so they need no second one
@@ -820,6 +944,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (lane == 0) {
           pr[0] = tloM; pr[1] = thiM; pr[2] = tloI1; pr[3] = thiI1; pr[4] = tloD1; pr[5] = thiD1;
           if (A2P) { pr[6] = tloI2; pr[7] = thiI2; pr[8] = tloD2; pr[9] = thiD2; }
+          if (EF) pr[kRedVals - 1] = qk;
         }
         __syncthreads();
         for (int w = 0; w < G / 32; ++w) {
@@ -831,8 +956,10 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
             tloI2 = min(tloI2, q[6]); thiI2 = max(thiI2, q[7]);
             tloD2 = min(tloD2, q[8]); thiD2 = max(thiD2, q[9]);
           }
+          if (EF) qk = min(qk, q[kRedVals - 1]);
         }
       }
+      if (EF) ef_k = qk;
       trim_fill<OffT, G>(oM, lo, hi, tloM, thiM, t, rb, g_pair);
       trim_fill<OffT, G>(oI1, lo, hi, tloI1, thiI1, t, rb, g_pair);
       trim_fill<OffT, G>(oD1, lo, hi, tloD1, thiD1, t, rb, g_pair);
@@ -891,17 +1018,40 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           p.status[pair] = st;
           p.scores[pair] = sc;
           if (CIGAR) p.ops_len[pair] = 0;
+          if (p.end_info) {
+            p.end_info[3 * (int64_t)pair] = -1;
+            p.end_info[3 * (int64_t)pair + 1] = -1;
+            p.end_info[3 * (int64_t)pair + 2] = s;
+          }
         }
       }
       group_sync<G>();
       continue;
     }
-    // classic score (wavefront/wavefront_compute.c:108-120)
-    const int score = (pen.match == 0) ? -s : ((-pen.match) * (plen + tlen) - s) / 2;
+    // the end position: (plen, tlen) end-to-end, the terminating diagonal's
+    // cell ends-free (wf_aligner->alignment_end_pos)
+    int end_k = k_end, end_v = plen, end_h = tlen;
+    if (EF) {
+      end_k = ef_k;
+      end_h = RING_LD(row(curM), ef_k);
+      end_v = end_h - ef_k;
+    }
+    // classic score (wavefront/wavefront_compute.c:108-120); a score-only
+    // run reports it for the whole sequences (wavefront/wavefront_unialign.c:
+    // 160-165), a full run for the end position
+    auto classic = [&](int ev, int eh) -> int {
+      return (pen.match == 0) ? -s : ((-pen.match) * (ev + eh) - s) / 2;
+    };
+    const int score = CIGAR ? classic(end_v, end_h) : classic(plen, tlen);
     if (!CIGAR) {
       if (t == 0) {
         p.scores[pair] = score;
         p.status[pair] = kStCompleted;
+        if (p.end_info) {
+          p.end_info[3 * (int64_t)pair] = plen;
+          p.end_info[3 * (int64_t)pair + 1] = tlen;
+          p.end_info[3 * (int64_t)pair + 2] = s;
+        }
       }
       group_sync<G>();
       continue;
@@ -914,9 +1064,10 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int64_t n = 0;
     bool bad = false;
     bool items_full = false;  // walk items did not fit the back-trace slice
+    int k_begin = 0;          // diagonal of the score-0 cell the walk reaches
     if (G == 32 || wig == 0) {
       int st = ce;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
-      int ss = s, kk = k_end;
+      int ss = s, kk = end_k;
       while (true) {
         if (n + 2 > items_cap) { items_full = true; break; }
         if (ss < 0) { bad = true; break; }
@@ -924,7 +1075,9 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           if (lane == 0 && CHK(n < items_cap, 33, n)) items[n] = 'E';
           ++n;
           if (ss == 0) {
-            bad = (kk != 0) || (cb != 0);
+            // ends-free: any diagonal of the score-0 wavefront
+            bad = EF ? (kk < e_lo || kk > e_hi) : ((kk != 0) || (cb != 0));
+            k_begin = kk;
             break;
           }
         } else if (ss == 0) {
@@ -984,9 +1137,21 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       continue;
     }
     int out_n = 0;
+    int fin_status = kStCompleted, fin_score = score, fin_v = end_v, fin_h = end_h;
     if ((G == 32 || wig == 0) && !bad) {
       uint8_t* const out = p.ops + p.ops_off[pair];
       int v = 0, h = 0;
+      if (EF && k_begin != 0) {
+        // a free beginning: insertions of the text's first k, or deletions of
+        // the pattern's first -k (wavefront/wavefront_backtrace.c:506-516)
+        const int nb = k_begin > 0 ? k_begin : -k_begin;
+        const uint8_t op = k_begin > 0 ? 'I' : 'D';
+        for (int j = lane; j < nb; j += 32)
+          if (CHK(j < plen + tlen, 39, j)) out[j] = op;
+        out_n = nb;
+        v = max(0, -k_begin);
+        h = max(0, k_begin);
+      }
       for (int64_t i = n - 1; i >= 0; --i) {
         const uint8_t it = items[i];
         if (it == 'E') {
@@ -1005,15 +1170,77 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           ++out_n;
         }
       }
-      if (v != plen || h != tlen) bad = true;
+      if (v != end_v || h != end_h) bad = true;
+      if (EF && !bad) {
+        // the free end: insertions, then deletions, up to the sequences' ends
+        // (wavefront/wavefront_backtrace.c:346-356)
+        const int ni = tlen - end_h, nd = plen - end_v;
+        for (int j = lane; j < ni + nd; j += 32)
+          if (CHK(out_n + j < plen + tlen, 40, out_n + j)) out[out_n + j] = j < ni ? 'I' : 'D';
+        out_n += ni + nd;
+        if (p.extension) {
+          __syncwarp();
+          if (lane == 0) {
+            int len = out_n, sc = 0, ev = 0, eh = 0;
+            const bool trimmed = maxtrim<A2P>(p, out, &len, &sc, &ev, &eh);
+            if (A2P && out_n == 0) {
+              // an empty CIGAR stays as the back-trace wrote it
+              // (alignment/cigar_utils.c:281): the WFA score, no end position
+              fin_score = s;
+              fin_v = fin_h = -1;
+            } else {
+              fin_status = trimmed ? kStPartial : kStCompleted;
+              fin_score = sc;
+              fin_v = ev;
+              fin_h = eh;
+              out_n = len;
+            }
+          }
+        }
+      }
     }
     if (t == 0) {
-      p.status[pair] = bad ? kStUnattainable : kStCompleted;
-      p.scores[pair] = score;
+      p.status[pair] = bad ? kStUnattainable : fin_status;
+      p.scores[pair] = bad ? score : fin_score;
       p.ops_len[pair] = bad ? 0 : out_n;
+      if (p.end_info) {
+        p.end_info[3 * (int64_t)pair] = bad ? -1 : fin_v;
+        p.end_info[3 * (int64_t)pair + 1] = bad ? -1 : fin_h;
+        p.end_info[3 * (int64_t)pair + 2] = s;
+      }
     }
     group_sync<G>();
   }
+}
+
+}  // namespace wf2g
+
+namespace wf2g {
+
+// Kernel table of one family (wf-adaptive H, group size G, ends-free EF):
+// (affine2p?, full CIGAR?, 2- or 8-bit staging, 2- or 4-byte offsets) -> the
+// kernel.  Taking the addresses instantiates the family in the including
+// unit; CTA-per-pair families exist for full-CIGAR runs only (nullptr else).
+template <typename T, bool H, int G, bool EF>
+void* align_kernel_t(int a2p, int cigar, int enc) {
+  if (cigar) {
+    if (enc == 2) return a2p ? (void*)wfa_align_kernel<true, true, 2, T, H, G, EF>
+                             : (void*)wfa_align_kernel<false, true, 2, T, H, G, EF>;
+    return a2p ? (void*)wfa_align_kernel<true, true, 8, T, H, G, EF>
+               : (void*)wfa_align_kernel<false, true, 8, T, H, G, EF>;
+  }
+  if constexpr (G == 32) {
+    if (enc == 2) return a2p ? (void*)wfa_align_kernel<true, false, 2, T, H, G, EF>
+                             : (void*)wfa_align_kernel<false, false, 2, T, H, G, EF>;
+    return a2p ? (void*)wfa_align_kernel<true, false, 8, T, H, G, EF>
+               : (void*)wfa_align_kernel<false, false, 8, T, H, G, EF>;
+  }
+  return nullptr;
+}
+template <bool H, int G, bool EF>
+void* align_kernel(int a2p, int cigar, int enc, int off_bytes) {
+  return off_bytes == 2 ? align_kernel_t<int16_t, H, G, EF>(a2p, cigar, enc)
+                        : align_kernel_t<int32_t, H, G, EF>(a2p, cigar, enc);
 }
 
 }  // namespace wf2g

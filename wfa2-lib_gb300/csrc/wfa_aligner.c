@@ -312,7 +312,9 @@ void wavefront_aligner_set_min_offsets_per_thread(wavefront_aligner_t* const wf,
 static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   const wavefront_penalties_t* p = &wf->penalties;
   if (p->distance_metric != gap_affine && p->distance_metric != gap_affine_2p) return -1;
-  if (wf->alignment_form.span != alignment_end2end || wf->alignment_form.extension) return -1;
+  const alignment_form_t* form = &wf->alignment_form;
+  /* extension is an ends-free form (wavefront/wavefront_aligner.c:526-530) */
+  if (form->span == alignment_end2end && form->extension) return -1;
   /* exact, or the wf-adaptive cut-off (wavefront/wavefront_heuristic.c:229-289);
    * wfmash, drops and bands are not computed on the GPU */
   const int wfadaptive = (wf->heuristic.strategy == wf_heuristic_wfadaptive);
@@ -332,6 +334,37 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   cfg->h_min_len = wfadaptive ? wf->heuristic.min_wavefront_length : 0;
   cfg->h_max_dist = wfadaptive ? wf->heuristic.max_distance_threshold : 0;
   cfg->h_steps = wfadaptive ? wf->heuristic.steps_between_cutoffs : 0;
+  /* alignment form (wavefront/wavefront_attributes.h:55-69) */
+  cfg->endsfree = (form->span == alignment_endsfree);
+  cfg->extension = cfg->endsfree && form->extension;
+  cfg->pbf = cfg->endsfree ? form->pattern_begin_free : 0;
+  cfg->pef = cfg->endsfree ? form->pattern_end_free : 0;
+  cfg->tbf = cfg->endsfree ? form->text_begin_free : 0;
+  cfg->tef = cfg->endsfree ? form->text_end_free : 0;
+  if (cfg->endsfree) {
+    /* BiWFA has no ends-free form (the reference exits,
+     * wavefront/wavefront_align.c:67-82) */
+    if (cfg->ultralow) return -1;
+    if (cfg->pbf < 0 || cfg->pef < 0 || cfg->tbf < 0 || cfg->tef < 0) return -1;
+    /* with match < 0 a begin-free run re-enters at every score that is a
+     * multiple of -match (wavefront/wavefront_compute.c:124-262): not computed */
+    if (!cfg->extension && p->match != 0 && (cfg->pbf > 0 || cfg->tbf > 0)) return -1;
+  }
+  /* the user's penalties, for maximal-score trimming (wavefront/wavefront_aligner.c:664-676) */
+  if (p->distance_metric == gap_affine) {
+    cfg->um = p->affine_penalties.match;
+    cfg->ux = p->affine_penalties.mismatch;
+    cfg->uo1 = p->affine_penalties.gap_opening;
+    cfg->ue1 = p->affine_penalties.gap_extension;
+    cfg->uo2 = cfg->ue2 = 0;
+  } else {
+    cfg->um = p->affine2p_penalties.match;
+    cfg->ux = p->affine2p_penalties.mismatch;
+    cfg->uo1 = p->affine2p_penalties.gap_opening1;
+    cfg->ue1 = p->affine2p_penalties.gap_extension1;
+    cfg->uo2 = p->affine2p_penalties.gap_opening2;
+    cfg->ue2 = p->affine2p_penalties.gap_extension2;
+  }
   return 0;
 }
 
@@ -351,7 +384,8 @@ static int align_one(wavefront_aligner_t* const wf, const char* seqbuf, int plen
     if (!warned_config) {
       fprintf(stderr,
               "[wfa2gpu] configuration not computed on the GPU (needs gap-affine or "
-              "gap-affine-2p, end-to-end, heuristic none)\n");
+              "gap-affine-2p; heuristic none or wf-adaptive; end-to-end, or ends-free "
+              "outside BiWFA with match 0 or no begin-free lengths)\n");
       warned_config = 1;
     }
     wf->align_status.status = WF_STATUS_UNATTAINABLE;
@@ -362,24 +396,40 @@ static int align_one(wavefront_aligner_t* const wf, const char* seqbuf, int plen
     wf->align_status.status = WF_STATUS_UNATTAINABLE;
     return WF_STATUS_UNATTAINABLE;
   }
+  /* wavefront/wavefront_align.c:90-101: the same check, message and exit */
+  if (cfg.endsfree && !cfg.extension &&
+      (cfg.pbf > plen || cfg.pef > plen || cfg.tbf > tlen || cfg.tef > tlen)) {
+    fprintf(stderr,
+            "[WFA] Ends-free parameters must be not larger than the sequences "
+            "(P0=%d,Pf=%d,T0=%d,Tf=%d). Must be (P0<=|P|,Pf<=|P|,T0<=|T|,Tf<=|T|) where "
+            "(|P|,|T|)=(%d,%d)\n",
+            cfg.pbf, cfg.pef, cfg.tbf, cfg.tef, plen, tlen);
+    exit(1);
+  }
   const int score_only = cfg.score_only;
   if (!score_only) cigar_resize(cigar, 2 * (plen + tlen) + 1);
   const int64_t p_off = 0, t_off = plen, ops_off = 0;
-  int32_t score = 0, status = 0, ops_len = 0;
+  int32_t score = 0, status = 0, ops_len = 0, end_info[3] = {-1, -1, 0};
   const int rc = wf2g_engine_align(wf->engine, &cfg, 1, 0, seqbuf, &p_off, &plen, &t_off, &tlen,
                                    0, &score, &status, score_only ? NULL : cigar->operations,
                                    score_only ? NULL : &ops_off, score_only ? NULL : &ops_len,
-                                   NULL);
+                                   cfg.ultralow ? NULL : end_info, NULL);
   if (rc != 0) {
     wf->align_status.status = WF_STATUS_UNATTAINABLE;
     return WF_STATUS_UNATTAINABLE;
   }
   wf->align_status.status = status;
-  if (status == WF_STATUS_ALG_COMPLETED) {
+  if (status == WF_STATUS_ALG_COMPLETED || status == WF_STATUS_ALG_PARTIAL) {
     cigar->score = score;
-    cigar->end_v = plen;
-    cigar->end_h = tlen;
-    wf->align_status.score = wf_score_of(wf, score, plen, tlen);
+    if (cfg.ultralow) {
+      cigar->end_v = plen;
+      cigar->end_h = tlen;
+      wf->align_status.score = wf_score_of(wf, score, plen, tlen);
+    } else {
+      cigar->end_v = end_info[0];
+      cigar->end_h = end_info[1];
+      wf->align_status.score = end_info[2];
+    }
     if (!score_only) {
       cigar->begin_offset = 0;
       cigar->end_offset = ops_len;
@@ -450,7 +500,25 @@ int wavefront_align_batch(wavefront_aligner_t* const wf_aligner, const int num_p
   return wf2g_engine_align(wf_aligner->engine, &cfg, num_pairs, 0, seqs, pattern_offsets,
                            pattern_lengths, text_offsets, text_lengths, 0, scores, status,
                            cfg.score_only ? NULL : cigar_ops, cfg.score_only ? NULL : cigar_offsets,
-                           cfg.score_only ? NULL : cigar_lengths, NULL);
+                           cfg.score_only ? NULL : cigar_lengths, NULL, NULL);
+}
+
+int wavefront_align_batch_ends(wavefront_aligner_t* const wf_aligner, const int num_pairs,
+                               const char* seqs, const int64_t* pattern_offsets,
+                               const int32_t* pattern_lengths, const int64_t* text_offsets,
+                               const int32_t* text_lengths, int32_t* scores, int32_t* status,
+                               char* cigar_ops, const int64_t* cigar_offsets,
+                               int32_t* cigar_lengths, int32_t* end_info) {
+  if (!wf_aligner || num_pairs < 0 || !end_info) return WF2G_ERR_ARGS;
+  if (!wf_aligner->engine) return WF2G_ERR_NO_GPU;
+  wf2g_cfg_t cfg;
+  if (make_cfg(wf_aligner, &cfg) != 0) return WF2G_ERR_CONFIG;
+  if (cfg.ultralow) return WF2G_ERR_CONFIG;
+  if (!cfg.score_only && (!cigar_ops || !cigar_offsets || !cigar_lengths)) return WF2G_ERR_ARGS;
+  return wf2g_engine_align(wf_aligner->engine, &cfg, num_pairs, 0, seqs, pattern_offsets,
+                           pattern_lengths, text_offsets, text_lengths, 0, scores, status,
+                           cfg.score_only ? NULL : cigar_ops, cfg.score_only ? NULL : cigar_offsets,
+                           cfg.score_only ? NULL : cigar_lengths, end_info, NULL);
 }
 
 int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const int num_pairs,
@@ -469,7 +537,7 @@ int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const in
                            d_pattern_lengths, d_text_offsets, d_text_lengths, max_sequence_length,
                            d_scores, d_status, cfg.score_only ? NULL : d_cigar_ops,
                            cfg.score_only ? NULL : d_cigar_offsets,
-                           cfg.score_only ? NULL : d_cigar_lengths, cuda_stream);
+                           cfg.score_only ? NULL : d_cigar_lengths, NULL, cuda_stream);
 }
 
 int wavefront_align_batch_device_noalloc(wavefront_aligner_t* const wf_aligner,

@@ -439,7 +439,7 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
                               (int32_t*)B->lscore.p + j0, (int32_t*)B->lstatus.p + j0,
                               (char*)B->lops.p, (const int64_t*)B->lopsoff.p + j0,
                               (int32_t*)B->lopslen.p + j0, (const int8_t*)B->lcb.p + j0,
-                              (const int8_t*)B->lce.p + j0, cap, st);
+                              (const int8_t*)B->lce.p + j0, cap, nullptr, st);
         if (rc) return rc;
         j0 = j1;
       }

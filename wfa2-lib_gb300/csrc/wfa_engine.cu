@@ -77,8 +77,9 @@ extern "C" void* wf2g_engine_new(int* err) {
         for (int ob = 2; ob <= 4; ob += 2)
           for (int h = 0; h < 2; ++h)
             for (int w = 0; w <= cig; ++w)
-              cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h, w),
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+              for (int ef = 0; ef < 2; ++ef)
+                cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h, w, ef),
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (err) *err = WF2G_OK_;
   return E;
 }
@@ -90,7 +91,7 @@ extern "C" void wf2g_engine_free(void* engine) {
   DevBuf* bufs[] = {&E->seqs,   &E->poff,     &E->plen,  &E->toff,     &E->tlen,
                     &E->scores, &E->status,   &E->ops,   &E->opsoff,   &E->opslen,
                     &E->counters, &E->retry,  &E->scratch1, &E->scratch2,
-                    &E->pool,   &E->poolctl};
+                    &E->pool,   &E->poolctl,  &E->endinfo};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   bi_state_free(E->bi);
@@ -141,7 +142,7 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   int wpc = ps.wide ? 1 : (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_group, 1));
   if (!ps.wide) wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
   size_t smem = (size_t)kp.smem_per_group * wpc;
-  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur, ps.wide);
+  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur, ps.wide, cfg.endsfree);
   if (!fn) return WF2G_ERR_CUDA_;
   // shared memory holds only the staged sequences and row limits; give the
   // rest of the SM's unified storage to L1, which caches the wavefront rows
@@ -193,7 +194,7 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                  const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
                  char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
-                 const int8_t* d_ce, int score_cap, cudaStream_t st) {
+                 const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st) {
   const bool cigar = !cfg.score_only;
   if (max_len < 1) max_len = 1;
   // counters: [0..3] work queues of passes 1-4, [4..6] retry counts of passes 1-3
@@ -212,6 +213,18 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   base.h_min_len = cfg.h_min_len;
   base.h_max_dist = cfg.h_max_dist;
   base.h_steps = cfg.h_steps;
+  base.pbf = cfg.pbf;
+  base.pef = cfg.pef;
+  base.tbf = cfg.tbf;
+  base.tef = cfg.tef;
+  base.extension = cfg.extension;
+  base.um = cfg.um;
+  base.ux = cfg.ux;
+  base.uo1 = cfg.uo1;
+  base.ue1 = cfg.ue1;
+  base.uo2 = cfg.uo2;
+  base.ue2 = cfg.ue2;
+  base.end_info = d_end_info;
   base.seqs = (const uint8_t*)d_seqs;
   base.p_off = d_poff;
   base.p_len = d_plen;
@@ -325,7 +338,8 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
                                  const char* seqs, const int64_t* p_off, const int32_t* p_len,
                                  const int64_t* t_off, const int32_t* t_len, int max_len,
                                  int32_t* scores, int32_t* status, char* ops,
-                                 const int64_t* ops_off, int32_t* ops_len, void* stream) {
+                                 const int64_t* ops_off, int32_t* ops_len, int32_t* end_info,
+                                 void* stream) {
   Engine* E = (Engine*)engine;
   if (!E) return WF2G_ERR_NO_GPU_;
   if (n < 0 || !cfg) return WF2G_ERR_ARGS_;
@@ -341,7 +355,7 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
                        ops, ops_off, ops_len, st);
   if (on_device) {
     return plan_and_run(E, *cfg, n, seqs, p_off, p_len, t_off, t_len, max_len, scores, status,
-                        ops, ops_off, ops_len, nullptr, nullptr, 0, st);
+                        ops, ops_off, ops_len, nullptr, nullptr, 0, end_info, st);
   }
   // ---- host path: stage inputs, run, copy results back
   int64_t seq_end = 0, ops_end = 0;
@@ -360,6 +374,7 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
     return WF2G_ERR_OOM_;
   if (cigar && (ensure(E->ops, (size_t)ops_end + 16) || ensure(E->opsoff, n8) || ensure(E->opslen, n4)))
     return WF2G_ERR_OOM_;
+  if (end_info && ensure(E->endinfo, 3 * n4)) return WF2G_ERR_OOM_;
   cudaError_t e = cudaSuccess;
   e = cudaMemcpyAsync(E->seqs.p, seqs, (size_t)seq_end, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(E->poff.p, p_off, n8, cudaMemcpyHostToDevice, st);
@@ -373,9 +388,12 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
                         (const int32_t*)E->tlen.p, mlen, (int32_t*)E->scores.p,
                         (int32_t*)E->status.p, cigar ? (char*)E->ops.p : nullptr,
                         cigar ? (const int64_t*)E->opsoff.p : nullptr,
-                        cigar ? (int32_t*)E->opslen.p : nullptr, nullptr, nullptr, 0, st);
+                        cigar ? (int32_t*)E->opslen.p : nullptr, nullptr, nullptr, 0,
+                        end_info ? (int32_t*)E->endinfo.p : nullptr, st);
   if (rc) return rc;
   e = cudaMemcpyAsync(scores, E->scores.p, n4, cudaMemcpyDeviceToHost, st);
+  if (end_info && e == cudaSuccess)
+    e = cudaMemcpyAsync(end_info, E->endinfo.p, 3 * n4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(status, E->status.p, n4, cudaMemcpyDeviceToHost, st);
   if (cigar && e == cudaSuccess) e = cudaMemcpyAsync(ops_len, E->opslen.p, n4, cudaMemcpyDeviceToHost, st);
   if (cigar && e == cudaSuccess) e = cudaMemcpyAsync(ops, E->ops.p, (size_t)ops_end, cudaMemcpyDeviceToHost, st);

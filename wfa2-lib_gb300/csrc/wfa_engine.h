@@ -23,6 +23,11 @@ typedef struct {
   int ultralow;  /* 1: BiWFA (wavefront_memory_ultralow) */
   /* wf-adaptive heuristic (heur = 1) and its parameters; 0: exact */
   int heur, h_min_len, h_max_dist, h_steps;
+  /* alignment form (wavefront/wavefront_attributes.h:55-69): endsfree = 1
+   * with the four free lengths, or extension = 1 (per-pair presets and
+   * maximal-score trimming with the user's penalties um..ue2) */
+  int endsfree, extension, pbf, pef, tbf, tef;
+  int um, ux, uo1, ue1, uo2, ue2;
 } wf2g_cfg_t;
 
 /* Creates an engine on the current CUDA device; NULL (and *err set to a
@@ -34,12 +39,14 @@ void wf2g_engine_free(void* engine);
  * in, computes and copies out, and returns when the results are in place.
  * on_device=1: every pointer is device memory, work is queued on `stream`
  * (NULL: the engine's own stream) and the call returns without waiting.
- * max_len bounds the pattern and text lengths (computed when on_device=0). */
+ * max_len bounds the pattern and text lengths (computed when on_device=0).
+ * end_info (optional, 3 int32 per pair): cigar->end_v, cigar->end_h and the
+ * WFA score (align_status.score). */
 int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int num_pairs, int on_device,
                       const char* seqs, const int64_t* p_off, const int32_t* p_len,
                       const int64_t* t_off, const int32_t* t_len, int max_len,
                       int32_t* scores, int32_t* status, char* ops, const int64_t* ops_off,
-                      int32_t* ops_len, void* stream);
+                      int32_t* ops_len, int32_t* end_info, void* stream);
 
 int64_t wf2g_engine_launches(const void* engine);
 

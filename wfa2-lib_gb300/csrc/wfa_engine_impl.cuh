@@ -21,7 +21,8 @@
 #define WF2G_ERR_OOM_ -5
 
 namespace wf2g {
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide);
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide,
+                                 int ef);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 extern "C" void* wf2g_bi_kernel_ptr(int a2p);
 extern "C" void* wf2g_bi_pack_ptr(void);
@@ -67,7 +68,7 @@ struct Engine {
   cudaStream_t stream = nullptr;
   int64_t launches = 0;
   // batch buffers (host-input path)
-  DevBuf seqs, poff, plen, toff, tlen, scores, status, ops, opsoff, opslen;
+  DevBuf seqs, poff, plen, toff, tlen, scores, status, ops, opsoff, opslen, endinfo;
   // control
   DevBuf counters;  // [0] queue pass 1, [1] queue pass 2, [2] retry count
   DevBuf retry;
@@ -122,7 +123,7 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                  const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
                  char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
-                 const int8_t* d_ce, int score_cap, cudaStream_t st);
+                 const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st);
 
 // BiWFA batch (wfa_bialign_host.cu); synchronises `st`.
 int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const char* seqs,

@@ -1,8 +1,8 @@
 // wfa_kernels.cu -- sm_103a kernels of the GB300 wavefront aligner: the
-// warp-per-pair exact variants, the block-pool set-up and the kernel table.
-// The alignment kernel itself is the template of wfa_align.cuh; its
-// wf-adaptive and CTA-per-pair variants are built by wfa_kernels_heur.cu and
-// wfa_kernels_wide.cu, in parallel with this unit.
+// warp-per-pair exact end-to-end variants, the block-pool set-up and the
+// kernel table.  The alignment kernel itself is the template of
+// wfa_align.cuh; its other families (wf-adaptive, ends-free, CTA per pair)
+// are built by the wfa_kernels_*.cu units, in parallel with this one.
 #include "wfa_align.cuh"
 
 namespace wf2g {
@@ -17,47 +17,36 @@ __global__ void wfa_pool_init_kernel(int32_t* stack, int32_t* count, int32_t* lo
   }
 }
 
-#define WF2G_INST(A2P, CIG, ENC, T) \
-  template __global__ void wfa_align_kernel<A2P, CIG, ENC, T, false, 32>(const KParams p);
-#define WF2G_INST_T(T)          \
-  WF2G_INST(false, false, 2, T) \
-  WF2G_INST(false, true, 2, T)  \
-  WF2G_INST(true, false, 2, T)  \
-  WF2G_INST(true, true, 2, T)   \
-  WF2G_INST(false, false, 8, T) \
-  WF2G_INST(false, true, 8, T)  \
-  WF2G_INST(true, false, 8, T)  \
-  WF2G_INST(true, true, 8, T)
-WF2G_INST_T(int16_t)
-WF2G_INST_T(int32_t)
-
-template <typename T>
-static void* pick(int a2p, int cigar, int enc) {
-  if (enc == 2) {
-    if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 2, T, false, 32> : (void*)wfa_align_kernel<false, false, 2, T, false, 32>;
-    return cigar ? (void*)wfa_align_kernel<true, true, 2, T, false, 32> : (void*)wfa_align_kernel<true, false, 2, T, false, 32>;
-  }
-  if (!a2p) return cigar ? (void*)wfa_align_kernel<false, true, 8, T, false, 32> : (void*)wfa_align_kernel<false, false, 8, T, false, 32>;
-  return cigar ? (void*)wfa_align_kernel<true, true, 8, T, false, 32> : (void*)wfa_align_kernel<true, false, 8, T, false, 32>;
-}
-
 WF2G_FAULT_READER(wf2g_fault_info_exact)
 
 }  // namespace wf2g
 
 extern "C" void* wf2g_kernel_ptr_heur(int a2p, int cigar, int enc, int off_bytes);
+extern "C" void* wf2g_kernel_ptr_ef(int a2p, int cigar, int enc, int off_bytes);
+extern "C" void* wf2g_kernel_ptr_ef_heur(int a2p, int cigar, int enc, int off_bytes);
 extern "C" void* wf2g_kernel_ptr_wide(int a2p, int enc, int off_bytes, int heur);
+extern "C" void* wf2g_kernel_ptr_wide_ef(int a2p, int enc, int off_bytes, int heur);
 extern "C" int wf2g_fault_info_exact(unsigned long long* out);
 extern "C" int wf2g_fault_info_heur(unsigned long long* out);
+extern "C" int wf2g_fault_info_ef(unsigned long long* out);
+extern "C" int wf2g_fault_info_ef_heur(unsigned long long* out);
 extern "C" int wf2g_fault_info_wide(unsigned long long* out);
+extern "C" int wf2g_fault_info_wide_ef(unsigned long long* out);
 
 // Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or
-// 4-byte offsets, wf-adaptive heuristic?, a CTA per pair?).  The CTA-per-pair
-// variants exist for full-CIGAR runs only.
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide) {
-  if (wide) return cigar ? wf2g_kernel_ptr_wide(a2p, enc, off_bytes, heur) : nullptr;
+// 4-byte offsets, wf-adaptive heuristic?, a CTA per pair?, ends-free form?).
+// The CTA-per-pair variants exist for full-CIGAR runs only.
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide,
+                                 int ef) {
+  if (wide) {
+    if (!cigar) return nullptr;
+    return ef ? wf2g_kernel_ptr_wide_ef(a2p, enc, off_bytes, heur)
+              : wf2g_kernel_ptr_wide(a2p, enc, off_bytes, heur);
+  }
+  if (ef) return heur ? wf2g_kernel_ptr_ef_heur(a2p, cigar, enc, off_bytes)
+                      : wf2g_kernel_ptr_ef(a2p, cigar, enc, off_bytes);
   if (heur) return wf2g_kernel_ptr_heur(a2p, cigar, enc, off_bytes);
-  return off_bytes == 2 ? wf2g::pick<int16_t>(a2p, cigar, enc) : wf2g::pick<int32_t>(a2p, cigar, enc);
+  return wf2g::align_kernel<false, 32, false>(a2p, cigar, enc, off_bytes);
 }
 
 extern "C" void* wf2g_pool_init_ptr(void) { return (void*)wf2g::wfa_pool_init_kernel; }
@@ -65,10 +54,11 @@ extern "C" void* wf2g_pool_init_ptr(void) { return (void*)wf2g::wfa_pool_init_ke
 // First bounds violation seen by a checked build: {site, index, pair, count}
 // (the first unit that recorded one; counts add up).
 extern "C" int wf2g_fault_info(unsigned long long* out) {
-  int (*const readers[3])(unsigned long long*) = {wf2g_fault_info_exact, wf2g_fault_info_heur,
-                                                  wf2g_fault_info_wide};
+  int (*const readers[6])(unsigned long long*) = {
+      wf2g_fault_info_exact, wf2g_fault_info_heur,    wf2g_fault_info_ef,
+      wf2g_fault_info_ef_heur, wf2g_fault_info_wide, wf2g_fault_info_wide_ef};
   for (int i = 0; i < 4; ++i) out[i] = 0;
-  for (int r = 0; r < 3; ++r) {
+  for (int r = 0; r < 6; ++r) {
     unsigned long long f[4];
     const int rc = readers[r](f);
     if (rc) return rc;

@@ -26,6 +26,10 @@ constexpr int kStPartial = 1;
 constexpr int kStMaxSteps = -100;
 constexpr int kStOOM = -200;
 constexpr int kStUnattainable = -300;
+// no reference counterpart: ends-free lengths longer than the pair's
+// sequences (the reference prints an error and exits,
+// wavefront/wavefront_align.c:90-101)
+constexpr int kStInvalidForm = -400;
 
 // Back-trace choice byte, one per computed cell (s,k):
 //   bits 0-2  source of M:  0 mismatch, 1 D1, 2 I1, 3 D2, 4 I2
@@ -110,6 +114,14 @@ struct KParams {
   // a pass with a retry list sends pairs this long or longer (either
   // sequence) straight to it: the CTA-per-pair passes take them (0: off)
   int wide_min_len;
+  // ends-free form (kernels built with EF; wavefront/wavefront_attributes.h:
+  // 55-69): free lengths, or the extension presets per pair
+  // (wavefront/wavefront_align.c:57-63) followed by maximal-score trimming
+  // with the user's penalties um..ue2 (alignment/cigar_utils.c:112-318)
+  int pbf, pef, tbf, tef, extension;
+  int um, ux, uo1, ue1, uo2, ue2;
+  // optional per-pair {cigar->end_v, cigar->end_h, WFA score} (nullptr: none)
+  int32_t* end_info;
 };
 
 }  // namespace wf2g

@@ -21,7 +21,8 @@
 #include "wfa_kernels.cuh"
 
 namespace wf2g {
-extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide);
+extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide,
+                                 int ef);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 }  // namespace wf2g
 
@@ -80,6 +81,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   }
   if (cfg->metric != 3 && cfg->metric != 4) return -2;  // WF2G_ERR_CONFIG
   if (cfg->ultralow) return -2;  // BiWFA allocates per recursion level
+  if (cfg->endsfree) return -2;  // the ends-free kernels are not in the fixed-scratch set
   const bool cigar = !cfg->score_only;
   if (cigar && (!d_ops || !d_opsoff || !d_opslen)) return -3;
   int err = 0;
@@ -157,7 +159,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.gscratch = base + 256;
   // calls share the array: clear the queue head left by the previous call
   if (cudaMemsetAsync(queue, 0, sizeof(int32_t), st) != cudaSuccess) return -4;
-  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur, 0);
+  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur, 0, 0);
   void* args[] = {(void*)&kp};
   const cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args,
                                          (size_t)kp.smem_per_group * wpc, st);

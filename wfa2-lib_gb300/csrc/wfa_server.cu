@@ -174,7 +174,7 @@ struct Server {
       const bool cig = !c.score_only;
       const int rc = wf2g_engine_align(E, &c, m, 0, seqs, p_off, p_len, t_off, t_len, 0, scores,
                                        status, cig ? opsb : nullptr, cig ? ops_off : nullptr,
-                                       cig ? ops_len : nullptr, nullptr);
+                                       cig ? ops_len : nullptr, nullptr, nullptr);
       for (int j = 0; j < m; ++j) {
         const int i = order[j0 + j];
         if (rc != 0) {
@@ -294,7 +294,8 @@ extern "C" void* wf2g_server_new(const wf2g_cfg_t* cfg, int64_t hbm_budget,
     if (err) *err = WF2G_ERR_NO_GPU_;
     return nullptr;
   }
-  if (!cfg || cfg->ultralow) {
+  // the BiWFA fallback has no ends-free form (wavefront/wavefront_align.c:67-82)
+  if (!cfg || cfg->ultralow || cfg->endsfree) {
     if (err) *err = WF2G_ERR_CONFIG_;
     return nullptr;
   }

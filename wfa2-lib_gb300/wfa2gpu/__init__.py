@@ -26,6 +26,8 @@ WF_STATUS_ALG_PARTIAL = 1
 WF_STATUS_MAX_STEPS_REACHED = -100
 WF_STATUS_OOM = -200
 WF_STATUS_UNATTAINABLE = -300
+WF2G_STATUS_INVALID_FORM = -400  # ends-free lengths longer than a pair's sequences
+ALIGNMENT_END2END, ALIGNMENT_ENDSFREE = 0, 1
 
 INDEL, EDIT, GAP_LINEAR, GAP_AFFINE, GAP_AFFINE_2P = 0, 1, 2, 3, 4
 COMPUTE_SCORE, COMPUTE_ALIGNMENT = 0, 1
@@ -147,7 +149,8 @@ EXPORTED = [
     "cigar_count_matches", "cigar_get_CIGAR", "cigar_score_edit", "cigar_score_gap_linear",
     "cigar_score_gap_affine", "cigar_score_gap_affine2p", "cigar_check_alignment",
     "cigar_print", "cigar_sprint", "cigar_print_SAM_CIGAR", "cigar_sprint_SAM_CIGAR",
-    "cigar_print_pretty", "wavefront_align_batch", "wavefront_align_batch_device",
+    "cigar_print_pretty", "wavefront_align_batch", "wavefront_align_batch_ends",
+    "wavefront_align_batch_device",
     "wavefront_aligner_gpu_launches", "wfa2gpu_device",
     "wavefront_align_batch_device_noalloc",
     "wavefront_server_new", "wavefront_server_submit", "wavefront_server_poll",
@@ -198,6 +201,9 @@ def lib() -> C.CDLL:
     L.wavefront_align_batch.argtypes = [C.POINTER(Aligner_t), C.c_int, P, P, P, P, P, P, P, P,
                                         P, P]
     L.wavefront_align_batch.restype = C.c_int
+    L.wavefront_align_batch_ends.argtypes = [C.POINTER(Aligner_t), C.c_int, P, P, P, P, P, P, P,
+                                             P, P, P, P]
+    L.wavefront_align_batch_ends.restype = C.c_int
     L.wavefront_align_batch_device.argtypes = [C.POINTER(Aligner_t), C.c_int, P, P, P, P, P,
                                                C.c_int, P, P, P, P, P, P]
     L.wavefront_align_batch_device.restype = C.c_int
@@ -259,6 +265,9 @@ class Config:
     # wf-adaptive heuristic: (min_wavefront_length, max_distance_threshold,
     # steps_between_cutoffs), or None for exact alignment
     wfadaptive: tuple | None = None
+    # alignment form: None (end-to-end), "extension", or the ends-free lengths
+    # (pattern_begin_free, pattern_end_free, text_begin_free, text_end_free)
+    form: tuple | str | None = None
 
     def attributes(self) -> AlignerAttr:
         a = default_attributes()
@@ -282,6 +291,15 @@ class Config:
         a.memory_mode = self.memory_mode
         if self.max_steps > 0:
             a.system.max_alignment_steps = self.max_steps
+        f = a.alignment_form
+        f.span, f.extension = ALIGNMENT_END2END, False
+        f.pattern_begin_free = f.pattern_end_free = f.text_begin_free = f.text_end_free = 0
+        if self.form == "extension":
+            f.span, f.extension = ALIGNMENT_ENDSFREE, True
+        elif self.form is not None:
+            f.span = ALIGNMENT_ENDSFREE
+            (f.pattern_begin_free, f.pattern_end_free, f.text_begin_free,
+             f.text_end_free) = self.form
         return a
 
 
@@ -355,6 +373,26 @@ class Aligner:
                                          _ptr(t_off), _ptr(t_len), _ptr(scores), _ptr(status),
                                          _ptr(ops), _ptr(ops_off), _ptr(ops_len))
         return rc, scores, status, ops, ops_len, ops_off
+
+    def align_batch_ends(self, seqs, p_off, p_len, t_off, t_len):
+        """wavefront_align_batch_ends(); returns (rc, scores, status, ops, ops_len, ops_off,
+        end_info) with end_info an (n, 3) array of cigar->end_v, cigar->end_h and the WFA
+        score."""
+        n = int(p_len.shape[0])
+        scores = np.zeros(n, np.int32)
+        status = np.zeros(n, np.int32)
+        end_info = np.zeros((n, 3), np.int32)
+        ops = ops_off = ops_len = None
+        if not self.cfg.score_only:
+            ops_off = np.zeros(n + 1, np.int64)
+            np.cumsum(p_len.astype(np.int64) + t_len.astype(np.int64), out=ops_off[1:])
+            ops = np.zeros(max(int(ops_off[n]), 1), np.uint8)
+            ops_len = np.zeros(n, np.int32)
+        rc = lib().wavefront_align_batch_ends(self._h, n, _ptr(seqs), _ptr(p_off), _ptr(p_len),
+                                              _ptr(t_off), _ptr(t_len), _ptr(scores),
+                                              _ptr(status), _ptr(ops), _ptr(ops_off),
+                                              _ptr(ops_len), _ptr(end_info))
+        return rc, scores, status, ops, ops_len, ops_off, end_info
 
     def align_batch_device(self, n, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len, d_scores,
                            d_status, d_ops=0, d_ops_off=0, d_ops_len=0, stream=0) -> int:
