@@ -26,6 +26,7 @@ PORT_LIB = os.path.join(HERE, "_build", "libwfa_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libwfa_ref.so")
 REF_SCALAR_LIB = os.path.join(HERE, "_ref", "libwfa_ref_scalar.so")
 
+INDEL, EDIT, GAP_LINEAR = 0, 1, 2
 GAP_AFFINE = 3
 GAP_AFFINE_2P = 4
 MEM_HIGH, MEM_MED, MEM_LOW, MEM_ULTRALOW = 0, 1, 2, 3
@@ -33,7 +34,9 @@ MEM_HIGH, MEM_MED, MEM_LOW, MEM_ULTRALOW = 0, 1, 2, 3
 
 @dataclass
 class Penalties:
-    """Penalties as the reference's attribute structs hold them (match <= 0)."""
+    """Penalties as the reference's attribute structs hold them (match <= 0).
+    Gap-linear keeps its indel penalty in gap_opening1; edit and indel take
+    none."""
 
     metric: int = GAP_AFFINE
     match: int = 0
@@ -241,6 +244,14 @@ def rescore_affine2p(ops: str, match: int, x: int, o1: int, e1: int, o2: int, e2
 
 
 def rescore(ops: str, pen: Penalties) -> int:
+    """Score of a CIGAR under the metric (alignment/cigar.c:244-346): the edit
+    or indel distance, or the negated gap-linear / affine / affine-2p cost
+    (gap-linear takes its indel penalty from gap_opening1)."""
+    if pen.metric in (INDEL, EDIT):
+        return sum(1 for c in ops if c in "XID")
+    if pen.metric == GAP_LINEAR:
+        return -sum(pen.match if c == "M" else pen.mismatch if c == "X" else pen.gap_opening1
+                    for c in ops)
     if pen.metric == GAP_AFFINE:
         return rescore_affine(ops, pen.match, pen.mismatch, pen.gap_opening1, pen.gap_extension1)
     return rescore_affine2p(ops, pen.match, pen.mismatch, pen.gap_opening1, pen.gap_extension1,

@@ -40,7 +40,11 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
     attr.affine2p_penalties.gap_extension1 = cfg[4];
     attr.affine2p_penalties.gap_opening2 = cfg[5];
     attr.affine2p_penalties.gap_extension2 = cfg[6];
-  } else {
+  } else if (cfg[0] == gap_linear) {
+    attr.linear_penalties.match = cfg[1];
+    attr.linear_penalties.mismatch = cfg[2];
+    attr.linear_penalties.indel = cfg[3];
+  } else if (cfg[0] != edit && cfg[0] != indel) {
     return -1;
   }
   attr.memory_mode = (wavefront_memory_t)cfg[7];

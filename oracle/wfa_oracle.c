@@ -55,7 +55,25 @@ static int setup_penalties(const int* cfg, pen_t* p) {
   p->ue1 = e1;
   p->uo2 = o2;
   p->ue2 = e2;
-  if (p->metric != 3 && p->metric != 4) return -1;
+  if (p->metric < 0 || p->metric > 4) return -1;
+  if (p->metric <= 2) {
+    /* wavefront/wavefront_penalties.c:39-94: indel (0), edit (1), gap-linear
+     * (2, cfg[3] = the indel penalty; Eizenga transform when match < 0) */
+    if (p->metric == 2) {
+      if (m > 0 || x <= 0 || o1 <= 0) return -1;
+      p->match = m;
+      p->x = m < 0 ? 2 * x - 2 * m : x;
+      p->o1 = m < 0 ? 2 * o1 - m : o1;
+      p->scope = imax(p->x, p->o1) + 1; /* wavefront/wavefront_components.c:63-79 */
+    } else {
+      p->match = 0;
+      p->x = p->metric == 1 ? 1 : -1;
+      p->o1 = 1;
+      p->scope = 2; /* wavefront/wavefront_components.c:47-61 */
+    }
+    p->e1 = p->o2 = p->e2 = -1;
+  }
+  if (p->metric <= 2) goto common;
   if (m > 0 || x <= 0 || o1 < 0 || e1 <= 0) return -1;
   if (p->metric == 4 && (o2 < 0 || e2 <= 0)) return -1;
   if (m < 0) {
@@ -77,10 +95,13 @@ static int setup_penalties(const int* cfg, pen_t* p) {
     p->o2 = -1;
     p->e2 = -1;
   }
-  /* wavefront/wavefront_components.c:81-120 */
-  int indel = p->o1 + p->e1;
-  if (p->metric == 4) indel = imax(indel, p->o2 + p->e2);
-  p->scope = imax(indel, p->x) + 1;
+  {
+    /* wavefront/wavefront_components.c:81-120 */
+    int indel = p->o1 + p->e1;
+    if (p->metric == 4) indel = imax(indel, p->o2 + p->e2);
+    p->scope = imax(indel, p->x) + 1;
+  }
+common:
   p->score_only = cfg[8] != 0;
   p->max_steps = cfg[9] > 0 ? cfg[9] : INT_MAX;
   /* wavefront/wavefront_heuristic.c:44-55 */
@@ -99,6 +120,10 @@ static int setup_penalties(const int* cfg, pen_t* p) {
   /* with match < 0 a begin-free run also re-enters at every score that is a
    * multiple of -match (wavefront/wavefront_compute.c:124-262): not restated */
   if (p->endsfree && !p->extension && p->match != 0 && (p->pbf > 0 || p->tbf > 0)) return -1;
+  /* edit and indel never widen the score-0 wavefront's initialised window
+   * [0,0] (wavefront/wavefront_compute_edit.c:321-374), so their back-trace
+   * reads begin-free diagonals as sourceless: not restated */
+  if (p->endsfree && !p->extension && p->metric <= 1 && (p->pbf > 0 || p->tbf > 0)) return -1;
   return 0;
 }
 
@@ -219,10 +244,127 @@ static void trim_row(orow_t* r, int plen, int tlen) {
   r->null = (r->lo > r->hi);
 }
 
+/* Edit-distance exact pruning of an end-to-end wavefront of at least 1000
+ * diagonals (wavefront/wavefront_compute_edit.c:199-279): diagonals whose
+ * best case (|k - k_end| edits left) exceeds the best worst case (the larger
+ * remainder) of any diagonal are dropped from the limits. */
+static void edit_exact_prune(orow_t* r, int plen, int tlen) {
+  const int lo = r->lo, hi = r->hi;
+  if (hi - lo + 1 < 1000) return;
+  const int k_end = tlen - plen;
+  const int sample_k = lo + (hi - lo) / 2;
+  const int32_t so = r->off[sample_k];
+  if (so < 0) return;
+  const int smax_sample = imax(plen - (so - sample_k), tlen - so);
+  const int smin_lo = lo - k_end >= 0 ? lo - k_end : k_end - lo;
+  const int smin_hi = hi - k_end >= 0 ? hi - k_end : k_end - hi;
+  if (smin_lo <= smax_sample && smin_hi <= smax_sample) return;
+  int wmin = INT_MAX;
+  for (int k = lo; k <= hi; ++k) {
+    const int32_t off = r->off[k];
+    if (off < 0) continue;
+    const int w = imax(plen - (off - k), tlen - off);
+    if (w < wmin) wmin = w;
+  }
+  /* the best case |(plen - v) - (tlen - h)| = |k - k_end| for any offset */
+  int nlo = lo;
+  for (int k = lo; k <= hi; ++k) {
+    const int b = k - k_end >= 0 ? k - k_end : k_end - k;
+    if (b <= wmin) break;
+    ++nlo;
+  }
+  int nhi = hi;
+  for (int k = hi; k > nlo; --k) {
+    const int b = k - k_end >= 0 ? k - k_end : k_end - k;
+    if (b <= wmin) break;
+    --nhi;
+  }
+  r->lo = nlo;
+  r->hi = nhi;
+}
+
+/* One compute step of the single-component metrics (indel, edit, gap-linear):
+ * wavefront/wavefront_compute_edit.c:321-374 (indel/edit: M[s-1] only, limits
+ * one wider, the two elements beyond each end of M[s-1] NULLed, a null result
+ * ends the alignment, end-to-end edit pruned) and
+ * wavefront/wavefront_compute_linear.c:168-197 (gap-linear: M[s-x], M[s-o]).
+ * Returns cells computed. */
+static int64_t compute_step_linear(oracle_ws_t* ws, const pen_t* p, int s, int plen, int tlen,
+                                   int* null_steps, int endsfree) {
+  ws_ensure_rows(ws, s);
+  orow_t nullrow = {1, 1, 1, -1, 1, -1, kbuf_at0(&ws->nullbuf)};
+  const int editlike = p->metric <= 1;
+  orow_t* mx = editlike ? (p->metric == 1 ? fetch(ws, &nullrow, s - 1, C_M) : &nullrow)
+                        : fetch(ws, &nullrow, s - p->x, C_M);
+  orow_t* mo = fetch(ws, &nullrow, s - p->o1, C_M);
+  for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, s, c), 0, sizeof(orow_t));
+  int lo, hi;
+  if (editlike) {
+    if (mo->null) {  /* wavefront/wavefront_compute_edit.c:372 */
+      *null_steps = INT_MAX / 2;
+      return 0;
+    }
+    lo = mo->lo - 1;
+    hi = mo->hi + 1;
+  } else {
+    if (mx->null && mo->null) {
+      (*null_steps)++;
+      return 0;
+    }
+    *null_steps = 0;
+    lo = imin(mx->lo, mo->lo - 1);
+    hi = imax(mx->hi, mo->hi + 1);
+  }
+  ws->hlo = imin(ws->hlo, lo - (p->scope + 1));
+  ws->hhi = imax(ws->hhi, hi + (p->scope + 1));
+  kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
+  kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
+  nullrow.off = kbuf_at0(&ws->nullbuf);
+  if (editlike) {
+    mo->off[lo - 1] = WF_NULL;
+    mo->off[lo] = WF_NULL;
+    mo->off[hi] = WF_NULL;
+    mo->off[hi + 1] = WF_NULL;
+  } else {
+    init_ends(mx, lo, hi);
+    init_ends(mo, lo - 1, hi + 1);
+  }
+  orow_t* r = row_at(ws, s, C_M);
+  r->off = row_storage(ws, s, C_M, ws->hlo, ws->hhi);
+  r->exists = 1;
+  r->lo = r->ilo = lo;
+  r->hi = r->ihi = hi;
+  const int32_t* const m_x = (editlike && p->metric == 1) ? mo->off : mx->off;
+  const int32_t* const m_o = mo->off;
+  int32_t* const o_m = r->off;
+  for (int k = lo; k <= hi; ++k) {
+    /* wavefront/wavefront_compute_edit.c:44-93, wavefront/wavefront_compute_linear.c:45-66 */
+    int32_t mmax;
+    if (p->metric == 0) {
+      const int32_t ins = m_o[k - 1] + 1, del = m_o[k + 1];
+      mmax = del > ins ? del : ins;
+    } else {
+      const int32_t ins = m_o[k - 1], misms = m_x[k], del = m_o[k + 1];
+      const int32_t im = (misms > ins ? misms : ins) + 1;
+      mmax = del > im ? del : im;
+    }
+    if ((uint32_t)mmax > (uint32_t)tlen) mmax = WF_NULL;
+    if ((uint32_t)(mmax - k) > (uint32_t)plen) mmax = WF_NULL;
+    o_m[k] = mmax;
+  }
+  trim_row(r, plen, tlen);
+  if (editlike) {
+    if (r->null) *null_steps = INT_MAX / 2;
+    if (p->metric == 1 && !endsfree && !r->null) edit_exact_prune(r, plen, tlen);
+  }
+  return hi - lo + 1;
+}
+
 /* One compute step at score s (wavefront/wavefront_compute_affine.c:229-260 and
  * wavefront/wavefront_compute_affine2p.c:322-360).  Returns cells computed. */
 static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, int tlen,
-                            int* null_steps) {
+                            int* null_steps, int endsfree) {
+  if (p->metric <= 2) return compute_step_linear(ws, p, s, plen, tlen, null_steps, endsfree);
   const int a2p = (p->metric == 4);
   ws_ensure_rows(ws, s);
   orow_t nullrow = {1, 1, 1, -1, 1, -1, kbuf_at0(&ws->nullbuf)};
@@ -408,6 +550,27 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
     const int sx = s - p->x, so1 = s - p->o1 - p->e1, so2 = s - p->o2 - p->e2;
     const int se1 = s - p->e1, se2 = s - p->e2;
     int64_t mall;
+    if (p->metric <= 2) {
+      /* wavefront/wavefront_backtrace.c:223-319: one component; the gap
+       * candidates read M[s - gap_opening1] */
+      const int sg = s - p->o1;
+      const int64_t misms = p->metric != 0 ? cand(ws, sx, C_M, k, 1, BT_M) : WF_NULL;
+      mall = max64(misms, max64(cand(ws, sg, C_M, k - 1, 1, BT_I1O), cand(ws, sg, C_M, k + 1, 0, BT_D1O)));
+      if (mall < 0) break;
+      const int moff = (int)(mall >> 4);
+      for (int i = offset - moff; i > 0; --i) rev[n++] = 'M';
+      offset = moff;
+      v = offset - k;
+      h = offset;
+      if (v <= 0 || h <= 0) break;
+      const int type = (int)(mall & 0xF);
+      if (type == BT_M) { s = sx; rev[n++] = 'X'; --offset; }
+      else if (type == BT_I1O) { s = sg; rev[n++] = 'I'; --k; --offset; }
+      else { s = sg; rev[n++] = 'D'; ++k; }
+      v = offset - k;
+      h = offset;
+      continue;
+    }
     switch (mat) {
       case C_M: {
         const int64_t misms = cand(ws, sx, C_M, k, 1, BT_M);
@@ -481,8 +644,9 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
   return n;
 }
 
-/* wavefront/wavefront_compute.c:108-120 */
+/* wavefront/wavefront_compute.c:108-120 (edit and indel: the distance) */
 static int classic_score(const pen_t* p, int plen, int tlen, int s) {
+  if (p->metric <= 1) return s;
   if (p->match == 0) return -s;
   const int swg_match = -p->match;
   return (swg_match * (plen + tlen) - s) / 2;
@@ -681,7 +845,8 @@ int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
 /* Computes wavefront s+1 (wavefront/wavefront_unialign.c:266-268). */
 void oracle_ua_compute(oracle_ua_t* ua) {
   ua->s++;
-  ua->cells += compute_step(ua->ws, ua->p, ua->s, ua->plen, ua->tlen, &ua->null_steps);
+  ua->cells += compute_step(ua->ws, ua->p, ua->s, ua->plen, ua->tlen, &ua->null_steps,
+                            ua->endsfree);
 }
 
 /* Full back-trace of a finished stepper into ops (forward order); returns the
@@ -728,7 +893,24 @@ static int maxtrim(const pen_t* p, const char* ops, int* n, int* score, int* ev,
   const int len = *n;
   int max_score = 0, max_off = 0, max_v = 0, max_h = 0;
   int sc = 0, v = 0, h = 0;
-  if (p->metric == 4) {
+  if (p->metric == 2) {
+    /* cigar_maxtrim_gap_linear (alignment/cigar_utils.c:112-160) */
+    const int mscore = p->um != 0 ? p->um : -1;
+    for (int i = 0; i < len; ++i) {
+      switch (ops[i]) {
+        case 'M': sc -= mscore; ++v; ++h; break;
+        case 'X': sc -= p->ux; ++v; ++h; break;
+        case 'I': sc -= p->uo1; ++h; break;
+        default: sc -= p->uo1; ++v; break;
+      }
+      if (max_score < sc) {
+        max_score = sc;
+        max_off = i;
+        max_v = v;
+        max_h = h;
+      }
+    }
+  } else if (p->metric == 4) {
     if (len <= 0) return 0;
     char last = 0;
     int run = 0;
@@ -854,13 +1036,16 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
   *ops_len = n;
   if (p->extension) {
     int sc = 0, ev = 0, eh = 0;
-    *out_status = maxtrim(p, ops, &n, &sc, &ev, &eh) ? 1 /* WF_STATUS_ALG_PARTIAL */ : ST_COMPLETED;
-    if (p->metric == 4 && *ops_len == 0) {
-      /* an empty affine2p CIGAR is left as the back-trace wrote it
-       * (alignment/cigar_utils.c:281): the WFA score, no end position */
+    if (p->metric <= 1 || (p->metric == 4 && *ops_len == 0)) {
+      /* no trimming for edit and indel (wavefront/wavefront_aligner.c:
+       * 664-676), nor of an empty affine2p CIGAR (alignment/cigar_utils.c:281):
+       * the CIGAR stays as the back-trace wrote it, with the WFA score and no
+       * end position */
+      *out_status = ST_COMPLETED;
       *out_score = ua.s;
       return;
     }
+    *out_status = maxtrim(p, ops, &n, &sc, &ev, &eh) ? 1 /* WF_STATUS_ALG_PARTIAL */ : ST_COMPLETED;
     *ops_len = n;
     *out_score = sc;
     end[0] = ev;
@@ -880,8 +1065,9 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
   pen_t p;
   if (setup_penalties(cfg, &p) != 0) return -1;
   const int ultralow = (cfg[7] == 3);
-  /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82) */
-  if (ultralow && p.endsfree) return -1;
+  /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82);
+   * its single-component metrics are not restated */
+  if (ultralow && (p.endsfree || p.metric <= 2)) return -1;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel num_threads(nthreads)

@@ -44,6 +44,14 @@ PENALTY_SETS = {
     "affine.p5": (3, -3, 5, 3, 2, 24, 1),
     "affine.wfapt0": (3, 0, 4, 6, 2, 24, 1),
     "affine.wfapt1": (3, 0, 4, 6, 2, 24, 1),
+    "edit": (1, 0, 0, 0, 0, 0, 0),
+    "indel": (0, 0, 0, 0, 0, 0, 0),
+}
+# penalty sets with no golden file of the reference test-suite (gap-linear:
+# the indel penalty sits in the gap_opening1 slot)
+EXTRA_SETS = {
+    "linear": (2, 0, 4, 2, 0, 0, 0),
+    "linear.m1": (2, -1, 3, 2, 0, 0, 0),
 }
 # wf-adaptive heuristic of a penalty set: (min_wavefront_length,
 # max_distance_threshold, steps_between_cutoffs); tests/wfa.utest.sh:61-63
@@ -84,6 +92,15 @@ SYNTHETIC = {
     "w4_wfapt0_full": (4, 60, "affine.wfapt0", False, 0, 0, 0),
     "w1_wfapt1_score": (1, 300, "affine.wfapt1", True, 0, 0, 0),
     "w5_wfapt0_biwfa_full": (5, 40, "affine.wfapt0", False, 3, 3000, 300),
+    "w1_edit_full": (1, 300, "edit", False, 0, 0, 0),
+    "w1_indel_full": (1, 300, "indel", False, 0, 0, 0),
+    "w1_linear_full": (1, 300, "linear", False, 0, 0, 0),
+    "w1_linear_score": (1, 300, "linear", True, 0, 0, 0),
+    "w5_linear_m1_full": (5, 60, "linear.m1", False, 0, 2000, 150),
+    "w6_edit_prune_full": (6, 12, "edit", False, 0, 3000, 200),
+    "w6_edit_prune_score": (6, 12, "edit", True, 0, 3000, 200),
+    "w5_indel_score": (5, 40, "indel", True, 0, 2000, 100),
+    "w1_edit_ms50": (1, 100, "edit", False, 0, 0, 0, 50),
 }
 
 # name: (workload, n, penalties, score_only, param, param2, form, wf-adaptive)
@@ -102,6 +119,10 @@ ENDSFREE = {
     "w5_affine_p3_endonly": (5, 100, "affine.p3", False, 300, 150, (0, 40, 0, 40), None),
     "w1_wfapt0_ef": (1, 200, "affine.wfapt0", False, 0, 0, (10, 10, 10, 10), (10, 50, 1)),
     "w0_affine_ef_bounds": (0, 100, "affine", False, 0, 0, (99, 99, 99, 99), None),
+    "w1_edit_ext": (1, 200, "edit", False, 0, 0, "extension", None),
+    "w1_linear_ef": (1, 200, "linear", False, 0, 0, (20, 20, 20, 20), None),
+    "w1_linear_ext": (1, 200, "linear.m1", False, 0, 0, "extension", None),
+    "w5_indel_endonly": (5, 60, "indel", False, 500, 100, (0, 40, 0, 40), None),
 }
 
 
@@ -130,8 +151,8 @@ def main():
                     rows.append([int(score), crc(cig)])
             expected[f"{mode_prefix}.{name}"] = rows
     with open(os.path.join(HERE, "utest_expected.json"), "w") as f:
-        json.dump({"penalty_sets": PENALTY_SETS, "heuristics": HEURISTICS, "modes": MODES,
-                   "expected": expected}, f, separators=(",", ":"))
+        json.dump({"penalty_sets": {**PENALTY_SETS, **EXTRA_SETS}, "heuristics": HEURISTICS,
+                   "modes": MODES, "expected": expected}, f, separators=(",", ":"))
 
     from oracle import oracle as O
     import wfa2gpu as W
@@ -141,7 +162,7 @@ def main():
     for name, spec in SYNTHETIC.items():
         wl, n, pset, so, mm, param, param2 = spec[:7]
         max_steps = spec[7] if len(spec) > 7 else 0
-        m, mi, mm_, o1, e1, o2, e2 = PENALTY_SETS[pset][0], *PENALTY_SETS[pset][1:]
+        m, mi, mm_, o1, e1, o2, e2 = {**PENALTY_SETS, **EXTRA_SETS}[pset]
         pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
                           gap_opening2=o2, gap_extension2=e2)
         p = W.generate(wl, n, param=param, param2=param2)
@@ -158,7 +179,7 @@ def main():
 
     ends = {}
     for name, (wl, n, pset, so, param, param2, form, heur) in ENDSFREE.items():
-        m, mi, mm_, o1, e1, o2, e2 = PENALTY_SETS[pset]
+        m, mi, mm_, o1, e1, o2, e2 = {**PENALTY_SETS, **EXTRA_SETS}[pset]
         pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
                           gap_opening2=o2, gap_extension2=e2)
         p = W.generate(wl, n, param=param, param2=param2)

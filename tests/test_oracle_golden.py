@@ -35,6 +35,8 @@ def test_oracle_matches_reference_goldens(oracle_mod, key):
             break
     mode, score_only = UT["modes"][prefix]
     pen = _pen(O, UT["penalty_sets"][name])
+    if mode == O.MEM_ULTRALOW and pen.metric <= O.GAP_LINEAR:
+        pytest.skip("BiWFA for the single-component metrics is not restated")
     pats, txts = helpers.utest_pairs()
     b = O.PairBatch.from_lists(pats, txts)
     r = O.align(b, pen, memory_mode=mode, score_only=score_only,
@@ -89,8 +91,9 @@ def test_oracle_matches_reference_endsfree(oracle_mod, wfa, name):
         assert got == (score, status, c, ev, eh), (name, i)
         if status in (0, 1) and not fx["score_only"] and r.cigar(i):
             # an ends-free CIGAR still spans both sequences (free ends as I/D);
-            # a trimmed extension CIGAR spans the prefixes up to its end
-            if fx["form"] == "extension":
+            # a trimmed extension CIGAR spans the prefixes up to its end (an
+            # untrimmed one -- edit, indel -- has no end position)
+            if fx["form"] == "extension" and ev >= 0:
                 assert O.check_cigar(r.cigar(i), b.pattern(i)[:ev], b.text(i)[:eh]), (name, i)
             else:
                 assert O.check_cigar(r.cigar(i), b.pattern(i), b.text(i)), (name, i)

@@ -21,6 +21,7 @@
  *      12 uniforms) clipped to [100,50000];
  *      d~U[0.01,0.20]; edits as in 0
  *   5  |P| given by `param` (fixed); d given by `param2/1000`; edits as in 0
+ *   6  as 5, then |P|/2 random bases appended to the text (very different lengths)
  */
 #include <math.h>
 #include <stdint.h>
@@ -148,6 +149,14 @@ static void gen_pair(int workload, int64_t pair, int param, int param2, text_t* 
       memmove(T->buf + pos, T->buf + pos + len, (size_t)(T->len - pos - len));
       T->len -= len;
     }
+  }
+  if (workload == 6) {
+    /* workload 5 with a random tail of half the pattern's length appended to
+     * the text: pairs of very different lengths */
+    const int tail = plen / 2;
+    text_reserve(T, T->len + tail + 1);
+    for (int i = 0; i < tail; ++i) T->buf[T->len + i] = kBases[rng_below(&r, 4)];
+    T->len += tail;
   }
 }
 
