@@ -58,6 +58,8 @@ def test_gpu_matches_reference_goldens(gpu_available, wfa, oracle_mod, key):
     prefix, name = _split_key(key)
     mode, score_only = UT["modes"][prefix]
     spec = UT["penalty_sets"][name]
+    if mode == W.MEM_ULTRALOW and spec[0] <= W.GAP_LINEAR:
+        pytest.skip("BiWFA serves the gap-affine metrics only")
     pats, txts = helpers.utest_pairs()
     batch = helpers.pack(pats, txts)
     scores, status, cig = run_batch(W, cfg_of(W, spec, score_only, mode, 0, HEUR.get(name)),

@@ -336,6 +336,37 @@ __device__ bool maxtrim(const KParams& p, const uint8_t* ops, int* n, int* score
   return trimmed;
 }
 
+// Maximal-score trimming under gap-linear penalties (alignment/cigar_utils.c:
+// 112-160): um, ux and the indel penalty uo1; same conventions as maxtrim.
+// Edit and indel are not trimmed; for them this returns false untouched.
+__device__ __forceinline__ bool maxtrim_linear(const KParams& p, const uint8_t* ops, int* n,
+                                               int* score, int* ev, int* eh) {
+  if (p.metric != 2) return false;
+  const int len = *n, msc = p.um != 0 ? p.um : -1;
+  int max_score = 0, max_off = 0, max_v = 0, max_h = 0, sc = 0, v = 0, h = 0;
+  for (int i = 0; i < len; ++i) {
+    const uint8_t op = ops[i];
+    if (op == 'M') { sc -= msc; ++v; ++h; }
+    else if (op == 'X') { sc -= p.ux; ++v; ++h; }
+    else if (op == 'I') { sc -= p.uo1; ++h; }
+    else { sc -= p.uo1; ++v; }
+    if (max_score < sc) { max_score = sc; max_off = i; max_v = v; max_h = h; }
+  }
+  const bool trimmed = (max_off != len - 1);
+  if (max_score == 0) {
+    *n = 0;
+    *score = INT32_MIN;
+    *ev = -1;
+    *eh = -1;
+  } else {
+    *n = max_off + 1;
+    *score = max_score;
+    *ev = max_v;
+    *eh = max_h;
+  }
+  return trimmed;
+}
+
 // 4 resident 256-thread blocks per SM (64 registers per thread): the kernel
 // is latency-bound, so residency matters more than registers.
 #ifndef WF2G_MIN_BLOCKS
@@ -348,7 +379,9 @@ __device__ bool maxtrim(const KParams& p, const uint8_t* ops, int* n, int* score
 // diagonals).  For G > 32 the back-trace walk and replay run on the group's
 // first warp while the others wait.
 // EF: the ends-free form (and its extension variant) is compiled in.
-template <bool A2P, bool CIGAR, int ENC, typename OffT, bool HEUR, int G, bool EF = false>
+// LIN: the single-component metrics (indel, edit, gap-linear; with A2P false).
+template <bool A2P, bool CIGAR, int ENC, typename OffT, bool HEUR, int G, bool EF = false,
+          bool LIN = false>
 __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const KParams p) {
   static_assert(G == 32 || G == 256, "a pair is aligned by a warp or a 256-thread CTA");
   typedef typename Seq<ENC>::Word Word;
@@ -386,7 +419,16 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
   int2* const imeta = meta + nrows;
   // G > 32: per-warp partial reductions [G/32][kRedVals] and a broadcast slot
   int32_t* const gred = reinterpret_cast<int32_t*>(imeta + nrows);
-  constexpr int kRedVals = EF ? 11 : 10, kBc = (G / 32) * kRedVals;
+  constexpr int kRedVals = 12, kBc = (G / 32) * kRedVals;  // [10] ends-free k, [11] edit pruning
+  // single-component metrics (indel, edit, gap-linear): only M rows carry
+  // wavefronts; indel has no mismatch; edit and indel follow the edit driver
+  // (wavefront/wavefront_compute_edit.c:321-374)
+  static_assert(!(LIN && A2P), "the single-component metrics have no second gap model");
+  constexpr bool lin = LIN;
+  const bool edit_like = LIN && p.metric <= 1;
+  const bool has_x = !LIN || p.metric != 0;
+  // end-to-end edit prunes wide wavefronts (wavefront/wavefront_compute_edit.c:362-366)
+  const bool prune = LIN && !EF && p.metric == 1;
   (void)gred;
   BtRow* const table = CIGAR ? reinterpret_cast<BtRow*>(gs) : nullptr;
   uint8_t* const bits = CIGAR ? reinterpret_cast<uint8_t*>(table + p.table_cap) : nullptr;
@@ -664,10 +706,10 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       const int sMo1 = ring_back(curM, pen.o1 + pen.e1, pen.R);
       const int sI1 = ring_back(cur1, pen.e1, pen.RI1);
       const int2 kEmpty = make_int2(1, 0);
-      const int2 eMx = (s - pen.x >= 0) ? meta[sMx] : kEmpty;
+      const int2 eMx = (has_x && s - pen.x >= 0) ? meta[sMx] : kEmpty;
       const int2 eMo1 = (s - pen.o1 - pen.e1 >= 0) ? meta[sMo1] : kEmpty;
-      const int2 eI1 = (s - pen.e1 >= 0) ? meta[rowI1 + sI1] : kEmpty;
-      const int2 eD1 = (s - pen.e1 >= 0) ? meta[rowD1 + sI1] : kEmpty;
+      const int2 eI1 = (!lin && s - pen.e1 >= 0) ? meta[rowI1 + sI1] : kEmpty;
+      const int2 eD1 = (!lin && s - pen.e1 >= 0) ? meta[rowD1 + sI1] : kEmpty;
       int sMo2 = 0, sI2 = 0;
       int2 eMo2 = kEmpty, eI2 = kEmpty, eD2 = kEmpty;
       if (A2P) {
@@ -800,7 +842,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       const OffT* wD1 = nullptr;
       const OffT* wI2 = nullptr;
       const OffT* wD2 = nullptr;
-      if (CIGAR && HEUR) {
+      if (CIGAR && HEUR && !lin) {
         wI1 = window_row(vI1, rowI1 + sI1, s - pen.e1);
         wD1 = window_row(vD1, rowD1 + sI1, s - pen.e1);
         if (A2P) {
@@ -810,11 +852,25 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
       const bool ghost = wI1 || wD1 || wI2 || wD2;
       uint8_t* const brow = CIGAR ? bt + bpos - lo : nullptr;
+      // edit and indel NULL the two elements beyond each end of M[s-1]
+      // (wavefront/wavefront_compute_edit.c:352-356): cells a cut-off left in
+      // the initialised window are the only ones that can hold values there
+      if (HEUR && edit_like && vMo1) {
+        const int2 w = imeta[sMo1];
+        OffT* const r = row(sMo1);
+        if (t == 0) {
+          const int ks[4] = {eMo1.x - 2, eMo1.x - 1, eMo1.y + 1, eMo1.y + 2};
+          for (int j = 0; j < 4; ++j)
+            if (ks[j] >= w.x && ks[j] <= w.y) RING_ST(r, ks[j], null_of<OffT>());
+        }
+        group_sync<G>();
+      }
 
       int tloM = INT32_MAX, thiM = INT32_MIN;
       int tloI1 = INT32_MAX, thiI1 = INT32_MIN, tloD1 = INT32_MAX, thiD1 = INT32_MIN;
       int tloI2 = INT32_MAX, thiI2 = INT32_MIN, tloD2 = INT32_MAX, thiD2 = INT32_MIN;
       int qk = INT32_MAX;  // ends-free: first terminating diagonal of this thread
+      int wmin = INT32_MAX;  // edit pruning: best worst case over the unextended cells
       // Software-pipelined: the next cell's inputs are loaded before the
       // current cell is computed, so one load latency overlaps the work.
       int32_t n_mo1_m = 0, n_mo1_p = 0, n_i1_e = 0, n_d1_e = 0, n_mx = 0;
@@ -863,6 +919,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         int32_t mext = null_of<OffT>();
         if (okM) {
           const int v = best - k;
+          if (prune) wmin = min(wmin, max(plen - v, tlen - best));
           mext = best + lcp<ENC>(P, T, v, best, min(plen - v, tlen - best), nwords, g_pair);
           if (EF && ef_done(mext, k)) qk = min(qk, k);
         }
@@ -889,8 +946,10 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           else if (d1 == best) c = kSrcD1;
           else if (A2P && i2 == best) c = kSrcI2;
           else c = kSrcI1;
-          c |= (uint8_t)(i1_e >= mo1_m) << 3;
-          c |= (uint8_t)(d1_e >= mo1_p) << 4;
+          if (!lin) {  // one component: every gap opens from M
+            c |= (uint8_t)(i1_e >= mo1_m) << 3;
+            c |= (uint8_t)(d1_e >= mo1_p) << 4;
+          }
           if (A2P) {
             c |= (uint8_t)(i2_e >= mo2_m) << 5;
             c |= (uint8_t)(d2_e >= mo2_p) << 6;
@@ -937,6 +996,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         thiD2 = __reduce_max_sync(kFull, thiD2);
       }
       if (EF) qk = __reduce_min_sync(kFull, qk);
+      if (prune) wmin = __reduce_min_sync(kFull, wmin);
       if (G > 32) {
         // across the group's warps: one barrier; the partials are next
         // written after the end-of-step barrier, so they need no second one
@@ -944,7 +1004,8 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (lane == 0) {
           pr[0] = tloM; pr[1] = thiM; pr[2] = tloI1; pr[3] = thiI1; pr[4] = tloD1; pr[5] = thiD1;
           if (A2P) { pr[6] = tloI2; pr[7] = thiI2; pr[8] = tloD2; pr[9] = thiD2; }
-          if (EF) pr[kRedVals - 1] = qk;
+          if (EF) pr[10] = qk;
+          if (prune) pr[11] = wmin;
         }
         __syncthreads();
         for (int w = 0; w < G / 32; ++w) {
@@ -956,10 +1017,31 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
             tloI2 = min(tloI2, q[6]); thiI2 = max(thiI2, q[7]);
             tloD2 = min(tloD2, q[8]); thiD2 = max(thiD2, q[9]);
           }
-          if (EF) qk = min(qk, q[kRedVals - 1]);
+          if (EF) qk = min(qk, q[10]);
+          if (prune) wmin = min(wmin, q[11]);
         }
       }
       if (EF) ef_k = qk;
+      if (prune && thiM - tloM + 1 >= 1000) {
+        // exact pruning of a wide end-to-end edit wavefront on its unextended
+        // offsets (wavefront/wavefront_compute_edit.c:220-279): a diagonal's
+        // best case is |k - k_end| edits, its worst the larger remainder;
+        // diagonals whose best exceeds the least worst are dropped
+        const int sk = tloM + (thiM - tloM) / 2;
+        int32_t so = max(RING_LD(rMo1, sk + 1), max(RING_LD(rMx, sk), RING_LD(rMo1, sk - 1)) + 1);
+        if (!in_bounds(so, sk, plen, tlen)) so = -1;
+        if (so >= 0) {
+          const int smax = max(plen - (so - sk), tlen - so);
+          if (!(abs(tloM - k_end) <= smax && abs(thiM - k_end) <= smax)) {
+            const int a = max(tloM, k_end - wmin);
+            const int nlo = (a <= min(thiM, k_end + wmin)) ? a : thiM + 1;
+            const int b = min(thiM, k_end + wmin);
+            const int nhi = (b > nlo && b >= k_end - wmin) ? b : nlo;
+            tloM = nlo;
+            thiM = nhi;
+          }
+        }
+      }
       trim_fill<OffT, G>(oM, lo, hi, tloM, thiM, t, rb, g_pair);
       trim_fill<OffT, G>(oI1, lo, hi, tloI1, thiI1, t, rb, g_pair);
       trim_fill<OffT, G>(oD1, lo, hi, tloD1, thiD1, t, rb, g_pair);
@@ -1040,6 +1122,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     // run reports it for the whole sequences (wavefront/wavefront_unialign.c:
     // 160-165), a full run for the end position
     auto classic = [&](int ev, int eh) -> int {
+      if (edit_like) return s;  // the distance itself
       return (pen.match == 0) ? -s : ((-pen.match) * (ev + eh) - s) / 2;
     };
     const int score = CIGAR ? classic(end_v, end_h) : classic(plen, tlen);
@@ -1182,10 +1265,13 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           __syncwarp();
           if (lane == 0) {
             int len = out_n, sc = 0, ev = 0, eh = 0;
-            const bool trimmed = maxtrim<A2P>(p, out, &len, &sc, &ev, &eh);
-            if (A2P && out_n == 0) {
-              // an empty CIGAR stays as the back-trace wrote it
-              // (alignment/cigar_utils.c:281): the WFA score, no end position
+            const bool trimmed = lin ? maxtrim_linear(p, out, &len, &sc, &ev, &eh)
+                                     : maxtrim<A2P>(p, out, &len, &sc, &ev, &eh);
+            if (edit_like || (A2P && out_n == 0)) {
+              // edit and indel are not trimmed (wavefront/wavefront_aligner.c:
+              // 664-676), nor is an empty affine2p CIGAR (alignment/cigar_utils.c:
+              // 281): the CIGAR stays as the back-trace wrote it, with the WFA
+              // score and no end position
               fin_score = s;
               fin_v = fin_h = -1;
             } else {
@@ -1218,29 +1304,32 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
 namespace wf2g {
 
 // Kernel table of one family (wf-adaptive H, group size G, ends-free EF):
-// (affine2p?, full CIGAR?, 2- or 8-bit staging, 2- or 4-byte offsets) -> the
-// kernel.  Taking the addresses instantiates the family in the including
-// unit; CTA-per-pair families exist for full-CIGAR runs only (nullptr else).
-template <typename T, bool H, int G, bool EF>
-void* align_kernel_t(int a2p, int cigar, int enc) {
+// (affine2p?, full CIGAR?, 2- or 8-bit staging, 2- or 4-byte offsets,
+// single-component metric?) -> the kernel.  Taking the addresses instantiates
+// the family in the including unit; CTA-per-pair families exist for
+// full-CIGAR runs only (nullptr else).
+template <typename T, bool H, int G, bool EF, bool L>
+void* align_kernel_tl(int a2p, int cigar, int enc) {
   if (cigar) {
-    if (enc == 2) return a2p ? (void*)wfa_align_kernel<true, true, 2, T, H, G, EF>
-                             : (void*)wfa_align_kernel<false, true, 2, T, H, G, EF>;
-    return a2p ? (void*)wfa_align_kernel<true, true, 8, T, H, G, EF>
-               : (void*)wfa_align_kernel<false, true, 8, T, H, G, EF>;
+    if (enc == 2) return a2p && !L ? (void*)wfa_align_kernel<!L, true, 2, T, H, G, EF, L>
+                                   : (void*)wfa_align_kernel<false, true, 2, T, H, G, EF, L>;
+    return a2p && !L ? (void*)wfa_align_kernel<!L, true, 8, T, H, G, EF, L>
+                     : (void*)wfa_align_kernel<false, true, 8, T, H, G, EF, L>;
   }
   if constexpr (G == 32) {
-    if (enc == 2) return a2p ? (void*)wfa_align_kernel<true, false, 2, T, H, G, EF>
-                             : (void*)wfa_align_kernel<false, false, 2, T, H, G, EF>;
-    return a2p ? (void*)wfa_align_kernel<true, false, 8, T, H, G, EF>
-               : (void*)wfa_align_kernel<false, false, 8, T, H, G, EF>;
+    if (enc == 2) return a2p && !L ? (void*)wfa_align_kernel<!L, false, 2, T, H, G, EF, L>
+                                   : (void*)wfa_align_kernel<false, false, 2, T, H, G, EF, L>;
+    return a2p && !L ? (void*)wfa_align_kernel<!L, false, 8, T, H, G, EF, L>
+                     : (void*)wfa_align_kernel<false, false, 8, T, H, G, EF, L>;
   }
   return nullptr;
 }
 template <bool H, int G, bool EF>
-void* align_kernel(int a2p, int cigar, int enc, int off_bytes) {
-  return off_bytes == 2 ? align_kernel_t<int16_t, H, G, EF>(a2p, cigar, enc)
-                        : align_kernel_t<int32_t, H, G, EF>(a2p, cigar, enc);
+void* align_kernel(int a2p, int cigar, int enc, int off_bytes, int lin) {
+  if (lin) return off_bytes == 2 ? align_kernel_tl<int16_t, H, G, EF, true>(0, cigar, enc)
+                                 : align_kernel_tl<int32_t, H, G, EF, true>(0, cigar, enc);
+  return off_bytes == 2 ? align_kernel_tl<int16_t, H, G, EF, false>(a2p, cigar, enc)
+                        : align_kernel_tl<int32_t, H, G, EF, false>(a2p, cigar, enc);
 }
 
 }  // namespace wf2g

@@ -148,8 +148,7 @@ static void penalties_set_affine2p(wavefront_penalties_t* wp, const affine2p_pen
   wp->internal_gap_e = ap->gap_extension1;
 }
 /* edit / indel / gap-linear keep the reference's representation
- * (wavefront/wavefront_penalties.c:37-94); they are accepted but not yet
- * computed on the GPU. */
+ * (wavefront/wavefront_penalties.c:37-94). */
 static void penalties_set_other(wavefront_penalties_t* wp, const wavefront_aligner_attr_t* a) {
   memset(wp, 0, sizeof(*wp));
   wp->distance_metric = a->distance_metric;
@@ -311,7 +310,7 @@ void wavefront_aligner_set_min_offsets_per_thread(wavefront_aligner_t* const wf,
  * GPU; otherwise the WF_STATUS_* / WF2G_ERR_* code to report. */
 static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   const wavefront_penalties_t* p = &wf->penalties;
-  if (p->distance_metric != gap_affine && p->distance_metric != gap_affine_2p) return -1;
+  const int lin = p->distance_metric <= gap_linear;  /* indel, edit, gap-linear */
   const alignment_form_t* form = &wf->alignment_form;
   /* extension is an ends-free form (wavefront/wavefront_aligner.c:526-530) */
   if (form->span == alignment_end2end && form->extension) return -1;
@@ -323,9 +322,9 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   cfg->match = p->match;
   cfg->x = p->mismatch;
   cfg->o1 = p->gap_opening1;
-  cfg->e1 = p->gap_extension1;
-  cfg->o2 = p->gap_opening2;
-  cfg->e2 = p->gap_extension2;
+  cfg->e1 = lin ? 0 : p->gap_extension1;
+  cfg->o2 = lin ? 0 : p->gap_opening2;
+  cfg->e2 = lin ? 0 : p->gap_extension2;
   cfg->score_only = (wf->alignment_scope == compute_score);
   cfg->max_steps = wf->system.max_alignment_steps > 0 ? wf->system.max_alignment_steps : INT_MAX;
   /* ultralow memory mode is BiWFA (wavefront/wavefront_align.c:138-146) */
@@ -349,9 +348,20 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
     /* with match < 0 a begin-free run re-enters at every score that is a
      * multiple of -match (wavefront/wavefront_compute.c:124-262): not computed */
     if (!cfg->extension && p->match != 0 && (cfg->pbf > 0 || cfg->tbf > 0)) return -1;
+    /* edit and indel never widen the score-0 wavefront's initialised window
+     * (wavefront/wavefront_compute_edit.c:321-374), so their back-trace reads
+     * begin-free diagonals as sourceless: not computed */
+    if (!cfg->extension && p->distance_metric <= edit && (cfg->pbf > 0 || cfg->tbf > 0)) return -1;
   }
+  /* BiWFA serves the gap-affine metrics only */
+  if (lin && cfg->ultralow) return -1;
   /* the user's penalties, for maximal-score trimming (wavefront/wavefront_aligner.c:664-676) */
-  if (p->distance_metric == gap_affine) {
+  if (lin) {
+    cfg->um = p->linear_penalties.match;
+    cfg->ux = p->linear_penalties.mismatch;
+    cfg->uo1 = p->linear_penalties.indel;
+    cfg->ue1 = cfg->uo2 = cfg->ue2 = 0;
+  } else if (p->distance_metric == gap_affine) {
     cfg->um = p->affine_penalties.match;
     cfg->ux = p->affine_penalties.mismatch;
     cfg->uo1 = p->affine_penalties.gap_opening;

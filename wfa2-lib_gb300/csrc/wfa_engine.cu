@@ -78,8 +78,9 @@ extern "C" void* wf2g_engine_new(int* err) {
           for (int h = 0; h < 2; ++h)
             for (int w = 0; w <= cig; ++w)
               for (int ef = 0; ef < 2; ++ef)
-                cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h, w, ef),
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                for (int lin = 0; lin <= 1 - a2p; ++lin)
+                  cudaFuncSetAttribute(wf2g_kernel_ptr(a2p, cig, enc, ob, h, w, ef, lin),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (err) *err = WF2G_OK_;
   return E;
 }
@@ -142,7 +143,8 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   int wpc = ps.wide ? 1 : (int)std::min<size_t>(8, E->smem_optin / std::max<size_t>(kp.smem_per_group, 1));
   if (!ps.wide) wpc = std::max(1, std::min(env_int("WF2G_WPC", wpc), 8));
   size_t smem = (size_t)kp.smem_per_group * wpc;
-  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur, ps.wide, cfg.endsfree);
+  void* fn = wf2g_kernel_ptr(a2p, cigar, ps.enc, off_bytes, base.heur, ps.wide, cfg.endsfree,
+                             cfg.metric <= 2);
   if (!fn) return WF2G_ERR_CUDA_;
   // shared memory holds only the staged sequences and row limits; give the
   // rest of the SM's unified storage to L1, which caches the wavefront rows
@@ -208,6 +210,7 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   KParams base;
   memset(&base, 0, sizeof(base));
   base.pen = make_pen(cfg);
+  base.metric = cfg.metric;
   base.max_steps = cfg.max_steps;
   base.heur = cfg.heur;
   base.h_min_len = cfg.h_min_len;
@@ -344,7 +347,9 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
   if (!E) return WF2G_ERR_NO_GPU_;
   if (n < 0 || !cfg) return WF2G_ERR_ARGS_;
   if (n == 0) return WF2G_OK_;
-  if (cfg->metric != 3 && cfg->metric != 4) return WF2G_ERR_CONFIG_;
+  if (cfg->metric < 0 || cfg->metric > 4) return WF2G_ERR_CONFIG_;
+  // BiWFA serves the gap-affine metrics only
+  if (cfg->ultralow && cfg->metric <= 2) return WF2G_ERR_CONFIG_;
   const bool cigar = !cfg->score_only;
   if (cigar && (!ops || !ops_off || !ops_len)) return WF2G_ERR_ARGS_;
   cudaSetDevice(E->device);

@@ -22,7 +22,7 @@
 
 namespace wf2g {
 extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide,
-                                 int ef);
+                                 int ef, int lin);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 extern "C" void* wf2g_bi_kernel_ptr(int a2p);
 extern "C" void* wf2g_bi_pack_ptr(void);
@@ -96,6 +96,18 @@ inline Penalties make_pen(const wf2g_cfg_t& c) {
   p.x = c.x;
   p.o1 = c.o1;
   p.e1 = c.e1;
+  if (c.metric <= 2) {
+    // one component: gaps read M[s - gap_opening1] (e1 = 0, no I/D rings);
+    // max_score_scope (wavefront/wavefront_components.c:47-79)
+    p.x = c.metric == 0 ? 1 : c.x;  // indel has no mismatch input
+    p.e1 = 0;
+    p.o2 = 0;
+    p.e2 = 1;
+    p.R = c.metric <= 1 ? 2 : std::max(c.x, c.o1) + 1;
+    p.RI1 = 1;
+    p.RI2 = 1;
+    return p;
+  }
   p.o2 = c.metric == 4 ? c.o2 : 0;
   p.e2 = c.metric == 4 ? c.e2 : 1;
   // wavefront/wavefront_components.c:81-120: max_score_scope
@@ -110,6 +122,8 @@ inline Penalties make_pen(const wf2g_cfg_t& c) {
 // Upper bound of the alignment score, as the reference sizes its wavefront
 // table (wavefront/wavefront_components.c:101-108), for lengths <= max_len.
 inline int score_bound(const wf2g_cfg_t& c, int max_len) {
+  if (c.metric <= 2)  // every base a mismatch or a gap
+    return (int)std::min<int64_t>((int64_t)(std::max(c.x, 0) + 2 * c.o1) * max_len + 8, INT32_MAX / 4);
   int64_t b = (int64_t)c.x * max_len + c.o1 + (int64_t)c.e1 * max_len;
   if (c.metric == 4) b = std::max<int64_t>(b, (int64_t)c.x * max_len + c.o2 + (int64_t)c.e2 * max_len);
   b += 8;

@@ -21,11 +21,11 @@ WF2G_FAULT_READER(wf2g_fault_info_exact)
 
 }  // namespace wf2g
 
-extern "C" void* wf2g_kernel_ptr_heur(int a2p, int cigar, int enc, int off_bytes);
-extern "C" void* wf2g_kernel_ptr_ef(int a2p, int cigar, int enc, int off_bytes);
-extern "C" void* wf2g_kernel_ptr_ef_heur(int a2p, int cigar, int enc, int off_bytes);
-extern "C" void* wf2g_kernel_ptr_wide(int a2p, int enc, int off_bytes, int heur);
-extern "C" void* wf2g_kernel_ptr_wide_ef(int a2p, int enc, int off_bytes, int heur);
+extern "C" void* wf2g_kernel_ptr_heur(int a2p, int cigar, int enc, int off_bytes, int lin);
+extern "C" void* wf2g_kernel_ptr_ef(int a2p, int cigar, int enc, int off_bytes, int lin);
+extern "C" void* wf2g_kernel_ptr_ef_heur(int a2p, int cigar, int enc, int off_bytes, int lin);
+extern "C" void* wf2g_kernel_ptr_wide(int a2p, int enc, int off_bytes, int heur, int lin);
+extern "C" void* wf2g_kernel_ptr_wide_ef(int a2p, int enc, int off_bytes, int heur, int lin);
 extern "C" int wf2g_fault_info_exact(unsigned long long* out);
 extern "C" int wf2g_fault_info_heur(unsigned long long* out);
 extern "C" int wf2g_fault_info_ef(unsigned long long* out);
@@ -34,19 +34,20 @@ extern "C" int wf2g_fault_info_wide(unsigned long long* out);
 extern "C" int wf2g_fault_info_wide_ef(unsigned long long* out);
 
 // Kernel variant for (affine2p?, full CIGAR?, 2- or 8-bit sequences, 2- or
-// 4-byte offsets, wf-adaptive heuristic?, a CTA per pair?, ends-free form?).
-// The CTA-per-pair variants exist for full-CIGAR runs only.
+// 4-byte offsets, wf-adaptive heuristic?, a CTA per pair?, ends-free form?,
+// single-component metric?).  The CTA-per-pair variants exist for full-CIGAR
+// runs only.
 extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide,
-                                 int ef) {
+                                 int ef, int lin) {
   if (wide) {
     if (!cigar) return nullptr;
-    return ef ? wf2g_kernel_ptr_wide_ef(a2p, enc, off_bytes, heur)
-              : wf2g_kernel_ptr_wide(a2p, enc, off_bytes, heur);
+    return ef ? wf2g_kernel_ptr_wide_ef(a2p, enc, off_bytes, heur, lin)
+              : wf2g_kernel_ptr_wide(a2p, enc, off_bytes, heur, lin);
   }
-  if (ef) return heur ? wf2g_kernel_ptr_ef_heur(a2p, cigar, enc, off_bytes)
-                      : wf2g_kernel_ptr_ef(a2p, cigar, enc, off_bytes);
-  if (heur) return wf2g_kernel_ptr_heur(a2p, cigar, enc, off_bytes);
-  return wf2g::align_kernel<false, 32, false>(a2p, cigar, enc, off_bytes);
+  if (ef) return heur ? wf2g_kernel_ptr_ef_heur(a2p, cigar, enc, off_bytes, lin)
+                      : wf2g_kernel_ptr_ef(a2p, cigar, enc, off_bytes, lin);
+  if (heur) return wf2g_kernel_ptr_heur(a2p, cigar, enc, off_bytes, lin);
+  return wf2g::align_kernel<false, 32, false>(a2p, cigar, enc, off_bytes, lin);
 }
 
 extern "C" void* wf2g_pool_init_ptr(void) { return (void*)wf2g::wfa_pool_init_kernel; }

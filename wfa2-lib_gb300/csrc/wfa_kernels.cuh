@@ -59,6 +59,11 @@ struct Penalties {
 
 struct KParams {
   Penalties pen;
+  // distance metric (wavefront/wavefront_penalties.h:42-48): 0 indel, 1 edit,
+  // 2 gap-linear -- one component, run on the gap-affine recurrence with e1 = 0
+  // and no I/D inputs, which is the same recurrence -- 3 gap-affine, 4
+  // gap-affine-2p
+  int metric;
   int max_steps;
   // wf-adaptive heuristic (0: none); min wavefront length, max distance
   // threshold, steps between cut-offs (wavefront/wavefront_heuristic.h:42-69)

@@ -9,7 +9,7 @@ namespace wf2g {
 WF2G_FAULT_READER(wf2g_fault_info_wide)
 }  // namespace wf2g
 
-extern "C" void* wf2g_kernel_ptr_wide(int a2p, int enc, int off_bytes, int heur) {
-  return heur ? wf2g::align_kernel<true, 256, false>(a2p, 1, enc, off_bytes)
-              : wf2g::align_kernel<false, 256, false>(a2p, 1, enc, off_bytes);
+extern "C" void* wf2g_kernel_ptr_wide(int a2p, int enc, int off_bytes, int heur, int lin) {
+  return heur ? wf2g::align_kernel<true, 256, false>(a2p, 1, enc, off_bytes, lin)
+              : wf2g::align_kernel<false, 256, false>(a2p, 1, enc, off_bytes, lin);
 }

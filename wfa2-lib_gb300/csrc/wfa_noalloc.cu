@@ -22,7 +22,7 @@
 
 namespace wf2g {
 extern "C" void* wf2g_kernel_ptr(int a2p, int cigar, int enc, int off_bytes, int heur, int wide,
-                                 int ef);
+                                 int ef, int lin);
 extern "C" int wf2g_seq_bytes(int enc, int max_len);
 }  // namespace wf2g
 
@@ -79,7 +79,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
             max_len, kNoAllocMaxLen);
     return -3;  // WF2G_ERR_ARGS
   }
-  if (cfg->metric != 3 && cfg->metric != 4) return -2;  // WF2G_ERR_CONFIG
+  if (cfg->metric != 3 && cfg->metric != 4) return -2;  // WF2G_ERR_CONFIG (gap-affine metrics only)
   if (cfg->ultralow) return -2;  // BiWFA allocates per recursion level
   if (cfg->endsfree) return -2;  // the ends-free kernels are not in the fixed-scratch set
   const bool cigar = !cfg->score_only;
@@ -94,6 +94,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   // penalties and ring geometry (the same layout the batch engine uses)
   KParams kp;
   memset(&kp, 0, sizeof(kp));
+  kp.metric = cfg->metric;
   Penalties& pen = kp.pen;
   pen.match = cfg->match;
   pen.x = cfg->x;
@@ -159,7 +160,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.gscratch = base + 256;
   // calls share the array: clear the queue head left by the previous call
   if (cudaMemsetAsync(queue, 0, sizeof(int32_t), st) != cudaSuccess) return -4;
-  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur, 0, 0);
+  void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur, 0, 0, 0);
   void* args[] = {(void*)&kp};
   const cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args,
                                          (size_t)kp.smem_per_group * wpc, st);

@@ -295,7 +295,8 @@ extern "C" void* wf2g_server_new(const wf2g_cfg_t* cfg, int64_t hbm_budget,
     return nullptr;
   }
   // the BiWFA fallback has no ends-free form (wavefront/wavefront_align.c:67-82)
-  if (!cfg || cfg->ultralow || cfg->endsfree) {
+  // and serves the gap-affine metrics only
+  if (!cfg || cfg->ultralow || cfg->endsfree || cfg->metric <= 2) {
     if (err) *err = WF2G_ERR_CONFIG_;
     return nullptr;
   }

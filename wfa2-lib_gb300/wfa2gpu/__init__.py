@@ -283,6 +283,10 @@ class Config:
         a.affine2p_penalties.gap_extension1 = self.gap_extension1
         a.affine2p_penalties.gap_opening2 = self.gap_opening2
         a.affine2p_penalties.gap_extension2 = self.gap_extension2
+        # gap-linear: the indel penalty is gap_opening1 (edit and indel take none)
+        a.linear_penalties.match = self.match
+        a.linear_penalties.mismatch = self.mismatch
+        a.linear_penalties.indel = self.gap_opening1
         a.heuristic.strategy = WF_HEURISTIC_NONE
         if self.wfadaptive:
             a.heuristic.strategy = WF_HEURISTIC_WFADAPTIVE
