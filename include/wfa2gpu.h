@@ -250,11 +250,21 @@ typedef enum {
   wf_align_biwfa_subsidiary = 4
 } wavefront_align_mode_t;
 
+/* The BiWFA sub-aligners (wavefront/wavefront_bialigner.h:43-54), as far as
+ * callers touch them (the reference's C++ binding tags their debug mode).
+ * The GPU path keeps no host sub-aligners: wavefront_aligner_t.bialigner is
+ * always NULL. */
+typedef struct {
+  wavefront_aligner_t* wf_forward;
+  wavefront_aligner_t* wf_reverse;
+  wavefront_aligner_t* wf_base;
+} wavefront_bialigner_t;
+
 /* wavefront/wfa.h:90-120.  The fields callers read (align_status, cigar,
- * alignment_scope, alignment_form, penalties, heuristic, memory_mode, system)
- * keep their names and types; the reference's CPU-only internals (wavefront
- * components, slab, mm_allocator, plot) are replaced by one opaque pointer to
- * the GPU engine. */
+ * alignment_scope, alignment_form, penalties, heuristic, memory_mode, system,
+ * bialigner) keep their names and types; the reference's CPU-only internals
+ * (wavefront components, slab, mm_allocator, plot) are replaced by one opaque
+ * pointer to the GPU engine. */
 typedef struct _wavefront_aligner_t {
   wavefront_align_mode_t align_mode;
   char* align_mode_tag;
@@ -266,6 +276,7 @@ typedef struct _wavefront_aligner_t {
   wavefront_memory_t memory_mode;
   cigar_t* cigar;
   alignment_system_t system;
+  wavefront_bialigner_t* bialigner; /* always NULL */
   void* engine; /* GPU engine (device, stream, slab); opaque */
 } wavefront_aligner_t;
 

@@ -129,7 +129,7 @@ class Aligner_t(C.Structure):
                 ("alignment_form", AlignmentForm), ("penalties", WavefrontPenalties),
                 ("heuristic", Heuristic), ("memory_mode", C.c_int),
                 ("cigar", C.POINTER(Cigar)), ("system", AlignmentSystem),
-                ("engine", C.c_void_p)]
+                ("bialigner", C.c_void_p), ("engine", C.c_void_p)]
 
 
 # exported symbols of include/wfa2gpu.h (checked by the CPU test-suite)
