@@ -574,9 +574,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     // (wavefront/wavefront_aligner.c:250-305)
     const int e_lo = (EF && cb == 0 && pen.match == 0) ? -pbf : 0;
     const int e_hi = (EF && cb == 0 && pen.match == 0) ? tbf : 0;
-    // ends-free: the first diagonal of the last extended M wavefront that
-    // reaches an end within the free lengths (INT32_MAX: none)
+    // the terminating diagonal of the last extended M wavefront (INT32_MAX:
+    // none): ends-free, the first one that reaches an end within the free
+    // lengths; end-to-end ending in M, k_end once its cell reaches (plen,
+    // tlen) -- found by the cell loop, so no step re-reads the row
     int ef_k = INT32_MAX;
+    const bool m_end = !EF && ce == 0;
     auto ef_done = [&](int off, int k) -> bool {
       const int vv = off - k;
       return (off >= tlen && plen - vv <= pef) || (vv >= plen && tlen - off <= tef);
@@ -596,6 +599,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
     } else {
       const int L0 = cb == 0 ? lcp<ENC>(P, T, 0, 0, min(plen, tlen), nwords, g_pair) : 0;
+      if (m_end && cb == 0 && plen == tlen && L0 >= tlen) ef_k = 0;  // k_end == 0
       if (t == 0) {
         const int r0 = comp_row(cb, 0, 0, 0);
         RING_ST(row(r0), 0, (OffT)L0);
@@ -622,14 +626,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       // component (wavefront/wavefront_termination.c:37-108); checked only
       // where M[s] exists (wavefront/wavefront_extend.c:93-106)
       if (m_exists) {
-        if (EF) {
-          // wavefront/wavefront_termination.c:115-162, in extension order
+        if (EF || m_end) {
+          // wavefront/wavefront_termination.c:37-60 (end-to-end: k_end's cell
+          // is in M[s]'s limits and has reached tlen) and :115-162 (ends-free,
+          // in extension order), as the cell loop found them
           if (ef_k != INT32_MAX) {
-            result = 1;
-            break;
-          }
-        } else if (ce == 0) {
-          if (mlo <= k_end && k_end <= mhi && RING_LD(row(curM), k_end) >= tlen) {
             result = 1;
             break;
           }
@@ -739,21 +740,31 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       // wavefront/wavefront_compute_affine.c:236-243: all inputs null -> null step
       if (!(vMx | vMo1 | vI1 | vD1 | vMo2 | vI2 | vD2)) {
         ++null_steps;
-        clear_outside<OffT, G>(oM, oldM, 1, 0, t, rb, g_pair);
-        clear_outside<OffT, G>(oI1, oldI1, 1, 0, t, rb, g_pair);
-        clear_outside<OffT, G>(oD1, oldD1, 1, 0, t, rb, g_pair);
-        if (A2P) {
-          clear_outside<OffT, G>(oI2, oldI2, 1, 0, t, rb, g_pair);
-          clear_outside<OffT, G>(oD2, oldD2, 1, 0, t, rb, g_pair);
-        }
-        group_sync<G>();
-        if (t == 0) {
-          meta[curM] = imeta[curM] = kEmpty;
-          meta[rowI1 + cur1] = imeta[rowI1 + cur1] = kEmpty;
-          meta[rowD1 + cur1] = imeta[rowD1 + cur1] = kEmpty;
+        // Exact runs read a row only within its limits, so a null step just
+        // empties the limits of the slots it takes over; they keep their old
+        // window, which the slot's next write (or the next pair) clears.
+        // Under the heuristic the windows are read too: clear them now.
+        if (HEUR) {
+          clear_outside<OffT, G>(oM, oldM, 1, 0, t, rb, g_pair);
+          clear_outside<OffT, G>(oI1, oldI1, 1, 0, t, rb, g_pair);
+          clear_outside<OffT, G>(oD1, oldD1, 1, 0, t, rb, g_pair);
           if (A2P) {
-            meta[rowI2 + cur2] = imeta[rowI2 + cur2] = kEmpty;
-            meta[rowD2 + cur2] = imeta[rowD2 + cur2] = kEmpty;
+            clear_outside<OffT, G>(oI2, oldI2, 1, 0, t, rb, g_pair);
+            clear_outside<OffT, G>(oD2, oldD2, 1, 0, t, rb, g_pair);
+          }
+          group_sync<G>();
+        }
+        if (t == 0) {
+          meta[curM] = kEmpty;
+          meta[rowI1 + cur1] = kEmpty;
+          meta[rowD1 + cur1] = kEmpty;
+          if (A2P) {
+            meta[rowI2 + cur2] = kEmpty;
+            meta[rowD2 + cur2] = kEmpty;
+          }
+          if (HEUR) {
+            imeta[curM] = imeta[rowI1 + cur1] = imeta[rowD1 + cur1] = kEmpty;
+            if (A2P) imeta[rowI2 + cur2] = imeta[rowD2 + cur2] = kEmpty;
           }
         }
         if (CIGAR) {
@@ -922,6 +933,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           if (prune) wmin = min(wmin, max(plen - v, tlen - best));
           mext = best + lcp<ENC>(P, T, v, best, min(plen - v, tlen - best), nwords, g_pair);
           if (EF && ef_done(mext, k)) qk = min(qk, k);
+          if (m_end && k == k_end && mext >= tlen) qk = k;
         }
         RING_ST(oM, k, (OffT)mext);
         RING_ST(oI1, k, (OffT)i1);
@@ -995,7 +1007,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         tloD2 = __reduce_min_sync(kFull, tloD2);
         thiD2 = __reduce_max_sync(kFull, thiD2);
       }
-      if (EF) qk = __reduce_min_sync(kFull, qk);
+      if (EF || m_end) qk = __reduce_min_sync(kFull, qk);
       if (prune) wmin = __reduce_min_sync(kFull, wmin);
       if (G > 32) {
         // across the group's warps: one barrier; the partials are next
@@ -1004,7 +1016,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (lane == 0) {
           pr[0] = tloM; pr[1] = thiM; pr[2] = tloI1; pr[3] = thiI1; pr[4] = tloD1; pr[5] = thiD1;
           if (A2P) { pr[6] = tloI2; pr[7] = thiI2; pr[8] = tloD2; pr[9] = thiD2; }
-          if (EF) pr[10] = qk;
+          if (EF || m_end) pr[10] = qk;
           if (prune) pr[11] = wmin;
         }
         __syncthreads();
@@ -1017,11 +1029,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
             tloI2 = min(tloI2, q[6]); thiI2 = max(thiI2, q[7]);
             tloD2 = min(tloD2, q[8]); thiD2 = max(thiD2, q[9]);
           }
-          if (EF) qk = min(qk, q[10]);
+          if (EF || m_end) qk = min(qk, q[10]);
           if (prune) wmin = min(wmin, q[11]);
         }
       }
-      if (EF) ef_k = qk;
+      if (EF || m_end) ef_k = qk;
       if (prune && thiM - tloM + 1 >= 1000) {
         // exact pruning of a wide end-to-end edit wavefront on its unextended
         // offsets (wavefront/wavefront_compute_edit.c:220-279): a diagonal's
