@@ -204,6 +204,7 @@ __device__ __forceinline__ void null_range(OffT* row, int a, int b, int t,
 template <typename OffT, int G>
 __device__ __forceinline__ void trim_fill(OffT* row, int lo, int hi, int tlo, int thi, int t,
                                           RingBounds rb, int g_pair) {
+  if (tlo == lo && thi == hi) return;  // nothing trimmed (the usual case)
   if (tlo > thi) {
     null_range<OffT, G>(row, lo, hi, t, rb, g_pair);
   } else {
@@ -216,7 +217,9 @@ __device__ __forceinline__ void trim_fill(OffT* row, int lo, int hi, int tlo, in
 template <typename OffT, int G>
 __device__ __forceinline__ void clear_outside(OffT* row, int2 old, int lo, int hi, int t,
                                               RingBounds rb, int g_pair) {
-  if (old.x <= old.y) {
+  // nothing outside [lo,hi] to clear when the old window lies inside it (the
+  // usual case: wavefronts grow) or is empty
+  if (old.x <= old.y && (old.x < lo || old.y > hi)) {
     null_range<OffT, G>(row, old.x, min(old.y, lo - 1), t, rb, g_pair);
     null_range<OffT, G>(row, max(old.x, hi + 1), old.y, t, rb, g_pair);
   }
