@@ -1065,9 +1065,8 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
   pen_t p;
   if (setup_penalties(cfg, &p) != 0) return -1;
   const int ultralow = (cfg[7] == 3);
-  /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82);
-   * its single-component metrics are not restated */
-  if (ultralow && (p.endsfree || p.metric <= 2)) return -1;
+  /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82) */
+  if (ultralow && p.endsfree) return -1;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel num_threads(nthreads)

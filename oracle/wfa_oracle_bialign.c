@@ -127,7 +127,7 @@ static void bp_overlap(const pen_t* p, oracle_ua_t* a0, oracle_ua_t* a1, int for
       const orow_t* i2_1 = row_or_null(a1->ws, si, C_I2);
       if (i2_0 && i2_1) bp_indel(plen, tlen, forward, score_0, si, i2_0, i2_1, C_I2, p->o2, bp);
     }
-    if (score_0 + si - p->o1 >= bp->score) continue;
+    if (p->metric >= 3 && score_0 + si - p->o1 >= bp->score) continue;
     const orow_t* d1_1 = row_or_null(a1->ws, si, C_D1);
     if (d1_0 && d1_1) bp_indel(plen, tlen, forward, score_0, si, d1_0, d1_1, C_D1, p->o1, bp);
     const orow_t* i1_1 = row_or_null(a1->ws, si, C_I1);
@@ -171,8 +171,8 @@ static int find_breakpoint_(bi_t* b, int pb, int pe, int tb, int te, int cb, int
     if (st) { *reached_score = R->s; return st; }
     if (R->s + F->s >= p->max_steps) return ST_MAX_STEPS;
   }
-  /* wavefront/wavefront_bialign.c:960-973 */
-  const int gap_opening = p->metric == 4 ? (p->o1 > p->o2 ? p->o1 : p->o2) : p->o1;
+  /* wavefront/wavefront_bialign.c:960-973 (0 for the single-component metrics) */
+  const int gap_opening = p->metric == 4 ? (p->o1 > p->o2 ? p->o1 : p->o2) : p->metric == 3 ? p->o1 : 0;
   const int scope = p->scope;
   while (1) {
     if (last_forward) {

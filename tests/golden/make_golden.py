@@ -101,6 +101,10 @@ SYNTHETIC = {
     "w6_edit_prune_score": (6, 12, "edit", True, 0, 3000, 200),
     "w5_indel_score": (5, 40, "indel", True, 0, 2000, 100),
     "w1_edit_ms50": (1, 100, "edit", False, 0, 0, 0, 50),
+    "w5_edit_biwfa_full": (5, 20, "edit", False, 3, 3000, 200),
+    "w6_edit_biwfa_full": (6, 8, "edit", False, 3, 3000, 150),
+    "w1_linear_biwfa_full": (1, 100, "linear", False, 3, 0, 0),
+    "w5_indel_biwfa_score": (5, 20, "indel", True, 3, 3000, 200),
 }
 
 # name: (workload, n, penalties, score_only, param, param2, form, wf-adaptive)

@@ -35,8 +35,6 @@ def test_oracle_matches_reference_goldens(oracle_mod, key):
             break
     mode, score_only = UT["modes"][prefix]
     pen = _pen(O, UT["penalty_sets"][name])
-    if mode == O.MEM_ULTRALOW and pen.metric <= O.GAP_LINEAR:
-        pytest.skip("BiWFA for the single-component metrics is not restated")
     pats, txts = helpers.utest_pairs()
     b = O.PairBatch.from_lists(pats, txts)
     r = O.align(b, pen, memory_mode=mode, score_only=score_only,
