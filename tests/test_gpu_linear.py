@@ -11,8 +11,9 @@ the edit driver's particulars:
 - end-to-end edit prunes wavefronts of 1000 or more diagonals;
 - edit and indel are not trimmed in the extension form.
 
-Golden coverage (the reference test-suite's edit/indel files, and reference
-outputs for gap-linear and the pruning cases) is in test_gpu_parity.py.
+Golden coverage (the reference test-suite's edit/indel files, BiWFA
+included, and reference outputs for gap-linear and the pruning cases) is in
+test_gpu_parity.py.
 Integer work: everything must be identical."""
 import pytest
 
@@ -104,13 +105,29 @@ def test_linear_metrics_dropin(gpu_available, wfa, oracle_mod):
         al.close()
 
 
+@pytest.mark.parametrize("name", sorted(PENS))
+@pytest.mark.parametrize("case", [(1, 100, 0, 0), (5, 12, 3000, 200), (6, 6, 3000, 150)])
+@pytest.mark.parametrize("score_only", [False, True])
+def test_linear_metrics_biwfa(gpu_available, wfa, oracle_mod, name, case, score_only):
+    """BiWFA (ultralow memory) for the single-component metrics: only M-to-M
+    breakpoints, no gap-open adjustment, edit pruning inside the breakpoint
+    searches and base cases (wavefront/wavefront_bialign.c:83-150, :878-973)."""
+    W, O = wfa, oracle_mod
+    wl, n, param, param2 = case
+    p = W.generate(wl, n, first=31, param=param, param2=param2)
+    pen = PENS[name]
+    got = _gpu(W, W.Config(**pen, memory_mode=W.MEM_ULTRALOW, score_only=score_only), p)
+    r = _oracle(O, pen, p, memory_mode=O.MEM_ULTRALOW, score_only=score_only)
+    for i in range(n):
+        assert got[i][:3] == (int(r.status[i]), int(r.score[i]), r.cigar(i)), (name, i)
+
+
 def test_linear_metrics_rejections(gpu_available, wfa):
-    """BiWFA serves the gap-affine metrics only; edit/indel begin-free lengths
-    are not served; serving takes the gap-affine metrics only."""
+    """Edit/indel begin-free lengths are not served; serving takes the
+    gap-affine metrics only."""
     W = wfa
     p = W.generate(1, 4, first=3)
-    for cfg in [W.Config(metric=1, memory_mode=W.MEM_ULTRALOW),
-                W.Config(metric=0, form=(5, 5, 5, 5))]:
+    for cfg in [W.Config(metric=0, form=(5, 5, 5, 5))]:
         al = W.Aligner(cfg)
         rc = al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)[0]
         al.close()

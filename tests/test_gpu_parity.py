@@ -58,8 +58,6 @@ def test_gpu_matches_reference_goldens(gpu_available, wfa, oracle_mod, key):
     prefix, name = _split_key(key)
     mode, score_only = UT["modes"][prefix]
     spec = UT["penalty_sets"][name]
-    if mode == W.MEM_ULTRALOW and spec[0] <= W.GAP_LINEAR:
-        pytest.skip("BiWFA serves the gap-affine metrics only")
     pats, txts = helpers.utest_pairs()
     batch = helpers.pack(pats, txts)
     scores, status, cig = run_batch(W, cfg_of(W, spec, score_only, mode, 0, HEUR.get(name)),
@@ -85,8 +83,6 @@ def test_gpu_matches_reference_on_synthetic(gpu_available, wfa, name):
     W = wfa
     fx = SY[name]
     spec = UT["penalty_sets"][fx["penalties"]]
-    if fx["memory_mode"] == W.MEM_ULTRALOW and spec[0] <= W.GAP_LINEAR:
-        pytest.skip("BiWFA serves the gap-affine metrics only")
     p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
     batch = (p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
     cfg = cfg_of(W, spec, fx["score_only"], fx["memory_mode"], fx.get("max_steps", 0),

@@ -353,8 +353,6 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
      * begin-free diagonals as sourceless: not computed */
     if (!cfg->extension && p->distance_metric <= edit && (cfg->pbf > 0 || cfg->tbf > 0)) return -1;
   }
-  /* BiWFA serves the gap-affine metrics only */
-  if (lin && cfg->ultralow) return -1;
   /* the user's penalties, for maximal-score trimming (wavefront/wavefront_aligner.c:664-676) */
   if (lin) {
     cfg->um = p->linear_penalties.match;

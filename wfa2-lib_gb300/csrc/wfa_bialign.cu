@@ -32,7 +32,7 @@ namespace {
 
 constexpr int kBiMaxThreads = 512;
 constexpr int kBiMaxWarps = kBiMaxThreads / 32;
-constexpr int kRed = 11;  // per step: (trimmed lo, hi) x 5 components + max antidiagonal
+constexpr int kRed = 12;  // per step: (trimmed lo, hi) x 5 components, max antidiagonal, edit pruning
 
 struct BiShared {
   int red[2][kBiMaxWarps][kRed];  // per-warp partials, alternating per step
@@ -241,11 +241,16 @@ struct BiCtx {
     const int s1 = s[d] + 1;
     const int slot = s1 % scope;
     const int2 E = make_int2(1, 0);
+    // single-component metrics (wavefront/wavefront_compute_edit.c,
+    // wavefront/wavefront_compute_linear.c): no I/D inputs; indel has no
+    // mismatch; end-to-end edit prunes wide wavefronts
+    const bool lin = p.metric <= 2;
+    const bool prune = p.metric == 1;
     auto in = [&](int c, int sc) -> int2 { return sc >= 0 ? mt(d, c, sc % scope) : E; };
-    const int2 eMx = in(kCompM, s1 - pen.x);
+    const int2 eMx = p.metric != 0 ? in(kCompM, s1 - pen.x) : E;
     const int2 eMo1 = in(kCompM, s1 - pen.o1 - pen.e1);
-    const int2 eI1 = in(kCompI1, s1 - pen.e1);
-    const int2 eD1 = in(kCompD1, s1 - pen.e1);
+    const int2 eI1 = lin ? E : in(kCompI1, s1 - pen.e1);
+    const int2 eD1 = lin ? E : in(kCompD1, s1 - pen.e1);
     int2 eMo2 = E, eI2 = E, eD2 = E;
     if (A2P) {
       eMo2 = in(kCompM, s1 - pen.o2 - pen.e2);
@@ -311,6 +316,20 @@ struct BiCtx {
       if (vI2) rI2 = row(d, kCompI2, (s1 - pen.e2) % scope);
       if (vD2) rD2 = row(d, kCompD2, (s1 - pen.e2) % scope);
     }
+    // edit and indel NULL the two elements beyond each end of M[s-1]
+    // (wavefront/wavefront_compute_edit.c:352-356): only cells a cut-off left
+    // in the initialised window can hold values there
+    if (p.heur && p.metric <= 1 && vMo1) {
+      if (tid == 0) {
+        const int sl = (s1 - pen.o1) % scope;
+        const int2 w = wm(d, kCompM, sl);
+        int32_t* const r = row(d, kCompM, sl);
+        const int ks[4] = {eMo1.x - 2, eMo1.x - 1, eMo1.y + 1, eMo1.y + 2};
+        for (int j = 0; j < 4; ++j)
+          if (ks[j] >= w.x && ks[j] <= w.y) r[ks[j]] = kNull;
+      }
+      __syncthreads();
+    }
     int32_t* const oM = row(d, kCompM, slot);
     int32_t* const oI1 = row(d, kCompI1, slot);
     int32_t* const oD1 = row(d, kCompD1, slot);
@@ -324,6 +343,7 @@ struct BiCtx {
       th[c] = INT_MIN;
     }
     int mak = 0;
+    int wmin = INT_MAX;  // edit pruning: best worst case over the unextended cells
     // kU cells per thread per iteration: every input load of the group is
     // issued before the first compute, and the first extend window of each
     // M cell is fetched for the whole group before any is compared
@@ -377,6 +397,7 @@ struct BiCtx {
         int32_t mext = kNull;
         if (okm[j]) {
           const int v = best - k;
+          if (prune) wmin = min(wmin, max(plen - v, tlen - best));
           const int lim = min(plen - v, tlen - best);
           int L;
           if (!enc2) L = lcp(d, v, best, lim);
@@ -407,6 +428,7 @@ struct BiCtx {
       th[c] = __reduce_max_sync(kFull, th[c]);
     }
     mak = __reduce_max_sync(kFull, mak);
+    if (prune) wmin = __reduce_min_sync(kFull, wmin);
     // partials of this step in buffer rsel: a warp reads them after the
     // barrier below and writes the other buffer next step, and no warp can
     // write this buffer again before every warp passed the next barrier
@@ -418,12 +440,13 @@ struct BiCtx {
         red[warp][2 * c + 1] = th[c];
       }
       red[warp][2 * NC] = mak;
+      red[warp][2 * NC + 1] = wmin;
     }
     __syncthreads();
     // every warp reduces the partials itself (the same values everywhere)
     int v = 0;
-    if (lane <= 2 * NC) {
-      const bool is_lo = (lane < 2 * NC) && !(lane & 1);
+    if (lane <= 2 * NC + 1) {
+      const bool is_lo = (lane < 2 * NC && !(lane & 1)) || lane == 2 * NC + 1;
       v = red[0][lane];
       for (int w = 1; w < nwarps; ++w) {
         const int x = red[w][lane];
@@ -439,6 +462,27 @@ struct BiCtx {
       nm[c] = a > b ? E : make_int2(a, b);
     }
     const int mk = __shfl_sync(kFull, v, 2 * NC);
+    if (lin) nm[kCompI1] = nm[kCompD1] = E;  // one component: no gap wavefronts
+    if (prune && nm[kCompM].y - nm[kCompM].x + 1 >= 1000) {
+      // exact pruning of a wide edit wavefront on its unextended offsets
+      // (wavefront/wavefront_compute_edit.c:220-279); every thread derives
+      // the same limits
+      const int wm_ = __shfl_sync(kFull, v, 2 * NC + 1);
+      const int tlo = nm[kCompM].x, thi = nm[kCompM].y;
+      const int sk = tlo + (thi - tlo) / 2;
+      int32_t so = max(rMo1[sk + 1], max(rMx[sk], rMo1[sk - 1]) + 1);
+      if (!((uint32_t)so <= (uint32_t)tlen && (uint32_t)(so - sk) <= (uint32_t)plen)) so = -1;
+      if (so >= 0) {
+        const int smax = max(plen - (so - sk), tlen - so);
+        if (!(abs(tlo - k_end) <= smax && abs(thi - k_end) <= smax)) {
+          const int a = max(tlo, k_end - wm_);
+          const int nlo = (a <= min(thi, k_end + wm_)) ? a : thi + 1;
+          const int b = min(thi, k_end + wm_);
+          const int nhi = (b > nlo && b >= k_end - wm_) ? b : nlo;
+          nm[kCompM] = nlo > nhi ? E : make_int2(nlo, nhi);
+        }
+      }
+    }
     // warp 0 NULLs the trimmed ends and publishes the limits; the next step
     // reads neither when every input lies two or more scores back (one_bar),
     // otherwise a second barrier orders them
@@ -703,7 +747,8 @@ struct BiCtx {
     }
     // wavefront/wavefront_bialign.c:960-973
     const Penalties& pen = p.pen;
-    const int gap_opening = A2P ? max(pen.o1, pen.o2) : pen.o1;
+    // wavefront/wavefront_bialign.c:960-973 (0 for the single-component metrics)
+    const int gap_opening = A2P ? max(pen.o1, pen.o2) : p.metric == 3 ? pen.o1 : 0;
     BP bp;
     bp.score = INT_MAX;
     bp.score_f = bp.score_r = bp.k_f = bp.off_f = bp.comp = 0;

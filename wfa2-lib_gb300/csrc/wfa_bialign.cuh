@@ -36,6 +36,10 @@ struct BiOut {
 
 struct BiParams {
   Penalties pen;  // x, o1, e1, o2, e2 as in the unidirectional kernel
+  // distance metric: 0 indel, 1 edit, 2 gap-linear (one component: the
+  // gap-affine recurrence with e1 = 0 and no I/D inputs), 3 gap-affine,
+  // 4 gap-affine-2p
+  int metric;
   int scope;      // max_score_scope: ring depth of every component
   int max_steps;
   // wf-adaptive heuristic of the forward/reverse searches (0: none)

@@ -75,6 +75,7 @@ struct Node {
 
 int classic_score(const wf2g_cfg_t& c, int plen, int tlen, int s) {
   // wavefront/wavefront_compute.c:108-120
+  if (c.metric <= 1) return s;  // edit and indel: the distance itself
   if (c.match == 0) return -s;
   return ((-c.match) * (plen + tlen) - s) / 2;
 }
@@ -124,6 +125,7 @@ int run_breakpoints(Ctx& C, const std::vector<BiSeg>& segs, std::vector<BiOut>& 
   BiParams bp;
   memset(&bp, 0, sizeof(bp));
   bp.pen = pen;
+  bp.metric = C.cfg.metric;
   bp.scope = scope;
   bp.max_steps = C.cfg.max_steps;
   // the forward/reverse searches inherit the heuristic

@@ -348,8 +348,6 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
   if (n < 0 || !cfg) return WF2G_ERR_ARGS_;
   if (n == 0) return WF2G_OK_;
   if (cfg->metric < 0 || cfg->metric > 4) return WF2G_ERR_CONFIG_;
-  // BiWFA serves the gap-affine metrics only
-  if (cfg->ultralow && cfg->metric <= 2) return WF2G_ERR_CONFIG_;
   const bool cigar = !cfg->score_only;
   if (cigar && (!ops || !ops_off || !ops_len)) return WF2G_ERR_ARGS_;
   cudaSetDevice(E->device);
