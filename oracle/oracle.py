@@ -30,6 +30,7 @@ INDEL, EDIT, GAP_LINEAR = 0, 1, 2
 GAP_AFFINE = 3
 GAP_AFFINE_2P = 4
 MEM_HIGH, MEM_MED, MEM_LOW, MEM_ULTRALOW = 0, 1, 2, 3
+FLAG_STALE_SOURCE, FLAG_OVER_BOUND = 1, 2
 
 
 @dataclass
@@ -47,12 +48,18 @@ class Penalties:
     gap_extension2: int = 1
 
     def cfg(self, memory_mode=MEM_HIGH, score_only=False, max_steps=0, wfadaptive=None,
-            form=None):
+            form=None, heuristic=None):
         """wfadaptive: None, or (min_wavefront_length, max_distance_threshold,
         steps_between_cutoffs) of the wf-adaptive heuristic.
         form: None (end-to-end), "extension", or the ends-free lengths
-        (pattern_begin_free, pattern_end_free, text_begin_free, text_end_free)."""
+        (pattern_begin_free, pattern_end_free, text_begin_free, text_end_free).
+        heuristic: None, or a Heuristic (any strategy set; overrides wfadaptive)."""
         h = [1, *wfadaptive] if wfadaptive else [0, 0, 0, 0]
+        hx = [0, 0, 0, 0, 0]
+        if heuristic is not None and heuristic.strategy:
+            hz = heuristic
+            h = [0, hz.min_wavefront_length, hz.max_distance_threshold, hz.steps_between_cutoffs]
+            hx = [hz.strategy, hz.xdrop, hz.zdrop, hz.min_k, hz.max_k]
         if form is None:
             f = [0, 0, 0, 0, 0, 0]
         elif form == "extension":
@@ -62,7 +69,27 @@ class Penalties:
         return np.array(
             [self.metric, self.match, self.mismatch, self.gap_opening1, self.gap_extension1,
              self.gap_opening2, self.gap_extension2, memory_mode, int(bool(score_only)),
-             max_steps, *h, *f], dtype=np.int32)
+             max_steps, *h, *f, *hx], dtype=np.int32)
+
+
+# wavefront/wavefront_heuristic.h:41-49
+HS_BANDED_STATIC, HS_BANDED_ADAPTIVE, HS_WFADAPTIVE = 0x01, 0x02, 0x04
+HS_XDROP, HS_ZDROP, HS_WFMASH = 0x10, 0x20, 0x40
+
+
+@dataclass
+class Heuristic:
+    """A heuristic strategy (bit set of HS_*) and its parameters, as the
+    reference's wavefront_heuristic_t holds them."""
+
+    strategy: int = 0
+    min_wavefront_length: int = 0
+    max_distance_threshold: int = 0
+    steps_between_cutoffs: int = 1
+    xdrop: int = 0
+    zdrop: int = 0
+    min_k: int = 0
+    max_k: int = 0
 
 
 def build(ref: bool = False) -> None:
@@ -80,9 +107,13 @@ def _lib(kind: str):
     if not os.path.exists(path):
         build(ref=(kind != "port"))
     lib = ctypes.CDLL(path)
-    fn = lib.oracle_align_batch if kind == "port" else lib.ref_align_batch
     P = ctypes.c_void_p
-    fn.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+    if kind == "port":
+        fn = lib.oracle_align_batch_flags
+        fn.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+    else:
+        fn = lib.ref_align_batch
+        fn.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
     fn.restype = ctypes.c_int
     _LIBS[kind] = fn
     return fn
@@ -149,17 +180,23 @@ class AlignResult:
     cells: np.ndarray
     ext: np.ndarray
     end: np.ndarray = None  # (n, 2) int32: cigar->end_v, cigar->end_h
+    # ORACLE_FLAG_* bits (port only): FLAG_STALE_SOURCE marks a back-trace that
+    # read a wavefront a heuristic cut had emptied
+    flags: np.ndarray = None
 
     def cigar(self, i) -> str:
+        if self.ops_len[i] < 0:
+            return "<longer than plen+tlen>"
         o = int(self.ops_off[i])
         return self.ops[o:o + int(self.ops_len[i])].tobytes().decode()
 
 
 def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=False,
-          max_steps=0, kind="port", nthreads=0, wfadaptive=None, form=None) -> AlignResult:
+          max_steps=0, kind="port", nthreads=0, wfadaptive=None, form=None,
+          heuristic=None) -> AlignResult:
     fn = _lib(kind)
     n = batch.n
-    cfg = pen.cfg(memory_mode, score_only, max_steps, wfadaptive, form)
+    cfg = pen.cfg(memory_mode, score_only, max_steps, wfadaptive, form, heuristic)
     score = np.zeros(n, np.int32)
     status = np.zeros(n, np.int32)
     ops_off = batch.ops_offsets()
@@ -172,12 +209,16 @@ def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=Fal
     def ptr(a):
         return a.ctypes.data_as(ctypes.c_void_p)
 
-    rc = fn(ptr(cfg), n, ptr(batch.seqs), ptr(batch.p_off), ptr(batch.p_len), ptr(batch.t_off),
+    flags = np.zeros(n, np.int32)
+    args = [ptr(cfg), n, ptr(batch.seqs), ptr(batch.p_off), ptr(batch.p_len), ptr(batch.t_off),
             ptr(batch.t_len), ptr(score), ptr(status), ptr(ops), ptr(ops_off), ptr(ops_len),
-            ptr(cells), ptr(ext), ptr(end), int(nthreads))
+            ptr(cells), ptr(ext), ptr(end)]
+    if kind == "port":
+        args.append(ptr(flags))
+    rc = fn(*args, int(nthreads))
     if rc != 0:
         raise ValueError("invalid configuration for the CPU checker")
-    return AlignResult(score, status, ops, ops_off, ops_len, cells, ext, end)
+    return AlignResult(score, status, ops, ops_off, ops_len, cells, ext, end, flags)
 
 
 # ---------------------------------------------------------------- formats

@@ -50,11 +50,16 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
   attr.memory_mode = (wavefront_memory_t)cfg[7];
   attr.alignment_scope = cfg[8] ? compute_score : compute_alignment;
   attr.heuristic.strategy = wf_heuristic_none;
-  if (cfg[10] == 1) {
-    attr.heuristic.strategy = wf_heuristic_wfadaptive;
+  if (cfg[10] == 1 || cfg[20] != 0) {
+    /* cfg[20]: a wf_heuristic_strategy bit set; cfg[10] == 1 alone: wf-adaptive */
+    attr.heuristic.strategy = cfg[20] != 0 ? (wf_heuristic_strategy)cfg[20] : wf_heuristic_wfadaptive;
     attr.heuristic.min_wavefront_length = cfg[11];
     attr.heuristic.max_distance_threshold = cfg[12];
     attr.heuristic.steps_between_cutoffs = cfg[13];
+    attr.heuristic.xdrop = cfg[21];
+    attr.heuristic.zdrop = cfg[22];
+    attr.heuristic.min_k = cfg[23];
+    attr.heuristic.max_k = cfg[24];
   }
   if (cfg[9] > 0) attr.system.max_alignment_steps = cfg[9];
   if (cfg[14] == 1) {
@@ -97,8 +102,12 @@ int ref_align_batch(const int* cfg, int num_pairs, const char* sequences, const 
       if (!cfg[8] && out_ops != NULL &&
           (wf->align_status.status == 0 || wf->align_status.status == 1)) {
         const int n = cg->end_offset - cg->begin_offset;
-        memcpy(out_ops + ops_off[i], cg->operations + cg->begin_offset, (size_t)n);
-        out_ops_len[i] = n;
+        if (n > p_len[i] + t_len[i]) {
+          out_ops_len[i] = -1; /* longer than the caller's buffer */
+        } else {
+          memcpy(out_ops + ops_off[i], cg->operations + cg->begin_offset, (size_t)n);
+          out_ops_len[i] = n;
+        }
       } else {
         out_ops_len[i] = 0;
       }

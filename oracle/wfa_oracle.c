@@ -104,11 +104,18 @@ static int setup_penalties(const int* cfg, pen_t* p) {
 common:
   p->score_only = cfg[8] != 0;
   p->max_steps = cfg[9] > 0 ? cfg[9] : INT_MAX;
-  /* wavefront/wavefront_heuristic.c:44-55 */
-  p->heur = cfg[10] == 1;
+  /* wavefront/wavefront_heuristic.c:40-113: cfg[20] is the strategy bit set
+   * (cfg[10] == 1 alone is the wf-adaptive shorthand), then its parameters */
+  p->heur = cfg[20] != 0 ? cfg[20] : (cfg[10] == 1 ? HS_WFADAPTIVE : 0);
   p->h_min_len = cfg[11];
   p->h_max_dist = cfg[12];
   p->h_steps = cfg[13];
+  p->h_xdrop = cfg[21];
+  p->h_zdrop = cfg[22];
+  p->h_min_k = cfg[23];
+  p->h_max_k = cfg[24];
+  /* drops with edit/indel: the reference exits (wavefront/wavefront_align.c:83-89) */
+  if ((p->heur & (HS_XDROP | HS_ZDROP)) && p->metric <= 1) return -1;
   /* alignment form (wavefront/wavefront_attributes.h:55-69) */
   p->endsfree = cfg[14] == 1;
   p->pbf = cfg[15];
@@ -215,12 +222,16 @@ static orow_t* fetch(oracle_ws_t* ws, orow_t* nullrow, int s, int c) {
  * initialised window so the compute loop reads [lo,hi] without peeling. */
 static void init_ends(orow_t* r, int lo, int hi) {
   if (r->null) return;
+  /* the pad starts beyond both the window and the limits: an ends-free
+   * start keeps the window [0,0] inside wider limits */
   if (r->ilo > lo) {
-    for (int k = lo; k < r->ilo; ++k) r->off[k] = WF_NULL;
+    const int end = imin(r->ilo, r->lo);
+    for (int k = lo; k < end; ++k) r->off[k] = WF_NULL;
     r->ilo = lo;
   }
   if (r->ihi < hi) {
-    for (int k = r->ihi + 1; k <= hi; ++k) r->off[k] = WF_NULL;
+    const int start = imax(r->ihi, r->hi) + 1;
+    for (int k = start; k <= hi; ++k) r->off[k] = WF_NULL;
     r->ihi = hi;
   }
 }
@@ -292,7 +303,7 @@ static void edit_exact_prune(orow_t* r, int plen, int tlen) {
 static int64_t compute_step_linear(oracle_ws_t* ws, const pen_t* p, int s, int plen, int tlen,
                                    int* null_steps, int endsfree) {
   ws_ensure_rows(ws, s);
-  orow_t nullrow = {1, 1, 1, -1, 1, -1, kbuf_at0(&ws->nullbuf)};
+  orow_t nullrow = {.exists = 1, .null = 1, .lo = 1, .hi = -1, .ilo = 1, .ihi = -1, .off = kbuf_at0(&ws->nullbuf)};
   const int editlike = p->metric <= 1;
   orow_t* mx = editlike ? (p->metric == 1 ? fetch(ws, &nullrow, s - 1, C_M) : &nullrow)
                         : fetch(ws, &nullrow, s - p->x, C_M);
@@ -367,7 +378,7 @@ static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, in
   if (p->metric <= 2) return compute_step_linear(ws, p, s, plen, tlen, null_steps, endsfree);
   const int a2p = (p->metric == 4);
   ws_ensure_rows(ws, s);
-  orow_t nullrow = {1, 1, 1, -1, 1, -1, kbuf_at0(&ws->nullbuf)};
+  orow_t nullrow = {.exists = 1, .null = 1, .lo = 1, .hi = -1, .ilo = 1, .ihi = -1, .off = kbuf_at0(&ws->nullbuf)};
   orow_t* mx = fetch(ws, &nullrow, s - p->x, C_M);
   orow_t* mo1 = fetch(ws, &nullrow, s - p->o1 - p->e1, C_M);
   orow_t* i1e = fetch(ws, &nullrow, s - p->e1, C_I1);
@@ -532,8 +543,26 @@ static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
 
 /* wavefront/wavefront_backtrace.c:320-529, writing into a reversed buffer.
  * Returns the number of operations, or -1 on an inconsistent trace. */
+#define PUT(c)            \
+  do {                    \
+    if (n >= cap) return -1; \
+    rev[n++] = (c);       \
+  } while (0)
+/* wavefront/wavefront_backtrace.c:76-100 moves the CIGAR's begin by the
+ * count first: a negative count (a source ahead of the cell, read from a
+ * wavefront a cut emptied) takes back that many operations */
+#define MATCHES(cnt)                               \
+  do {                                             \
+    const int nm_ = (cnt);                         \
+    if (nm_ < 0) {                                 \
+      n += nm_;                                    \
+      if (n < 0) return -1;                        \
+    } else {                                       \
+      for (int i_ = 0; i_ < nm_; ++i_) PUT('M');   \
+    }                                              \
+  } while (0)
 static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int score, int k_end,
-                     int32_t off_end, int comp_end, char* rev) {
+                     int32_t off_end, int comp_end, char* rev, int cap, int* stale) {
   int n = 0;
   int mat = comp_end;
   int s = score, k = k_end;
@@ -543,8 +572,8 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
   /* ending deletions, then insertions: the free end of an ends-free alignment
    * (wavefront/wavefront_backtrace.c:346-356); none end-to-end (v==plen, h==tlen) */
   if (comp_end == C_M) {
-    for (int i = plen - v; i > 0; --i) rev[n++] = 'D';
-    for (int i = tlen - h; i > 0; --i) rev[n++] = 'I';
+    for (int i = plen - v; i > 0; --i) PUT('D');
+    for (int i = tlen - h; i > 0; --i) PUT('I');
   }
   while (v > 0 && h > 0 && s > 0) {
     const int sx = s - p->x, so1 = s - p->o1 - p->e1, so2 = s - p->o2 - p->e2;
@@ -558,15 +587,16 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
       mall = max64(misms, max64(cand(ws, sg, C_M, k - 1, 1, BT_I1O), cand(ws, sg, C_M, k + 1, 0, BT_D1O)));
       if (mall < 0) break;
       const int moff = (int)(mall >> 4);
-      for (int i = offset - moff; i > 0; --i) rev[n++] = 'M';
+      MATCHES(offset - moff);
       offset = moff;
       v = offset - k;
       h = offset;
       if (v <= 0 || h <= 0) break;
       const int type = (int)(mall & 0xF);
-      if (type == BT_M) { s = sx; rev[n++] = 'X'; --offset; }
-      else if (type == BT_I1O) { s = sg; rev[n++] = 'I'; --k; --offset; }
-      else { s = sg; rev[n++] = 'D'; ++k; }
+      if (type == BT_M) { s = sx; PUT('X'); --offset; }
+      else if (type == BT_I1O) { s = sg; PUT('I'); --k; --offset; }
+      else { s = sg; PUT('D'); ++k; }
+      if (row_at(ws, s, C_M)->cut_null) *stale = 1;
       v = offset - k;
       h = offset;
       continue;
@@ -601,8 +631,7 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
     if (mall < 0) break;
     if (mat == C_M) {
       const int moff = (int)(mall >> 4);
-      const int nm = offset - moff;
-      for (int i = 0; i < nm; ++i) rev[n++] = 'M';
+      MATCHES(offset - moff);
       offset = moff;
       v = offset - k;
       h = offset;
@@ -621,10 +650,11 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
       case BT_D2E: s = se2; mat = C_D2; break;
       default: return -1;
     }
+    if (row_at(ws, s, mat)->cut_null) *stale = 1;
     switch (type) {
-      case BT_M: rev[n++] = 'X'; --offset; break;
-      case BT_I1O: case BT_I1E: case BT_I2O: case BT_I2E: rev[n++] = 'I'; --k; --offset; break;
-      default: rev[n++] = 'D'; ++k; break;
+      case BT_M: PUT('X'); --offset; break;
+      case BT_I1O: case BT_I1E: case BT_I2O: case BT_I2E: PUT('I'); --k; --offset; break;
+      default: PUT('D'); ++k; break;
     }
     v = offset - k;
     h = offset;
@@ -632,17 +662,19 @@ static int backtrace(oracle_ws_t* ws, const pen_t* p, int plen, int tlen, int sc
   if (mat == C_M) {
     if (v > 0 && h > 0) {
       const int nm = imin(v, h);
-      for (int i = 0; i < nm; ++i) rev[n++] = 'M';
+      for (int i = 0; i < nm; ++i) PUT('M');
       v -= nm;
       h -= nm;
     }
-    while (v > 0) { rev[n++] = 'D'; --v; }
-    while (h > 0) { rev[n++] = 'I'; --h; }
+    while (v > 0) { PUT('D'); --v; }
+    while (h > 0) { PUT('I'); --h; }
   } else if (v != 0 || h != 0 || (s != 0 && p->match == 0)) {
     return -1;
   }
   return n;
 }
+#undef PUT
+#undef MATCHES
 
 /* wavefront/wavefront_compute.c:108-120 (edit and indel: the distance) */
 static int classic_score(const pen_t* p, int plen, int tlen, int s) {
@@ -650,6 +682,15 @@ static int classic_score(const pen_t* p, int plen, int tlen, int s) {
   if (p->match == 0) return -s;
   const int swg_match = -p->match;
   return (swg_match * (plen + tlen) - s) / 2;
+}
+
+/* classic_score in the reference's int arithmetic, which wraps for the NULL
+ * end position of an alignment that ran out of wavefronts */
+static int classic_score_wrapped(const pen_t* p, int v, int h, int s) {
+  if (p->metric <= 1) return s;
+  if (p->match == 0) return -s;
+  const uint32_t sum = (uint32_t)v + (uint32_t)h;
+  return (int)((uint32_t)(-p->match) * sum - (uint32_t)s) / 2;
 }
 
 /* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273). */
@@ -685,6 +726,12 @@ void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const cha
   ua->ext = 0;
   ua->heur = p->heur;
   ua->steps_wait = p->h_steps;
+  ua->max_sw = 0;
+  ua->max_sw_k = INT32_MAX; /* DPMATRIX_DIAGONAL_NULL */
+  ua->max_sw_off = WF_NULL;
+  ua->max_wf_score = -1;
+  ua->zdropped = 0;
+  ua->stale_source = 0;
   ua->endsfree = 0;
   ua->pbf = ua->pef = ua->tbf = ua->tef = 0;
   ua->end_k = tlen - plen;
@@ -709,9 +756,9 @@ void oracle_ua_start(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const cha
 /* Ends-free start (wavefront/wavefront_aligner.c:250-305): with match 0 the
  * score-0 M wavefront spans [-pattern_begin_free, text_begin_free], diagonal
  * k > 0 starting at (v,h) = (0,k) and k < 0 at (-k,0).  Its initialised window
- * stays [0,0]: compute steps NULL-pad only beyond max(window, limits)
- * (wavefront/wavefront_compute.c:498-527), so the oracle keeps the limits as
- * its window, which reads the same. */
+ * stays [0,0]: compute steps NULL-pad only beyond min/max(window, limits)
+ * (wavefront/wavefront_compute.c:498-527), so cells a heuristic cut from the
+ * limits before the first such pad are NULLed by it. */
 void oracle_ua_start_endsfree(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, const char* P,
                               int plen, const char* T, int tlen, int pbf, int pef, int tbf,
                               int tef) {
@@ -733,36 +780,44 @@ void oracle_ua_start_endsfree(oracle_ua_t* ua, oracle_ws_t* ws, const pen_t* p, 
   r0->off = row_storage(ws, 0, C_M, ws->hlo, ws->hhi);
   r0->exists = 1;
   r0->null = 0;
-  r0->lo = r0->ilo = lo;
-  r0->hi = r0->ihi = hi;
+  r0->lo = lo;
+  r0->hi = hi;
+  r0->ilo = r0->ihi = 0;
   for (int k = lo; k <= hi; ++k) r0->off[k] = k > 0 ? k : 0;
 }
 
-/* wf-adaptive cut-off of M[s] after its extension
- * (wavefront/wavefront_heuristic.c:229-289, dispatcher :506-566).  Only the
- * limits shrink: the cut offsets stay inside the initialised window, where
- * later compute steps (wavefront/wavefront_compute.c:498-527 pads only beyond
- * it) and the back-trace (wavefront/wavefront_backtrace.c:63-75) still read
- * them.  I/D rows of the same score take the intersection of limits. */
-static void wfadaptive_cutoff(oracle_ua_t* ua) {
-  oracle_ws_t* ws = ua->ws;
+/* Wrapping int32 arithmetic: the reference computes these differences in
+ * int, where the NULL offsets and an INT_MIN maximum can overflow. */
+static int wsub(int a, int b) { return (int)((uint32_t)a - (uint32_t)b); }
+
+/* Distance of a cell to the end (wavefront/wavefront_heuristic.c:125-145);
+ * wfmash weighs each side by its length. */
+static int hs_distance(const oracle_ua_t* ua, int k, int32_t off, int wfmash) {
+  if (off < 0) return -WF_NULL;
+  const int plen = ua->plen, tlen = ua->tlen;
+  const int v = off - k, h = off;
+  if (!wfmash) return imax(plen - v, tlen - h);
+  const int mfactor = (int)((float)(plen + tlen) / 2);
+  const int left_v = (int)((float)(plen - v) / plen * mfactor);
+  const int left_h = (int)((float)(tlen - h) / tlen * mfactor);
+  return imax(left_v, left_h);
+}
+
+/* wf-adaptive and wfmash (wavefront/wavefront_heuristic.c:229-289): cells
+ * further than max_distance_threshold beyond the closest are cut from both
+ * ends, keeping the end diagonal's side. */
+static void hs_wfadaptive(oracle_ua_t* ua, orow_t* m, int wfmash) {
   const pen_t* p = ua->p;
-  orow_t* m = row_at(ws, ua->s, C_M);
-  if (!m->exists || m->lo > m->hi) return;
-  --ua->steps_wait;
   if (ua->steps_wait > 0) return;
   const int lo = m->lo, hi = m->hi;
   if (hi - lo + 1 < p->h_min_len) return;
-  const int plen = ua->plen, tlen = ua->tlen;
   int* dist = (int*)malloc((size_t)(hi - lo + 1) * sizeof(int));
-  int min_d = imax(plen, tlen);
+  int min_d = imax(ua->plen, ua->tlen);
   for (int k = lo; k <= hi; ++k) {
-    const int32_t off = m->off[k];
-    const int d = off >= 0 ? imax(plen - (off - k), tlen - off) : -WF_NULL;
-    dist[k - lo] = d;
-    min_d = imin(min_d, d);
+    dist[k - lo] = hs_distance(ua, k, m->off[k], wfmash);
+    min_d = imin(min_d, dist[k - lo]);
   }
-  const int k_a = tlen - plen;
+  const int k_a = ua->tlen - ua->plen;
   const int top = imin(k_a, hi);
   int nlo = lo;
   for (int k = lo; k < top; ++k) {
@@ -776,19 +831,166 @@ static void wfadaptive_cutoff(oracle_ua_t* ua) {
     --nhi;
   }
   free(dist);
-  ua->steps_wait = p->h_steps;
-  if (nlo == lo && nhi == hi) return;
   m->lo = nlo;
   m->hi = nhi;
-  if (nlo > nhi) m->null = 1;
+  ua->steps_wait = p->h_steps;
+}
+
+/* SW-style score of every cell (wavefront/wavefront_heuristic.c:294-325,
+ * wavefront/wavefront_penalties.h:73) and the first maximum. */
+static int* hs_sw_scores(const oracle_ua_t* ua, const orow_t* m, int* cmax, int* cmax_k,
+                         int32_t* cmax_off) {
+  const int swg = ua->p->match != 0 ? -ua->p->match : -1;
+  int* sw = (int*)malloc((size_t)(m->hi - m->lo + 1) * sizeof(int));
+  *cmax = INT_MIN;
+  *cmax_k = 0;
+  *cmax_off = 0;
+  for (int k = m->lo; k <= m->hi; ++k) {
+    const int32_t off = m->off[k];
+    if (off < 0) continue;
+    const int v = off - k, h = off;
+    const int sc = (swg * (v + h) - ua->s) / 2;
+    sw[k - m->lo] = sc;
+    if (*cmax < sc) {
+      *cmax = sc;
+      *cmax_k = k;
+      *cmax_off = off;
+    }
+  }
+  return sw;
+}
+
+/* X-drop (wavefront/wavefront_heuristic.c:326-380): cells whose score fell
+ * xdrop or more below the best seen so far are cut from both ends. */
+static void hs_xdrop(oracle_ua_t* ua, orow_t* m) {
+  const pen_t* p = ua->p;
+  if (ua->steps_wait > 0) return;
+  int cmax, cmax_k;
+  int32_t cmax_off;
+  const int base = m->lo;
+  int* sw = hs_sw_scores(ua, m, &cmax, &cmax_k, &cmax_off);
+  if (ua->max_sw_k != INT32_MAX) {
+    int k;
+    for (k = m->lo; k <= m->hi; ++k) {
+      if (m->off[k] < 0) continue;
+      if (wsub(ua->max_sw, sw[k - base]) < p->h_xdrop) break;
+    }
+    m->lo = k;
+    for (k = m->hi; k >= m->lo; --k) {
+      if (m->off[k] < 0) continue;
+      if (wsub(ua->max_sw, sw[k - base]) < p->h_xdrop) break;
+    }
+    m->hi = k;
+    if (cmax > ua->max_sw) {
+      ua->max_sw = cmax;
+      ua->max_sw_k = cmax_k;
+    }
+  } else {
+    ua->max_sw = cmax;
+    ua->max_sw_k = cmax_k;
+  }
+  free(sw);
+  ua->steps_wait = p->h_steps;
+}
+
+/* Z-drop (wavefront/wavefront_heuristic.c:397-450): ends the alignment once
+ * the best score of a wavefront falls more than zdrop below the best seen,
+ * at the position of that best.  Returns 1 when dropped. */
+static int hs_zdrop(oracle_ua_t* ua, orow_t* m) {
+  const pen_t* p = ua->p;
+  if (ua->steps_wait > 0) return 0;
+  int cmax, cmax_k;
+  int32_t cmax_off;
+  free(hs_sw_scores(ua, m, &cmax, &cmax_k, &cmax_off));
+  if (ua->max_sw_k != INT32_MAX) {
+    if (cmax > ua->max_sw) {
+      ua->max_sw = cmax;
+      ua->max_wf_score = ua->s;
+      ua->max_sw_k = cmax_k;
+      ua->max_sw_off = cmax_off;
+    } else if (wsub(ua->max_sw, cmax) > p->h_zdrop) {
+      ua->zdropped = 1;
+      ua->end_k = ua->max_sw_k;
+      ua->end_off = ua->max_sw_off;
+      return 1;
+    }
+  } else {
+    ua->max_sw = cmax;
+    ua->max_wf_score = ua->s;
+    ua->max_sw_k = cmax_k;
+    ua->max_sw_off = cmax_off;
+  }
+  ua->steps_wait = p->h_steps;
+  return 0;
+}
+
+/* Banded, adaptive (wavefront/wavefront_heuristic.c:460-505): a band of
+ * max_k-min_k+1 diagonals placed by sampling four cells' distances. */
+static void hs_banded_adaptive(oracle_ua_t* ua, orow_t* m) {
+  const pen_t* p = ua->p;
+  if (ua->steps_wait > 0) return;
+  const int lo = m->lo, hi = m->hi;
+  const int len = hi - lo + 1;
+  if (len < 4) return;
+  const int max_len = p->h_max_k - p->h_min_k + 1;
+  if (len > max_len) {
+    const int leeway = (len - max_len) / 2;
+    const int quarter = len / 4;
+    const int d0 = hs_distance(ua, lo, m->off[lo], 0);
+    const int d1 = hs_distance(ua, lo + quarter, m->off[lo + quarter], 0);
+    const int d2 = hs_distance(ua, lo + 2 * quarter, m->off[lo + 2 * quarter], 0);
+    const int d3 = hs_distance(ua, hi, m->off[hi], 0);
+    int nlo = lo;
+    if (d0 > d3) nlo += leeway;
+    if (d1 > d2) nlo += leeway;
+    m->lo = imax(nlo, lo);
+    m->hi = imin(nlo + max_len - 1, hi);
+  }
+  ua->steps_wait = p->h_steps;
+}
+
+/* Heuristic cut-off of the extended M[s] (dispatcher,
+ * wavefront/wavefront_heuristic.c:506-563).  Only the limits shrink: the cut
+ * offsets stay inside the initialised window, where later compute steps
+ * (wavefront/wavefront_compute.c:498-527 pads only beyond it) and the
+ * back-trace (wavefront/wavefront_backtrace.c:63-75) still read them.  I/D
+ * rows of the same score take the intersection of limits.  Returns 1 when
+ * z-drop ends the alignment. */
+static int heuristic_cutoff(oracle_ua_t* ua) {
+  oracle_ws_t* ws = ua->ws;
+  const pen_t* p = ua->p;
+  orow_t* m = row_at(ws, ua->s, C_M);
+  if (!m->exists || m->lo > m->hi) return 0;
+  --ua->steps_wait;
+  const int lo = m->lo, hi = m->hi;
+  if (p->heur & HS_WFADAPTIVE) {
+    hs_wfadaptive(ua, m, 0);
+  } else if (p->heur & HS_WFMASH) {
+    hs_wfadaptive(ua, m, 1);
+  }
+  if (p->heur & HS_XDROP) {
+    hs_xdrop(ua, m);
+  } else if (p->heur & HS_ZDROP) {
+    if (hs_zdrop(ua, m)) return 1;
+  }
+  if (p->heur & HS_BANDED_STATIC) {
+    if (m->lo < p->h_min_k) m->lo = p->h_min_k;
+    if (m->hi > p->h_max_k) m->hi = p->h_max_k;
+  } else if (p->heur & HS_BANDED_ADAPTIVE) {
+    hs_banded_adaptive(ua, m);
+  }
+  if (m->lo == lo && m->hi == hi) return 0;
+  if (m->lo > m->hi && !m->null) m->null = m->cut_null = 1;
+  if (p->metric <= 2) return 0;
   const int ncomp = p->metric == 4 ? NCOMP : 3;
   for (int c = 1; c < ncomp; ++c) {
     orow_t* r = row_at(ws, ua->s, c);
     if (!r->exists) continue;
-    if (nlo > r->lo) r->lo = nlo;
-    if (nhi < r->hi) r->hi = nhi;
-    if (r->lo > r->hi) r->null = 1;
+    if (m->lo > r->lo) r->lo = m->lo;
+    if (m->hi < r->hi) r->hi = m->hi;
+    if (r->lo > r->hi && !r->null) r->null = r->cut_null = 1;
   }
+  return 0;
 }
 
 /* Extends M[s] and tests termination on component ce
@@ -828,7 +1030,7 @@ int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
     }
   }
   if (ua->endsfree) {
-    if (ua->heur) wfadaptive_cutoff(ua);
+    if (ua->heur && heuristic_cutoff(ua)) return ST_END_UNREACHABLE;
     if (max_ak) *max_ak = mak;
     return 0;
   }
@@ -836,8 +1038,8 @@ int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
   const int k_end = ua->k_end;
   if (e->exists && e->lo <= k_end && k_end <= e->hi && e->off[k_end] >= ua->tlen)
     return ST_END_REACHED;
-  /* wavefront/wavefront_extend.c:112-119 (wf-adaptive never drops) */
-  if (ua->heur) wfadaptive_cutoff(ua);
+  /* wavefront/wavefront_extend.c:112-119 */
+  if (ua->heur && heuristic_cutoff(ua)) return ST_END_UNREACHABLE;
   if (max_ak) *max_ak = mak;
   return 0;
 }
@@ -852,9 +1054,13 @@ void oracle_ua_compute(oracle_ua_t* ua) {
 /* Full back-trace of a finished stepper into ops (forward order); returns the
  * number of operations or -1. */
 int oracle_ua_backtrace(oracle_ua_t* ua, char* ops) {
-  char* rev = (char*)malloc((size_t)(ua->plen + ua->tlen + 8));
+  /* the reference's CIGAR buffer holds 2*(plen+tlen) operations
+   * (wavefront/wavefront_aligner.c:403-405); a trace through stale sources
+   * can be longer than plen+tlen */
+  const int cap = 2 * (ua->plen + ua->tlen) + 8;
+  char* rev = (char*)malloc((size_t)cap);
   const int n = backtrace(ua->ws, ua->p, ua->plen, ua->tlen, ua->s, ua->end_k, ua->end_off, ua->ce,
-                          rev);
+                          rev, cap, &ua->stale_source);
   if (n >= 0)
     for (int i = 0; i < n; ++i) ops[i] = rev[n - 1 - i];
   free(rev);
@@ -969,10 +1175,26 @@ static int maxtrim(const pen_t* p, const char* ops, int* n, int* score, int* ev,
   return trimmed;
 }
 
-/* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273). */
-void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
-                      int tlen, int32_t* out_score, int32_t* out_status, char* ops,
-                      int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end) {
+/* Wavefronts the reference allocates for a pair in high-memory mode
+ * (wavefront/wavefront_components.c:41-124). */
+static int64_t score_table_size(const pen_t* p, int plen, int tlen) {
+  const int64_t mn = imin(plen, tlen), diff = plen > tlen ? plen - tlen : tlen - plen;
+  if (p->metric <= 1) return imax(plen, tlen) + 1;
+  if (p->metric == 2) return mn * p->x + (int64_t)p->o1 * diff + 1;
+  int64_t indel = p->o1 + diff * p->e1;
+  if (p->metric == 4) {
+    const int64_t indel2 = p->o2 + diff * p->e2;
+    if (indel2 < indel) indel = indel2;
+  }
+  return mn * p->x + indel + 1;
+}
+
+/* One unidirectional alignment (wavefront/wavefront_unialign.c:242-273),
+ * writing up to 2*(plen+tlen)+8 operations into ops. */
+static void align_one_impl(oracle_ws_t* ws, const pen_t* p, const char* P, int plen,
+                           const char* T, int tlen, int32_t* out_score, int32_t* out_status,
+                           char* ops, int32_t* ops_len, int64_t* cells, int64_t* ext,
+                           int32_t* end, int32_t* flags) {
   int32_t end_dummy[2];
   if (!end) end = end_dummy;
   end[0] = end[1] = -1;
@@ -1011,10 +1233,45 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
   }
   if (cells) *cells = ua.cells;
   if (ext) *ext = ua.ext;
+  /* a heuristic can run an alignment past the score bound the reference
+   * sizes its wavefront table by (wavefront/wavefront_components.c:41-124);
+   * it exits there (wavefront/wavefront_compute.c:442-446) unless an earlier,
+   * longer pair of the same aligner grew the table */
+  if (!p->score_only && ua.s >= score_table_size(p, plen, tlen)) *flags |= ORACLE_FLAG_OVER_BOUND;
   if (status == ST_END_UNREACHABLE) {
-    *out_score = classic_score(p, 0, 0, ua.s);
+    /* wavefront/wavefront_unialign.c:147-237.  The end position is z-drop's
+     * best cell, or none (DPMATRIX_DIAGONAL_NULL, WAVEFRONT_OFFSET_NULL) when
+     * the null steps ran out. */
+    const int k = ua.zdropped ? ua.end_k : INT32_MAX;
+    const int32_t off = ua.zdropped ? ua.end_off : WF_NULL;
     *out_status = 1; /* WF_STATUS_ALG_PARTIAL */
-    *ops_len = 0;
+    if (p->score_only || ops == NULL) {
+      end[0] = wsub(off, k);
+      end[1] = off;
+      *out_score = classic_score_wrapped(p, end[0], end[1], ua.s);
+      *ops_len = 0;
+      return;
+    }
+    /* the back-trace starts from the current score at that cell, adding the
+     * gaps to both ends (wavefront/wavefront_backtrace.c:339-356); then the
+     * maximal-score trim (wavefront/wavefront_aligner.c:664-676) */
+    int n = 0, sc = INT32_MIN, ev = -1, eh = -1;
+    if (ua.zdropped) {
+      n = oracle_ua_backtrace(&ua, ops);
+      if (ua.stale_source) *flags |= ORACLE_FLAG_STALE_SOURCE;
+      if (n < 0) {
+        *out_status = ST_UNATTAINABLE;
+        *ops_len = 0;
+        *out_score = 0;
+        return;
+      }
+      sc = ua.s;
+    }
+    if (p->metric > 1 && !(p->metric == 4 && n == 0)) maxtrim(p, ops, &n, &sc, &ev, &eh);
+    *ops_len = n;
+    *out_score = sc;
+    end[0] = ev;
+    end[1] = eh;
     return;
   }
   /* wavefront/wavefront_unialign.c:147-237 */
@@ -1027,6 +1284,7 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
     return;
   }
   int n = oracle_ua_backtrace(&ua, ops);
+  if (ua.stale_source) *flags |= ORACLE_FLAG_STALE_SOURCE;
   if (n < 0) {
     *out_status = ST_UNATTAINABLE;
     *ops_len = 0;
@@ -1057,16 +1315,51 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
   if (ua.endsfree) *out_score = classic_score(p, end[0], end[1], ua.s);
 }
 
+/* The same with the caller's buffer of plen+tlen operations.  flags (if
+ * given) receives ORACLE_FLAG_* bits; a CIGAR longer than the buffer (a trace
+ * through stale sources) is reported with ops_len = -1. */
+void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
+                      int tlen, int32_t* out_score, int32_t* out_status, char* ops,
+                      int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end,
+                      int32_t* flags) {
+  char* full = ops ? (char*)malloc((size_t)(2 * (plen + tlen) + 8)) : NULL;
+  int32_t fl = 0;
+  align_one_impl(ws, p, P, plen, T, tlen, out_score, out_status, full, ops_len, cells, ext, end,
+                 &fl);
+  if (ops) {
+    if (*ops_len > plen + tlen) {
+      *ops_len = -1;
+    } else if (*ops_len > 0) {
+      memcpy(ops, full, (size_t)*ops_len);
+    }
+    free(full);
+  }
+  if (flags) *flags = fl;
+}
+
 int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, const int64_t* p_off,
                        const int32_t* p_len, const int64_t* t_off, const int32_t* t_len,
                        int32_t* out_score, int32_t* out_status, char* out_ops,
                        const int64_t* ops_off, int32_t* out_ops_len, int64_t* out_cells,
                        int64_t* out_ext, int32_t* out_end, int nthreads) {
+  return oracle_align_batch_flags(cfg, num_pairs, sequences, p_off, p_len, t_off, t_len,
+                                  out_score, out_status, out_ops, ops_off, out_ops_len, out_cells,
+                                  out_ext, out_end, NULL, nthreads);
+}
+
+int oracle_align_batch_flags(const int* cfg, int num_pairs, const char* sequences,
+                             const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
+                             const int32_t* t_len, int32_t* out_score, int32_t* out_status,
+                             char* out_ops, const int64_t* ops_off, int32_t* out_ops_len,
+                             int64_t* out_cells, int64_t* out_ext, int32_t* out_end,
+                             int32_t* out_flags, int nthreads) {
   pen_t p;
   if (setup_penalties(cfg, &p) != 0) return -1;
   const int ultralow = (cfg[7] == 3);
   /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82) */
   if (ultralow && p.endsfree) return -1;
+  /* BiWFA is restated with the wf-adaptive heuristic or none */
+  if (ultralow && (p.heur & ~HS_WFADAPTIVE)) return -1;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel num_threads(nthreads)
@@ -1091,7 +1384,8 @@ int oracle_align_batch(const int* cfg, int num_pairs, const char* sequences, con
         }
       } else {
         oracle_align_one(&ws, &p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i],
-                  &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext, end);
+                         &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext, end,
+                         out_flags ? &out_flags[i] : NULL);
       }
     }
     ws_free(&ws);

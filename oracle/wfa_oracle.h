@@ -37,8 +37,11 @@ extern "C" {
  *           text_end_free
  *   cfg[19] extension        (1: ends-free with the extension presets and
  *           maximal-score trimming, wavefront/wavefront_align.c:57-63)
+ *   cfg[20] heuristic strategy bit set (wf_heuristic_strategy,
+ *           wavefront/wavefront_heuristic.h:41-49); non-zero overrides cfg[10]
+ *   cfg[21] xdrop  cfg[22] zdrop  cfg[23] band min_k  cfg[24] band max_k
  */
-#define ORACLE_CFG_LEN 20
+#define ORACLE_CFG_LEN 25
 
 /* Align num_pairs pairs with nthreads host threads (OpenMP, one aligner per
  * thread, as tools/align_benchmark/align_benchmark.c:504-586 does).
@@ -68,6 +71,19 @@ int oracle_align_batch(
     int32_t* out_score, int32_t* out_status,
     char* out_ops, const int64_t* ops_off, int32_t* out_ops_len,
     int64_t* out_cells, int64_t* out_ext, int32_t* out_end, int nthreads);
+
+/* The same, with out_flags[i] (may be NULL) receiving ORACLE_FLAG_* bits.  A
+ * CIGAR longer than p_len[i]+t_len[i] is reported with out_ops_len[i] = -1. */
+#define ORACLE_FLAG_STALE_SOURCE 1 /* back-trace read a wavefront a cut emptied */
+#define ORACLE_FLAG_OVER_BOUND 2   /* ran past the reference's per-pair wavefront table */
+int oracle_align_batch_flags(
+    const int* cfg, int num_pairs,
+    const char* sequences,
+    const int64_t* p_off, const int32_t* p_len,
+    const int64_t* t_off, const int32_t* t_len,
+    int32_t* out_score, int32_t* out_status,
+    char* out_ops, const int64_t* ops_off, int32_t* out_ops_len,
+    int64_t* out_cells, int64_t* out_ext, int32_t* out_end, int32_t* out_flags, int nthreads);
 
 #ifdef __cplusplus
 }

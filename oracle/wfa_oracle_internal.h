@@ -21,14 +21,27 @@
 
 enum { C_M = 0, C_I1 = 1, C_D1 = 2, C_I2 = 3, C_D2 = 4, NCOMP = 5 };
 
+/* wavefront/wavefront_heuristic.h:41-49 */
+enum {
+  HS_BANDED_STATIC = 0x01,
+  HS_BANDED_ADAPTIVE = 0x02,
+  HS_WFADAPTIVE = 0x04,
+  HS_XDROP = 0x10,
+  HS_ZDROP = 0x20,
+  HS_WFMASH = 0x40,
+};
+
 typedef struct {
   int metric; /* 3 affine, 4 affine2p */
   int match, x, o1, e1, o2, e2;
   int scope; /* max_score_scope */
   int score_only;
   int max_steps;
-  /* heuristic: 0 none, 1 wf-adaptive (wavefront/wavefront_heuristic.c:254-289) */
+  /* heuristic strategy: a bit set of the reference's wf_heuristic_strategy
+   * values (wavefront/wavefront_heuristic.h:41-49), 0 for none, and its
+   * parameters (wavefront/wavefront_heuristic.h:51-69) */
   int heur, h_min_len, h_max_dist, h_steps;
+  int h_xdrop, h_zdrop, h_min_k, h_max_k;
   /* the user's penalties, as maximal-score trimming reads them
    * (wavefront/wavefront_aligner.c:664-676) */
   int um, ux, uo1, ue1, uo2, ue2;
@@ -39,6 +52,7 @@ typedef struct {
 typedef struct {
   int exists;   /* wavefront stored for this score/component */
   int null;     /* wavefront->null after trimming */
+  int cut_null; /* null because a heuristic cut emptied it */
   int lo, hi;   /* trimmed limits */
   int ilo, ihi; /* NULL-initialised window (wf_elements_init_min/max) */
   int32_t* off; /* off[k] addressable for every k of the allocated range */
@@ -78,7 +92,16 @@ typedef struct {
   int tlen;
   int cb, ce;
   int s, null_steps, k_end;
-  int heur, steps_wait; /* wf-adaptive cut-off state (wavefront_heuristic_clear) */
+  /* cut-off state, as wavefront_heuristic_clear leaves it at the start of
+   * each alignment (wavefront/wavefront_heuristic.c:114-121) */
+  int heur, steps_wait;
+  int max_sw, max_sw_k, max_wf_score;
+  int32_t max_sw_off;
+  int zdropped; /* z-drop ended the alignment at (end_k, end_off) */
+  /* the back-trace took a source from a wavefront that a cut emptied: the
+   * reference's compute step read that wavefront as NULL, its back-trace
+   * reads the cells (wavefront/wavefront_backtrace.c:63-75) */
+  int stale_source;
   int64_t cells, ext;
   /* ends-free form of this alignment (0: end-to-end) and the free lengths after
    * the per-pair presets; the end position found by termination
@@ -106,7 +129,8 @@ void oracle_ws_free(oracle_ws_t* ws);
 /* One unidirectional end-to-end alignment (high-memory semantics). */
 void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, const char* T,
                       int tlen, int32_t* out_score, int32_t* out_status, char* ops,
-                      int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end);
+                      int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end,
+                      int32_t* flags);
 
 /* BiWFA (ultralow memory mode). */
 void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int tlen,

@@ -18,8 +18,16 @@ sources are available; the fixtures themselves travel with the repo).
    forms (wavefront/wavefront_attributes.h:55-69), from the reference built
    without host tuning (oracle/_ref/libwfa_ref_scalar.so: its portable
    extension kernels, as on aarch64), with cigar->end_v / end_h per pair.
+5. ``heuristics_expected.json`` -- the same for the heuristics other than
+   wf-adaptive (wavefront/wavefront_heuristic.c: banded static and adaptive,
+   wfmash, x-drop, z-drop and combinations).  Pairs the reference cannot
+   finish are left out, found first with the CPU restatement: those that run
+   past its per-pair wavefront table (it exits, wavefront/wavefront_compute.c:
+   442-446) and, for edit/indel, those a cut leaves unable to reach the end
+   (it faults in alignment scope and loops in score-only scope).  Each set
+   lists the pair indices it keeps.
 
-Usage:  python tests/golden/make_golden.py [/path/to/WFA2-lib]
+Usage:  python tests/golden/make_golden.py [/path/to/WFA2-lib] [--only=heuristics]
 """
 import gzip
 import json
@@ -130,12 +138,74 @@ ENDSFREE = {
 }
 
 
+# heuristic strategies (wavefront/wavefront_heuristic.h:41-49) and parameters
+def _h(strategy, **kw):
+    return {"strategy": strategy, **kw}
+
+
+BS, BA, WA, XD, ZD, WM = 0x01, 0x02, 0x04, 0x10, 0x20, 0x40
+# name: (workload, n, penalties, score_only, param, param2, form, heuristic)
+HEURISTIC_SETS = {
+    "w1_affine_bstatic": (1, 60, "affine", False, 0, 0, None, _h(BS, min_k=-30, max_k=30)),
+    "w1_affine_bstatic_score": (1, 60, "affine", True, 0, 0, None, _h(BS, min_k=-30, max_k=30)),
+    "w6_affine_badapt": (6, 60, "affine", False, 0, 0, None,
+                         _h(BA, min_k=-20, max_k=20, steps_between_cutoffs=1)),
+    "w1_affine_badapt3_ext": (1, 60, "affine", False, 0, 0, "extension",
+                              _h(BA, min_k=-20, max_k=20, steps_between_cutoffs=3)),
+    "w1_affine_wfmash": (1, 60, "affine", False, 0, 0, None,
+                         _h(WM, min_wavefront_length=10, max_distance_threshold=50,
+                            steps_between_cutoffs=1)),
+    "w6_affine_p4_xdrop": (6, 60, "affine.p4", False, 0, 0, None,
+                           _h(XD, xdrop=50, steps_between_cutoffs=1)),
+    "w6_affine_p3_xdrop_ext": (6, 60, "affine.p3", False, 0, 0, "extension",
+                               _h(XD, xdrop=100, steps_between_cutoffs=1)),
+    "w6_affine_p4_zdrop_score": (6, 60, "affine.p4", True, 0, 0, None,
+                                 _h(ZD, zdrop=50, steps_between_cutoffs=1)),
+    "w6_affine_p4_zdrop_full": (6, 60, "affine.p4", False, 0, 0, None,
+                                _h(ZD, zdrop=50, steps_between_cutoffs=1)),
+    "w6_affine_p4_zdrop_ext": (6, 60, "affine.p4", False, 0, 0, "extension",
+                               _h(ZD, zdrop=50, steps_between_cutoffs=2)),
+    "w6_affine_p4_wfa_xdrop": (6, 60, "affine.p4", False, 0, 0, None,
+                               _h(WA | XD, min_wavefront_length=10, max_distance_threshold=50,
+                                  xdrop=60, steps_between_cutoffs=1)),
+    "w1_affine_xdrop_bstatic_ef": (1, 60, "affine", False, 0, 0, (20, 20, 20, 20),
+                                   _h(XD | BS, xdrop=40, min_k=-30, max_k=30,
+                                      steps_between_cutoffs=1)),
+    "w6_affine2p_xdrop": (6, 60, "affine2p", False, 0, 0, None,
+                          _h(XD, xdrop=100, steps_between_cutoffs=1)),
+    "w1_affine2p_bstatic_score": (1, 60, "affine2p", True, 0, 0, None,
+                                  _h(BS, min_k=-25, max_k=25)),
+    "w6_affine2p_zdrop": (6, 60, "affine2p", False, 0, 0, None,
+                          _h(ZD, zdrop=100, steps_between_cutoffs=1)),
+    "w1_linear_badapt": (1, 60, "linear", False, 0, 0, None,
+                         _h(BA, min_k=-20, max_k=20, steps_between_cutoffs=1)),
+    "w6_linear_m1_xdrop_ext": (6, 60, "linear.m1", False, 0, 0, "extension",
+                               _h(XD, xdrop=60, steps_between_cutoffs=1)),
+    "w1_edit_bstatic": (1, 60, "edit", False, 0, 0, None, _h(BS, min_k=-60, max_k=60)),
+    "w1_edit_badapt": (1, 60, "edit", False, 0, 0, None,
+                       _h(BA, min_k=-30, max_k=30, steps_between_cutoffs=1)),
+    "w1_indel_wfmash_score": (1, 60, "indel", True, 0, 0, None,
+                              _h(WM, min_wavefront_length=10, max_distance_threshold=50,
+                                 steps_between_cutoffs=1)),
+}
+
+
+def heuristic_of(spec):
+    """The CPU checker's Heuristic for a fixture set's heuristic dict."""
+    from oracle import oracle as O
+    return O.Heuristic(**spec)
+
+
 def crc(s: str) -> int:
     return zlib.crc32(s.encode()) & 0xFFFFFFFF
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    only = [a[len("--only="):] for a in sys.argv[1:] if a.startswith("--only=")]
+    if only == ["heuristics"]:
+        return heuristics_fixtures()
+    ref = args[0] if args else "/root/reference"
     with open(os.path.join(ref, "tests", "wfa.utest.seq"), "rb") as f:
         raw = f.read()
     with open(os.path.join(HERE, "utest.seq.gz"), "wb") as fo:
@@ -197,6 +267,36 @@ def main():
         print(name, "done")
     with open(os.path.join(HERE, "endsfree_expected.json"), "w") as f:
         json.dump(ends, f, separators=(",", ":"))
+
+    heuristics_fixtures()
+
+
+def heuristics_fixtures():
+    from oracle import oracle as O
+    import wfa2gpu as W
+    O.build(ref=True)
+    W.build()
+    heur = {}
+    for name, (wl, n, pset, so, param, param2, form, hspec) in HEURISTIC_SETS.items():
+        m, mi, mm_, o1, e1, o2, e2 = {**PENALTY_SETS, **EXTRA_SETS}[pset]
+        pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
+                          gap_opening2=o2, gap_extension2=e2)
+        h = heuristic_of(hspec)
+        p = W.generate(wl, n, param=param, param2=param2)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        a = O.align(b, pen, score_only=so, kind="port", form=form, heuristic=h)
+        keep = [i for i in range(n) if not (a.flags[i] & O.FLAG_OVER_BOUND)
+                and not (m <= 1 and a.status[i] == 1)]
+        sub = O.PairBatch.from_lists([b.pattern(i) for i in keep], [b.text(i) for i in keep])
+        r = O.align(sub, pen, score_only=so, kind="reference_scalar", form=form, heuristic=h)
+        rows = [[int(r.score[j]), int(r.status[j]), crc(r.cigar(j)), int(r.end[j][0]),
+                 int(r.end[j][1])] for j in range(sub.n)]
+        heur[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
+                      "penalties": pset, "score_only": so, "form": form, "heuristic": hspec,
+                      "keep": keep, "rows": rows}
+        print(name, "done", len(keep), "of", n)
+    with open(os.path.join(HERE, "heuristics_expected.json"), "w") as f:
+        json.dump(heur, f, separators=(",", ":"))
 
 
 if __name__ == "__main__":

@@ -46,6 +46,25 @@ def endsfree_expected():
     return d
 
 
+def heuristics_expected():
+    """Reference outputs under the heuristics other than wf-adaptive; a
+    fixture's "keep" lists the generated pairs it holds rows for."""
+    with open(os.path.join(GOLDEN, "heuristics_expected.json")) as f:
+        d = json.load(f)
+    for fx in d.values():
+        if isinstance(fx["form"], list):
+            fx["form"] = tuple(fx["form"])
+    return d
+
+
+def heuristic_pairs(O, W, fx):
+    """The kept pairs of a heuristic fixture set, as one PairBatch."""
+    p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    return O.PairBatch.from_lists([b.pattern(i) for i in fx["keep"]],
+                                  [b.text(i) for i in fx["keep"]])
+
+
 def pack(patterns, texts):
     """Concatenated ASCII batch: (seqs, p_off, p_len, t_off, t_len)."""
     parts, p_off, t_off, pos = [], [], [], 0

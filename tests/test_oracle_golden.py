@@ -7,7 +7,8 @@ Pins the C restatement (oracle/wfa_oracle.c) to
     (tests/golden/synthetic_expected.json), and in the ends-free and
     extension forms (tests/golden/endsfree_expected.json: score, status,
     CIGAR and end position; the reference built with its portable extension
-    kernels).
+    kernels), and under the heuristics other than wf-adaptive
+    (tests/golden/heuristics_expected.json).
 """
 import numpy as np
 import pytest
@@ -95,6 +96,45 @@ def test_oracle_matches_reference_endsfree(oracle_mod, wfa, name):
                 assert O.check_cigar(r.cigar(i), b.pattern(i)[:ev], b.text(i)[:eh]), (name, i)
             else:
                 assert O.check_cigar(r.cigar(i), b.pattern(i), b.text(i)), (name, i)
+
+
+HX = helpers.heuristics_expected()
+
+
+@pytest.mark.parametrize("name", sorted(HX.keys()))
+def test_oracle_matches_reference_heuristics(oracle_mod, wfa, name):
+    """Banded static/adaptive, wfmash, x-drop, z-drop and combinations
+    (wavefront/wavefront_heuristic.c:229-563): score, status, CIGAR and end
+    position equal the reference's, including the back-traces that read a
+    wavefront a cut emptied."""
+    O, W = oracle_mod, wfa
+    fx = HX[name]
+    pen = _pen(O, UT["penalty_sets"][fx["penalties"]])
+    b = helpers.heuristic_pairs(O, W, fx)
+    r = O.align(b, pen, score_only=fx["score_only"], form=fx["form"],
+                heuristic=O.Heuristic(**fx["heuristic"]))
+    assert len(fx["rows"]) == b.n
+    for i, (score, status, c, ev, eh) in enumerate(fx["rows"]):
+        got = (int(r.score[i]), int(r.status[i]), helpers.crc(r.cigar(i)), int(r.end[i][0]),
+               int(r.end[i][1]))
+        assert got == (score, status, c, ev, eh), (name, i)
+
+
+def test_oracle_heuristic_rejections(oracle_mod, wfa):
+    """Drops with edit/indel (the reference exits, wavefront/wavefront_align.c:
+    83-89) and BiWFA with heuristics other than wf-adaptive fail loudly."""
+    O, W = oracle_mod, wfa
+    p = W.generate(1, 4, first=3)
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    for metric in (O.EDIT, O.INDEL):
+        for st in (O.HS_XDROP, O.HS_ZDROP):
+            with pytest.raises(ValueError):
+                O.align(b, O.Penalties(metric), heuristic=O.Heuristic(st, xdrop=10, zdrop=10))
+    with pytest.raises(ValueError):
+        O.align(b, O.Penalties(), memory_mode=O.MEM_ULTRALOW,
+                heuristic=O.Heuristic(O.HS_BANDED_STATIC, min_k=-5, max_k=5))
+    O.align(b, O.Penalties(), memory_mode=O.MEM_ULTRALOW,
+            heuristic=O.Heuristic(O.HS_WFADAPTIVE, 10, 50, 1))
 
 
 def test_oracle_endsfree_rejections(oracle_mod, wfa):
