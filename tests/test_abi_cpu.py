@@ -140,3 +140,33 @@ int main(void) {
   return st == 0 ? 0 : 1;
 }
 '''
+
+
+def test_heuristic_setters_add_strategies(wfa):
+    """The setters add to the strategy set as the reference's do
+    (wavefront/wavefront_heuristic.c:40-113); "none" clears it; one
+    steps_between_cutoffs serves every strategy."""
+    L = wfa.lib()
+    attr = wfa.default_attributes()  # wf-adaptive (wavefront/wavefront_attributes.c:71-76)
+    h = L.wavefront_aligner_new(C.byref(attr))
+    assert h
+    L.wavefront_aligner_set_heuristic_none.argtypes = [C.c_void_p]
+    for name in ("xdrop", "zdrop"):
+        getattr(L, f"wavefront_aligner_set_heuristic_{name}").argtypes = [C.c_void_p, C.c_int,
+                                                                          C.c_int]
+    L.wavefront_aligner_set_heuristic_banded_static.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.wavefront_aligner_set_heuristic_wfadaptive.argtypes = [C.c_void_p, C.c_int, C.c_int,
+                                                             C.c_int]
+    assert h.contents.heuristic.strategy == wfa.WF_HEURISTIC_WFADAPTIVE
+    L.wavefront_aligner_set_heuristic_none(h)
+    assert h.contents.heuristic.strategy == 0
+    L.wavefront_aligner_set_heuristic_xdrop(h, 40, 3)
+    L.wavefront_aligner_set_heuristic_banded_static(h, -12, 12)
+    hs = h.contents.heuristic
+    assert hs.strategy == wfa.WF_HEURISTIC_XDROP | wfa.WF_HEURISTIC_BANDED_STATIC
+    assert (hs.xdrop, hs.min_k, hs.max_k, hs.steps_between_cutoffs) == (40, -12, 12, 3)
+    L.wavefront_aligner_set_heuristic_wfadaptive(h, 10, 50, 1)
+    assert h.contents.heuristic.strategy == (wfa.WF_HEURISTIC_XDROP | wfa.WF_HEURISTIC_BANDED_STATIC
+                                             | wfa.WF_HEURISTIC_WFADAPTIVE)
+    assert h.contents.heuristic.steps_between_cutoffs == 1
+    wfa.lib().wavefront_aligner_delete(h)

@@ -1,0 +1,156 @@
+"""Heuristic cut-offs other than wf-adaptive on the GPU, through the C ABI.
+
+Strategies (wavefront/wavefront_heuristic.c:229-563): wfmash, x-drop, z-drop,
+banded static and banded adaptive, alone and combined (one of wf-adaptive /
+wfmash, one of x-drop / z-drop, one of the bands, sharing one wait counter).
+
+Integer work: scores, statuses, CIGARs and end positions must equal the
+reference's own outputs (tests/golden/heuristics_expected.json) and the CPU
+checker's on further cases, for every pair except one documented class: a
+back-trace that takes a source from a wavefront a cut emptied, which the
+reference's compute step read as NULL but its back-trace reads cell by cell
+(wavefront/wavefront_backtrace.c:63-100).  Where that source lies ahead of
+the cell, the reference takes back CIGAR operations it already wrote; the GPU
+records each cell's own source instead.  The CPU checker flags those pairs
+(FLAG_STALE_SOURCE); they are counted, not compared.
+
+Configurations the GPU does not compute yet (z-drop with a full alignment;
+gap-affine-2p with x-drop, z-drop or the adaptive band; the static band in
+score-only scope) must be refused: WF2G_ERR_CONFIG for a batch."""
+import pytest
+
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+UT = helpers.utest_expected()
+HX = helpers.heuristics_expected()
+
+
+def _spec(name):
+    m, match, x, o1, e1, o2, e2 = UT["penalty_sets"][name]
+    return dict(metric=m, match=match, mismatch=x, gap_opening1=o1, gap_extension1=e1,
+                gap_opening2=o2, gap_extension2=e2)
+
+
+def _served(metric, score_only, strategy):
+    """The GPU's refusals (make_cfg in wfa2-lib_gb300/csrc/wfa_aligner.c)."""
+    if strategy & 0x20 and not score_only:
+        return False
+    if metric == 4 and strategy & (0x10 | 0x20 | 0x02):
+        return False
+    return not (strategy & 0x01 and score_only)
+
+
+def _gpu(W, cfg, b):
+    al = W.Aligner(cfg)
+    rc, scores, status, ops, ops_len, ops_off, end = al.align_batch_ends(
+        b.seqs, b.p_off, b.p_len, b.t_off, b.t_len)
+    al.close()
+    if not _served(cfg.metric, cfg.score_only, cfg.heuristic["strategy"]):
+        assert rc == -2  # WF2G_ERR_CONFIG: refused, no answer
+        return None
+    assert rc == 0
+    out = []
+    for i in range(b.n):
+        cig = "" if ops is None else ops[ops_off[i]:ops_off[i] + ops_len[i]].tobytes().decode()
+        out.append((int(status[i]), int(scores[i]), cig, int(end[i][0]), int(end[i][1])))
+    return out
+
+
+def _oracle_flags(O, pen_spec, b, score_only, form, hspec):
+    pen = O.Penalties(**{"metric": pen_spec["metric"], "match": pen_spec["match"],
+                         "mismatch": pen_spec["mismatch"],
+                         "gap_opening1": pen_spec["gap_opening1"],
+                         "gap_extension1": pen_spec["gap_extension1"],
+                         "gap_opening2": pen_spec["gap_opening2"],
+                         "gap_extension2": pen_spec["gap_extension2"]})
+    return O.align(b, pen, score_only=score_only, form=form, heuristic=O.Heuristic(**hspec))
+
+
+@pytest.mark.parametrize("name", sorted(HX.keys()))
+def test_heuristics_match_reference_fixtures(gpu_available, wfa, oracle_mod, name):
+    W, O = wfa, oracle_mod
+    fx = HX[name]
+    spec = _spec(fx["penalties"])
+    b = helpers.heuristic_pairs(O, W, fx)
+    ref = _oracle_flags(O, spec, b, fx["score_only"], fx["form"], fx["heuristic"])
+    got = _gpu(W, W.Config(**spec, score_only=fx["score_only"], form=fx["form"],
+                           heuristic=fx["heuristic"]), b)
+    if got is None:
+        return
+    compared = 0
+    for i, (score, status, c, ev, eh) in enumerate(fx["rows"]):
+        if ref.flags[i] & O.FLAG_STALE_SOURCE:
+            continue
+        st, sc, cig, gv, gh = got[i]
+        assert (st, sc, helpers.crc(cig), gv, gh) == (status, score, c, ev, eh), (name, i)
+        compared += 1
+    assert compared >= len(fx["rows"]) // 2, (name, compared)
+
+
+CASES = [
+    # (workload, n, param, param2)
+    (1, 120, 0, 0),          # 0.5-1.5 kbp, warp per pair
+    (6, 120, 0, 0),          # random tails: the drops fire
+    (5, 16, 6000, 300),      # 6 kbp: the CTA-per-pair passes
+]
+H = {
+    "bstatic": dict(strategy=0x01, min_k=-40, max_k=40),
+    "badapt": dict(strategy=0x02, min_k=-25, max_k=25, steps_between_cutoffs=2),
+    "wfmash": dict(strategy=0x40, min_wavefront_length=10, max_distance_threshold=50,
+                   steps_between_cutoffs=1),
+    "xdrop": dict(strategy=0x10, xdrop=80, steps_between_cutoffs=1),
+    "zdrop": dict(strategy=0x20, zdrop=80, steps_between_cutoffs=1),
+    "wfa_xdrop_band": dict(strategy=0x04 | 0x10 | 0x01, min_wavefront_length=10,
+                           max_distance_threshold=50, xdrop=100, min_k=-60, max_k=60,
+                           steps_between_cutoffs=1),
+}
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("hname", sorted(H.keys()))
+@pytest.mark.parametrize("spec_name,score_only", [("affine.p4", False), ("affine2p", False),
+                                                  ("affine.p4", True)])
+def test_heuristics_match_oracle(gpu_available, wfa, oracle_mod, case, hname, spec_name,
+                                 score_only):
+    W, O = wfa, oracle_mod
+    wl, n, param, param2 = case
+    spec = _spec(spec_name)
+    p = W.generate(wl, n, param=param, param2=param2)
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    ref = _oracle_flags(O, spec, b, score_only, None, H[hname])
+    got = _gpu(W, W.Config(**spec, score_only=score_only, heuristic=H[hname]), b)
+    if got is None:
+        return
+    compared = 0
+    for i in range(b.n):
+        if ref.flags[i] & (O.FLAG_STALE_SOURCE | O.FLAG_OVER_BOUND):
+            continue
+        want = (int(ref.status[i]), int(ref.score[i]), ref.cigar(i), int(ref.end[i][0]),
+                int(ref.end[i][1]))
+        assert got[i] == want, (hname, spec_name, case, i)
+        compared += 1
+    assert compared >= b.n // 2, (hname, compared)
+
+
+def test_heuristic_rejections(gpu_available, wfa):
+    """Drops with edit/indel (the reference exits, wavefront/wavefront_align.c:
+    83-89), BiWFA with a heuristic other than wf-adaptive, and serving with
+    one are refused loudly."""
+    W = wfa
+    p = W.generate(1, 4, first=3)
+    for cfg in [W.Config(metric=W.EDIT, heuristic=dict(strategy=0x10, xdrop=20)),
+                W.Config(metric=W.INDEL, heuristic=dict(strategy=0x20, zdrop=20)),
+                W.Config(heuristic=dict(strategy=0x20, zdrop=20)),
+                W.Config(metric=W.GAP_AFFINE_2P, heuristic=dict(strategy=0x10, xdrop=20)),
+                W.Config(score_only=True, heuristic=dict(strategy=0x01, min_k=-9, max_k=9)),
+                W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x01, min_k=-9,
+                                                                    max_k=9))]:
+        al = W.Aligner(cfg)
+        st, _, _ = al.align(bytes(p.seqs[p.p_off[0]:p.p_off[0] + p.p_len[0]]),
+                            bytes(p.seqs[p.t_off[0]:p.t_off[0] + p.t_len[0]]))
+        al.close()
+        assert st == W.WF_STATUS_UNATTAINABLE
+    with pytest.raises(RuntimeError):
+        W.Server(W.Config(heuristic=dict(strategy=0x10, xdrop=20)))

@@ -72,6 +72,10 @@ __device__ __forceinline__ bool wf2g_ok(bool ok, int site, long long idx, int pa
   }
 #endif
 
+// a - b in wrapping int32 arithmetic: the reference computes score
+// differences in int, where an INT_MIN best overflows
+__device__ __forceinline__ int wsub32(int a, int b) { return (int)((uint32_t)a - (uint32_t)b); }
+
 __device__ __forceinline__ int ring_back(int cur, int d, int R) {
   // slot of score (s-d) when the slot of s is cur, 0 <= d < R
   const int t = cur - d;
@@ -615,7 +619,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     int s = 0;
     int curM = 0, cur1 = 0, cur2 = 0;  // ring slots of score s
     int null_steps = 0;
-    int steps_wait = p.h_steps;  // wf-adaptive (wavefront/wavefront_heuristic.c:114-121)
+    // cut-off state as wavefront_heuristic_clear leaves it
+    // (wavefront/wavefront_heuristic.c:114-121): wait counter, best SW score,
+    // its diagonal (INT32_MAX: none yet), offset and WFA score
+    int steps_wait = p.h_steps;
+    int max_sw = 0, max_sw_k = INT32_MAX, max_wf = -1;
+    int32_t max_sw_off = kNull;
     int64_t cursor = 0;  // choice bytes used (slice)
     int nblk = 0, cur_blk = -1;  // pool: blocks held, block being filled
     int64_t blk_off = 0, pool_used = 0;
@@ -650,39 +659,149 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         break;
       }
 
-      // ================= wf-adaptive cut-off of the extended M[s]
-      // (wavefront/wavefront_heuristic.c:229-289, :506-566): only the limits
-      // of M[s] (and, intersected, of its I/D rows) shrink; the cut offsets
-      // stay in the rows' initialised windows
+      // ================= heuristic cut-off of the extended M[s]
+      // (wavefront/wavefront_heuristic.c:506-563): one of wf-adaptive/wfmash,
+      // one of x-drop/z-drop, one of banded static/adaptive, sharing one
+      // wait counter.  Only the limits of M[s] (and, intersected, of its I/D
+      // rows) shrink; the cut offsets stay in the rows' initialised windows.
       if (HEUR && m_exists && mlo <= mhi) {
         --steps_wait;
-        if (steps_wait <= 0 && mhi - mlo + 1 >= p.h_min_len) {
-          const OffT* const mr = row(curM);
+        const OffT* const mr = row(curM);
+        const int hs = p.heur;
+        int nlo = mlo, nhi = mhi;
+        // wf-adaptive / wfmash (:229-289): cells further from the end than the
+        // closest by more than max_distance_threshold, from both ends, keeping
+        // the end diagonal's side
+        if ((hs & (kHsWfadaptive | kHsWfmash)) && steps_wait <= 0 && nhi - nlo + 1 >= p.h_min_len) {
+          const bool wm = !(hs & kHsWfadaptive);
+          // wfmash weighs each side by its length (:134-145), in float as the
+          // reference does
+          const int mfactor = wm ? __float2int_rz(__fdiv_rn((float)(plen + tlen), 2.0f)) : 0;
           auto dist = [&](int k) -> int {
             const int32_t off = RING_LD(mr, k);
-            return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
+            if (off < 0) return 1 << 30;
+            if (!wm) return max(plen - (off - k), tlen - off);
+            const int lv = __float2int_rz(
+                __fmul_rn(__fdiv_rn((float)(plen - (off - k)), (float)plen), (float)mfactor));
+            const int lh = __float2int_rz(
+                __fmul_rn(__fdiv_rn((float)(tlen - off), (float)tlen), (float)mfactor));
+            return max(lv, lh);
           };
           int dmin = max(plen, tlen);
-          for (int k = mlo + t; k <= mhi; k += G) dmin = min(dmin, dist(k));
+          for (int k = nlo + t; k <= nhi; k += G) dmin = min(dmin, dist(k));
           dmin = gmin(dmin);
-          const int top = min(k_end, mhi);
+          const int top = min(k_end, nhi);
           int first = INT32_MAX;
-          for (int k = mlo + t; k < top; k += G)
+          for (int k = nlo + t; k < top; k += G)
             if (dist(k) - dmin <= p.h_max_dist) { first = k; break; }
           first = gmin(first);
-          const int nlo = first == INT32_MAX ? max(mlo, top) : first;
-          const int bot = max(k_end, nlo);
+          const int wlo = first == INT32_MAX ? max(nlo, top) : first;
+          const int bot = max(k_end, wlo);
           int last = INT32_MIN;
-          for (int k = mhi - t; k > bot; k -= G)
+          for (int k = nhi - t; k > bot; k -= G)
             if (dist(k) - dmin <= p.h_max_dist) { last = k; break; }
           last = gmax(last);
-          const int nhi = last == INT32_MIN ? min(mhi, bot) : last;
+          nhi = last == INT32_MIN ? min(nhi, bot) : last;
+          nlo = wlo;
           steps_wait = p.h_steps;
-          if (nlo != mlo || nhi != mhi) {
-            mlo = nlo;
-            mhi = nhi;
-            if (t == 0) {
-              meta[curM] = make_int2(nlo, nhi);
+        }
+        // x-drop (:326-380) / z-drop (:397-450) on the cells' SW scores
+        // (wavefront/wavefront_penalties.h:73), with the first best cell
+        if ((hs & (kHsXdrop | kHsZdrop)) && steps_wait <= 0) {
+          const int swg = pen.match != 0 ? -pen.match : -1;
+          auto sw = [&](int k, int32_t off) -> int { return (swg * (2 * off - k) - s) / 2; };
+          int tbest = INT32_MIN, tk = INT32_MAX;
+          int32_t toff = 0;
+          for (int k = nlo + t; k <= nhi; k += G) {
+            const int32_t off = RING_LD(mr, k);
+            if (off < 0) continue;
+            const int sc = sw(k, off);
+            if (sc > tbest) { tbest = sc; tk = k; toff = off; }
+          }
+          const int cmax = gmax(tbest);
+          int cmax_k = gmin(tbest == cmax ? tk : INT32_MAX);
+          int32_t cmax_off = gmax(tk == cmax_k && tbest == cmax ? toff : INT32_MIN);
+          if (cmax == INT32_MIN) { cmax_k = 0; cmax_off = 0; }
+          bool dropped = false;
+          if (hs & kHsXdrop) {
+            if (max_sw_k != INT32_MAX) {
+              // cells xdrop or more below the best seen are cut from both ends
+              auto keep = [&](int k) -> bool {
+                const int32_t off = RING_LD(mr, k);
+                return off >= 0 && wsub32(max_sw, sw(k, off)) < p.h_xdrop;
+              };
+              int first = INT32_MAX;
+              for (int k = nlo + t; k <= nhi; k += G)
+                if (keep(k)) { first = k; break; }
+              first = gmin(first);
+              const int xlo = first == INT32_MAX ? nhi + 1 : first;
+              int last = INT32_MIN;
+              for (int k = nhi - t; k >= xlo; k -= G)
+                if (keep(k)) { last = k; break; }
+              last = gmax(last);
+              if (xlo <= nhi) nhi = last;
+              nlo = xlo;
+              if (cmax > max_sw) { max_sw = cmax; max_sw_k = cmax_k; }
+            } else {
+              max_sw = cmax;
+              max_sw_k = cmax_k;
+            }
+          } else if (max_sw_k != INT32_MAX) {
+            if (cmax > max_sw) {
+              max_sw = cmax; max_wf = s; max_sw_k = cmax_k; max_sw_off = cmax_off;
+            } else if (wsub32(max_sw, cmax) > p.h_zdrop) {
+              dropped = true;
+            }
+          } else {
+            max_sw = cmax; max_wf = s; max_sw_k = cmax_k; max_sw_off = cmax_off;
+          }
+          if (dropped) {  // z-drop ends the alignment at the best cell seen
+            result = 5;
+            break;
+          }
+          steps_wait = p.h_steps;
+        }
+        // banded (:451-505)
+        if (hs & kHsBandedStatic) {
+          nlo = max(nlo, p.h_min_k);
+          nhi = min(nhi, p.h_max_k);
+        } else if ((hs & kHsBandedAdaptive) && steps_wait <= 0 && nhi - nlo + 1 >= 4) {
+          const int len = nhi - nlo + 1, maxlen = p.h_max_k - p.h_min_k + 1;
+          if (len > maxlen) {
+            // place the band by the distances of four sampled cells
+            auto dist = [&](int k) -> int {
+              const int32_t off = RING_LD(mr, k);
+              return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
+            };
+            const int leeway = (len - maxlen) / 2, quarter = len / 4;
+            int blo = nlo;
+            if (dist(nlo) > dist(nhi)) blo += leeway;
+            if (dist(nlo + quarter) > dist(nlo + 2 * quarter)) blo += leeway;
+            nhi = min(blo + maxlen - 1, nhi);
+            nlo = max(blo, nlo);
+          }
+          steps_wait = p.h_steps;
+        }
+        if (nlo != mlo || nhi != mhi) {
+          if (EF && s == 0) {
+            // the ends-free score-0 wavefront keeps the initialised window
+            // [0,0] inside its limits; the first compute step NULL-pads from
+            // beyond min/max(window, limits) (wavefront/wavefront_compute.c:
+            // 498-527), so the cells cut here are NULLed, and a null row keeps
+            // [0,0]
+            const int2 ow = imeta[curM];
+            const int wx = nlo <= nhi ? min(0, nlo) : 0, wy = nlo <= nhi ? max(0, nhi) : 0;
+            OffT* const mw = row(curM);
+            for (int k = ow.x + t; k < wx; k += G) RING_ST(mw, k, null_of<OffT>());
+            for (int k = wy + 1 + t; k <= ow.y; k += G) RING_ST(mw, k, null_of<OffT>());
+            group_sync<G>();
+            if (t == 0) imeta[curM] = make_int2(wx, wy);
+          }
+          mlo = nlo;
+          mhi = nhi;
+          if (t == 0) {
+            meta[curM] = make_int2(nlo, nhi);
+            if (!lin) {  // one component: nothing to intersect (:540-541)
               const int nr = A2P ? 4 : 2;
               for (int j = 0; j < nr; ++j) {
                 const int r = j == 0 ? rowI1 + cur1 : j == 1 ? rowD1 + cur1 : j == 2 ? rowI2 + cur2 : rowD2 + cur2;
@@ -690,8 +809,8 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
                 meta[r] = make_int2(max(m.x, nlo), min(m.y, nhi));
               }
             }
-            group_sync<G>();
           }
+          group_sync<G>();
         }
       }
 
@@ -845,8 +964,8 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       // The reference's back-trace reads an input within its initialised
       // window even when the row is null (wavefront/wavefront_backtrace.c:
       // 63-219), while the compute step reads the all-NULL row: the two
-      // differ only for an I/D row that a cut-off left with empty limits and
-      // a non-empty window.  Choice bytes then follow the back-trace.
+      // differ only for a row that a cut-off left with empty limits and a
+      // non-empty window.  Choice bytes then follow the back-trace.
       auto window_row = [&](bool valid, int r, int score_back) -> const OffT* {
         if (valid || score_back < 0) return nullptr;
         const int2 w = imeta[r];
@@ -864,7 +983,15 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           wD2 = window_row(vD2, rowD2 + sI2, s - pen.e2);
         }
       }
-      const bool ghost = wI1 || wD1 || wI2 || wD2;
+      const OffT* wMx = nullptr;
+      const OffT* wMo1 = nullptr;
+      const OffT* wMo2 = nullptr;
+      if (CIGAR && HEUR) {
+        if (has_x) wMx = window_row(vMx, sMx, s - pen.x);
+        wMo1 = window_row(vMo1, sMo1, s - pen.o1 - pen.e1);
+        if (A2P) wMo2 = window_row(vMo2, sMo2, s - pen.o2 - pen.e2);
+      }
+      const bool ghost = wI1 || wD1 || wI2 || wD2 || wMx || wMo1 || wMo2;
       uint8_t* const brow = CIGAR ? bt + bpos - lo : nullptr;
       // edit and indel NULL the two elements beyond each end of M[s-1]
       // (wavefront/wavefront_compute_edit.c:352-356): cells a cut-off left in
@@ -971,27 +1098,35 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           }
           if (HEUR && ghost) {
             // back-trace candidates with the cut rows' window values
+            const int32_t gmis = wMx ? RING_LD(wMx, k) + 1 : mis;
+            const int32_t gmo1m = wMo1 ? RING_LD(wMo1, k - 1) : mo1_m;
+            const int32_t gmo1p = wMo1 ? RING_LD(wMo1, k + 1) : mo1_p;
             const int32_t wi1e = wI1 ? RING_LD(wI1, k - 1) : i1_e;
             const int32_t wd1e = wD1 ? RING_LD(wD1, k + 1) : d1_e;
-            const int32_t wi1 = max(mo1_m, wi1e) + 1, wd1 = max(mo1_p, wd1e);
+            const int32_t wi1 = max(gmo1m, wi1e) + 1, wd1 = max(gmo1p, wd1e);
             int32_t wi2 = kNull, wd2 = kNull, wi2e = i2_e, wd2e = d2_e;
+            int32_t gmo2m = mo2_m, gmo2p = mo2_p;
             if (A2P) {
+              gmo2m = wMo2 ? RING_LD(wMo2, k - 1) : mo2_m;
+              gmo2p = wMo2 ? RING_LD(wMo2, k + 1) : mo2_p;
               wi2e = wI2 ? RING_LD(wI2, k - 1) : i2_e;
               wd2e = wD2 ? RING_LD(wD2, k + 1) : d2_e;
-              wi2 = max(mo2_m, wi2e) + 1;
-              wd2 = max(mo2_p, wd2e);
+              wi2 = max(gmo2m, wi2e) + 1;
+              wd2 = max(gmo2p, wd2e);
             }
-            const int32_t wbest = max(max(wd1, wd2), max(mis, max(wi1, wi2)));
-            if (mis == wbest) c = kSrcX;
+            const int32_t wbest = max(max(wd1, wd2), max(gmis, max(wi1, wi2)));
+            if (gmis == wbest) c = kSrcX;
             else if (A2P && wd2 == wbest) c = kSrcD2;
             else if (wd1 == wbest) c = kSrcD1;
             else if (A2P && wi2 == wbest) c = kSrcI2;
             else c = kSrcI1;
-            c |= (uint8_t)(wi1e >= mo1_m) << 3;
-            c |= (uint8_t)(wd1e >= mo1_p) << 4;
+            if (!lin) {
+              c |= (uint8_t)(wi1e >= gmo1m) << 3;
+              c |= (uint8_t)(wd1e >= gmo1p) << 4;
+            }
             if (A2P) {
-              c |= (uint8_t)(wi2e >= mo2_m) << 5;
-              c |= (uint8_t)(wd2e >= mo2_p) << 6;
+              c |= (uint8_t)(wi2e >= gmo2m) << 5;
+              c |= (uint8_t)(wd2e >= gmo2p) << 6;
             }
           }
           if (CHK(pooled || cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
@@ -1100,24 +1235,44 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       }
     };
 
+    // classic score (wavefront/wavefront_compute.c:108-120), in the
+    // reference's wrapping int arithmetic
+    auto classic = [&](int ev, int eh) -> int {
+      if (edit_like) return s;  // the distance itself
+      if (pen.match == 0) return -s;
+      return (int)((uint32_t)(-pen.match) * ((uint32_t)ev + (uint32_t)eh) - (uint32_t)s) / 2;
+    };
     // ================= finish the pair (warp-uniform from here on)
-    if (result != 1) {
+    if (result != 1 && result != 5) {
       release_blocks();
       if (t == 0) {
         if (result == -1 && !p.final_pass) {
           p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
         } else {
-          int st, sc;
+          int st, sc, ev = -1, eh = -1;
           if (result == -1) { st = kStOOM; sc = 0; }
           else if (result == 2) { st = kStMaxSteps; sc = -p.max_steps; }
-          else if (result == 3) { st = kStPartial; sc = -s; }
+          else if (result == 3) {
+            // the end unreachable (wavefront/wavefront_unialign.c:147-237) with
+            // no end position (DPMATRIX_DIAGONAL_NULL, WAVEFRONT_OFFSET_NULL):
+            // score-only reports the classic score there; a full run has no
+            // CIGAR to trim, which leaves the cleared one
+            st = kStPartial;
+            if (CIGAR) {
+              sc = INT32_MIN;
+            } else {
+              eh = kNull;
+              ev = wsub32(kNull, INT32_MAX);
+              sc = classic(ev, eh);
+            }
+          }
           else { st = kStUnattainable; sc = 0; }
           p.status[pair] = st;
           p.scores[pair] = sc;
           if (CIGAR) p.ops_len[pair] = 0;
           if (p.end_info) {
-            p.end_info[3 * (int64_t)pair] = -1;
-            p.end_info[3 * (int64_t)pair + 1] = -1;
+            p.end_info[3 * (int64_t)pair] = ev;
+            p.end_info[3 * (int64_t)pair + 1] = eh;
             p.end_info[3 * (int64_t)pair + 2] = s;
           }
         }
@@ -1126,28 +1281,29 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       continue;
     }
     // the end position: (plen, tlen) end-to-end, the terminating diagonal's
-    // cell ends-free (wf_aligner->alignment_end_pos)
+    // cell ends-free, the best cell seen when z-dropped
+    // (wf_aligner->alignment_end_pos)
+    const bool zdrop = HEUR && result == 5;
     int end_k = k_end, end_v = plen, end_h = tlen;
-    if (EF) {
+    if (zdrop) {
+      end_k = max_sw_k;
+      end_h = max_sw_off;
+      end_v = end_h - end_k;
+    } else if (EF) {
       end_k = ef_k;
       end_h = RING_LD(row(curM), ef_k);
       end_v = end_h - ef_k;
     }
-    // classic score (wavefront/wavefront_compute.c:108-120); a score-only
-    // run reports it for the whole sequences (wavefront/wavefront_unialign.c:
-    // 160-165), a full run for the end position
-    auto classic = [&](int ev, int eh) -> int {
-      if (edit_like) return s;  // the distance itself
-      return (pen.match == 0) ? -s : ((-pen.match) * (ev + eh) - s) / 2;
-    };
-    const int score = CIGAR ? classic(end_v, end_h) : classic(plen, tlen);
+    // a score-only run reports the classic score for the whole sequences
+    // (wavefront/wavefront_unialign.c:160-165), a full run for the end position
+    const int score = (CIGAR || zdrop) ? classic(end_v, end_h) : classic(plen, tlen);
     if (!CIGAR) {
       if (t == 0) {
         p.scores[pair] = score;
-        p.status[pair] = kStCompleted;
+        p.status[pair] = zdrop ? kStPartial : kStCompleted;
         if (p.end_info) {
-          p.end_info[3 * (int64_t)pair] = plen;
-          p.end_info[3 * (int64_t)pair + 1] = tlen;
+          p.end_info[3 * (int64_t)pair] = zdrop ? end_v : plen;
+          p.end_info[3 * (int64_t)pair + 1] = zdrop ? end_h : tlen;
           p.end_info[3 * (int64_t)pair + 2] = s;
         }
       }
@@ -1250,10 +1406,22 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         v = max(0, -k_begin);
         h = max(0, k_begin);
       }
+      int pops = 0;  // z-drop: trailing gaps the first match count takes back
       for (int64_t i = n - 1; i >= 0; --i) {
         const uint8_t it = items[i];
         if (it == 'E') {
-          const int L = lcp<ENC>(P, T, v, h, min(plen - v, tlen - h), nwords, g_pair);
+          int L;
+          if (zdrop && i == 0) {
+            // the walk began at the best cell's diagonal from the current
+            // score: the reference counts the matches up to the best cell's
+            // offset without reading the sequences, and a negative count
+            // takes back that many of the gaps it wrote to the ends first
+            // (wavefront/wavefront_backtrace.c:76-100, :339-356)
+            L = max(0, end_h - h);
+            pops = max(0, h - end_h);
+          } else {
+            L = lcp<ENC>(P, T, v, h, min(plen - v, tlen - h), nwords, g_pair);
+          }
           for (int j = lane; j < L; j += 32)
             if (CHK(out_n + j < plen + tlen, 37, out_n + j)) out[out_n + j] = 'M';
           out_n += L;
@@ -1268,8 +1436,36 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           ++out_n;
         }
       }
-      if (v != end_v || h != end_h) bad = true;
-      if (EF && !bad) {
+      if (zdrop) {
+        // the end gaps (tlen-end_h insertions, plen-end_v deletions) only
+        // lower the score, so the maximal-score trim of the whole CIGAR ends
+        // inside the walked part; a count past them leaves no CIGAR
+        if (pops > (tlen - end_h) + (plen - end_v)) bad = true;
+        if (!bad) {
+          __syncwarp();
+          if (lane == 0) {
+            int len = out_n, sc = 0, ev = 0, eh = 0;
+            fin_status = kStPartial;
+            if (A2P && out_n == 0) {
+              // an empty affine2p CIGAR is not trimmed (alignment/cigar_utils.c:
+              // 281); gaps alone trim to nothing
+              const bool gaps = (tlen - end_h) + (plen - end_v) > pops;
+              fin_score = gaps ? INT32_MIN : s;
+              fin_v = fin_h = -1;
+            } else {
+              if (lin) maxtrim_linear(p, out, &len, &sc, &ev, &eh);
+              else maxtrim<A2P>(p, out, &len, &sc, &ev, &eh);
+              fin_score = sc;
+              fin_v = ev;
+              fin_h = eh;
+              out_n = len;
+            }
+          }
+        }
+      } else if (v != end_v || h != end_h) {
+        bad = true;
+      }
+      if (EF && !bad && !zdrop) {
         // the free end: insertions, then deletions, up to the sequences' ends
         // (wavefront/wavefront_backtrace.c:346-356)
         const int ni = tlen - end_h, nd = plen - end_v;
@@ -1302,7 +1498,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     }
     if (t == 0) {
       p.status[pair] = bad ? kStUnattainable : fin_status;
-      p.scores[pair] = bad ? score : fin_score;
+      p.scores[pair] = bad ? (zdrop ? 0 : score) : fin_score;
       p.ops_len[pair] = bad ? 0 : out_n;
       if (p.end_info) {
         p.end_info[3 * (int64_t)pair] = bad ? -1 : fin_v;

@@ -235,18 +235,17 @@ void wavefront_aligner_set_alignment_extension(wavefront_aligner_t* const wf) {
   wf->alignment_form.span = alignment_endsfree;
   wf->alignment_form.extension = true;
 }
-static void heuristic_reset(wavefront_heuristic_t* h, wf_heuristic_strategy s) {
-  memset(h, 0, sizeof(*h));
-  h->strategy = s;
-}
+/* The setters add a strategy to the set, as the reference's do
+ * (wavefront/wavefront_heuristic.c:40-113); only "none" clears it.  One
+ * steps_between_cutoffs serves every strategy of the set. */
 void wavefront_aligner_set_heuristic_none(wavefront_aligner_t* const wf) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_none);
+  wf->heuristic.strategy = wf_heuristic_none;
 }
 void wavefront_aligner_set_heuristic_wfadaptive(wavefront_aligner_t* const wf,
                                                 const int min_wavefront_length,
                                                 const int max_distance_threshold,
                                                 const int score_steps) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_wfadaptive);
+  wf->heuristic.strategy |= wf_heuristic_wfadaptive;
   wf->heuristic.min_wavefront_length = min_wavefront_length;
   wf->heuristic.max_distance_threshold = max_distance_threshold;
   wf->heuristic.steps_between_cutoffs = score_steps;
@@ -255,33 +254,33 @@ void wavefront_aligner_set_heuristic_wfmash(wavefront_aligner_t* const wf,
                                             const int min_wavefront_length,
                                             const int max_distance_threshold,
                                             const int score_steps) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_wfmash);
+  wf->heuristic.strategy |= wf_heuristic_wfmash;
   wf->heuristic.min_wavefront_length = min_wavefront_length;
   wf->heuristic.max_distance_threshold = max_distance_threshold;
   wf->heuristic.steps_between_cutoffs = score_steps;
 }
 void wavefront_aligner_set_heuristic_xdrop(wavefront_aligner_t* const wf, const int xdrop,
                                            const int score_steps) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_xdrop);
+  wf->heuristic.strategy |= wf_heuristic_xdrop;
   wf->heuristic.xdrop = xdrop;
   wf->heuristic.steps_between_cutoffs = score_steps;
 }
 void wavefront_aligner_set_heuristic_zdrop(wavefront_aligner_t* const wf, const int ydrop,
                                            const int score_steps) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_zdrop);
+  wf->heuristic.strategy |= wf_heuristic_zdrop;
   wf->heuristic.zdrop = ydrop;
   wf->heuristic.steps_between_cutoffs = score_steps;
 }
 void wavefront_aligner_set_heuristic_banded_static(wavefront_aligner_t* const wf,
                                                    const int band_min_k, const int band_max_k) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_banded_static);
+  wf->heuristic.strategy |= wf_heuristic_banded_static;
   wf->heuristic.min_k = band_min_k;
   wf->heuristic.max_k = band_max_k;
 }
 void wavefront_aligner_set_heuristic_banded_adaptive(wavefront_aligner_t* const wf,
                                                      const int band_min_k, const int band_max_k,
                                                      const int score_steps) {
-  heuristic_reset(&wf->heuristic, wf_heuristic_banded_adaptive);
+  wf->heuristic.strategy |= wf_heuristic_banded_adaptive;
   wf->heuristic.min_k = band_min_k;
   wf->heuristic.max_k = band_max_k;
   wf->heuristic.steps_between_cutoffs = score_steps;
@@ -314,10 +313,23 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   const alignment_form_t* form = &wf->alignment_form;
   /* extension is an ends-free form (wavefront/wavefront_aligner.c:526-530) */
   if (form->span == alignment_end2end && form->extension) return -1;
-  /* exact, or the wf-adaptive cut-off (wavefront/wavefront_heuristic.c:229-289);
-   * wfmash, drops and bands are not computed on the GPU */
-  const int wfadaptive = (wf->heuristic.strategy == wf_heuristic_wfadaptive);
-  if (wf->heuristic.strategy != wf_heuristic_none && !wfadaptive) return -1;
+  /* the heuristic cut-offs (wavefront/wavefront_heuristic.c:506-563): one of
+   * wf-adaptive/wfmash, one of x-drop/z-drop, one of banded static/adaptive */
+  const int strategy = (int)wf->heuristic.strategy;
+  /* drops with edit/indel: the reference exits (wavefront/wavefront_align.c:83-89) */
+  if ((strategy & (wf_heuristic_xdrop | wf_heuristic_zdrop)) && p->distance_metric <= edit)
+    return -1;
+  /* BiWFA is computed with the wf-adaptive cut-off or none */
+  if (wf->memory_mode == wavefront_memory_ultralow && (strategy & ~wf_heuristic_wfadaptive))
+    return -1;
+  /* not computed on the GPU yet: z-drop with a full alignment; gap-affine-2p
+   * with x-drop, z-drop or the adaptive band; the static band in score-only
+   * scope */
+  if ((strategy & wf_heuristic_zdrop) && wf->alignment_scope == compute_alignment) return -1;
+  if (p->distance_metric == gap_affine_2p &&
+      (strategy & (wf_heuristic_xdrop | wf_heuristic_zdrop | wf_heuristic_banded_adaptive)))
+    return -1;
+  if ((strategy & wf_heuristic_banded_static) && wf->alignment_scope == compute_score) return -1;
   cfg->metric = (int)p->distance_metric;
   cfg->match = p->match;
   cfg->x = p->mismatch;
@@ -329,10 +341,14 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   cfg->max_steps = wf->system.max_alignment_steps > 0 ? wf->system.max_alignment_steps : INT_MAX;
   /* ultralow memory mode is BiWFA (wavefront/wavefront_align.c:138-146) */
   cfg->ultralow = (wf->memory_mode == wavefront_memory_ultralow);
-  cfg->heur = wfadaptive;
-  cfg->h_min_len = wfadaptive ? wf->heuristic.min_wavefront_length : 0;
-  cfg->h_max_dist = wfadaptive ? wf->heuristic.max_distance_threshold : 0;
-  cfg->h_steps = wfadaptive ? wf->heuristic.steps_between_cutoffs : 0;
+  cfg->heur = strategy;
+  cfg->h_min_len = wf->heuristic.min_wavefront_length;
+  cfg->h_max_dist = wf->heuristic.max_distance_threshold;
+  cfg->h_steps = wf->heuristic.steps_between_cutoffs;
+  cfg->h_xdrop = wf->heuristic.xdrop;
+  cfg->h_zdrop = wf->heuristic.zdrop;
+  cfg->h_min_k = wf->heuristic.min_k;
+  cfg->h_max_k = wf->heuristic.max_k;
   /* alignment form (wavefront/wavefront_attributes.h:55-69) */
   cfg->endsfree = (form->span == alignment_endsfree);
   cfg->extension = cfg->endsfree && form->extension;
@@ -391,9 +407,9 @@ static int align_one(wavefront_aligner_t* const wf, const char* seqbuf, int plen
   if (make_cfg(wf, &cfg) != 0) {
     if (!warned_config) {
       fprintf(stderr,
-              "[wfa2gpu] configuration not computed on the GPU (needs gap-affine or "
-              "gap-affine-2p; heuristic none or wf-adaptive; end-to-end, or ends-free "
-              "outside BiWFA with match 0 or no begin-free lengths)\n");
+              "[wfa2gpu] configuration not computed on the GPU (drops with edit/indel; "
+              "BiWFA with a heuristic other than wf-adaptive or with free ends; begin-free "
+              "lengths with match < 0 or edit/indel)\n");
       warned_config = 1;
     }
     wf->align_status.status = WF_STATUS_UNATTAINABLE;

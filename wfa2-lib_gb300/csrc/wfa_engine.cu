@@ -216,6 +216,10 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   base.h_min_len = cfg.h_min_len;
   base.h_max_dist = cfg.h_max_dist;
   base.h_steps = cfg.h_steps;
+  base.h_xdrop = cfg.h_xdrop;
+  base.h_zdrop = cfg.h_zdrop;
+  base.h_min_k = cfg.h_min_k;
+  base.h_max_k = cfg.h_max_k;
   base.pbf = cfg.pbf;
   base.pef = cfg.pef;
   base.tbf = cfg.tbf;

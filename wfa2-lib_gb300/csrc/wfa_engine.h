@@ -21,8 +21,10 @@ typedef struct {
   int score_only;
   int max_steps; /* INT32_MAX when unlimited */
   int ultralow;  /* 1: BiWFA (wavefront_memory_ultralow) */
-  /* wf-adaptive heuristic (heur = 1) and its parameters; 0: exact */
+  /* heuristic strategy: a bit set of wf_heuristic_strategy values
+   * (wavefront/wavefront_heuristic.h:41-49), 0 exact, and its parameters */
   int heur, h_min_len, h_max_dist, h_steps;
+  int h_xdrop, h_zdrop, h_min_k, h_max_k;
   /* alignment form (wavefront/wavefront_attributes.h:55-69): endsfree = 1
    * with the four free lengths, or extension = 1 (per-pair presets and
    * maximal-score trimming with the user's penalties um..ue2) */

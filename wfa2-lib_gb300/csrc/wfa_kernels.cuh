@@ -57,6 +57,10 @@ struct Penalties {
   int RI2;  // I2/D2 ring depth = e2+1 (affine2p)
 };
 
+// heuristic strategy bits (wavefront/wavefront_heuristic.h:41-49)
+constexpr int kHsBandedStatic = 0x01, kHsBandedAdaptive = 0x02, kHsWfadaptive = 0x04;
+constexpr int kHsXdrop = 0x10, kHsZdrop = 0x20, kHsWfmash = 0x40;
+
 struct KParams {
   Penalties pen;
   // distance metric (wavefront/wavefront_penalties.h:42-48): 0 indel, 1 edit,
@@ -65,9 +69,11 @@ struct KParams {
   // gap-affine-2p
   int metric;
   int max_steps;
-  // wf-adaptive heuristic (0: none); min wavefront length, max distance
-  // threshold, steps between cut-offs (wavefront/wavefront_heuristic.h:42-69)
+  // heuristic strategy bits (wavefront/wavefront_heuristic.h:41-49; 0: none)
+  // and parameters: min wavefront length, max distance threshold, steps
+  // between cut-offs, x-drop, z-drop, band limits (:51-69)
   int heur, h_min_len, h_max_dist, h_steps;
+  int h_xdrop, h_zdrop, h_min_k, h_max_k;
   // inputs
   const uint8_t* seqs;
   const int64_t* p_off;

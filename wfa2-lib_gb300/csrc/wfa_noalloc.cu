@@ -82,6 +82,7 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   if (cfg->metric != 3 && cfg->metric != 4) return -2;  // WF2G_ERR_CONFIG (gap-affine metrics only)
   if (cfg->ultralow) return -2;  // BiWFA allocates per recursion level
   if (cfg->endsfree) return -2;  // the ends-free kernels are not in the fixed-scratch set
+  if (cfg->heur & ~wf2g::kHsWfadaptive) return -2;  // wf-adaptive or none only
   const bool cigar = !cfg->score_only;
   if (cigar && (!d_ops || !d_opsoff || !d_opslen)) return -3;
   int err = 0;

@@ -296,7 +296,7 @@ extern "C" void* wf2g_server_new(const wf2g_cfg_t* cfg, int64_t hbm_budget,
   }
   // the BiWFA fallback has no ends-free form (wavefront/wavefront_align.c:67-82)
   // and serves the gap-affine metrics only
-  if (!cfg || cfg->ultralow || cfg->endsfree || cfg->metric <= 2) {
+  if (!cfg || cfg->ultralow || cfg->endsfree || cfg->metric <= 2 || (cfg->heur & ~wf2g::kHsWfadaptive)) {
     if (err) *err = WF2G_ERR_CONFIG_;
     return nullptr;
   }

@@ -33,7 +33,13 @@ INDEL, EDIT, GAP_LINEAR, GAP_AFFINE, GAP_AFFINE_2P = 0, 1, 2, 3, 4
 COMPUTE_SCORE, COMPUTE_ALIGNMENT = 0, 1
 MEM_HIGH, MEM_MED, MEM_LOW, MEM_ULTRALOW = 0, 1, 2, 3
 WF_HEURISTIC_NONE = 0
+# wavefront/wavefront_heuristic.h:41-49
+WF_HEURISTIC_BANDED_STATIC = 0x1
+WF_HEURISTIC_BANDED_ADAPTIVE = 0x2
 WF_HEURISTIC_WFADAPTIVE = 0x4
+WF_HEURISTIC_XDROP = 0x10
+WF_HEURISTIC_ZDROP = 0x20
+WF_HEURISTIC_WFMASH = 0x40
 
 
 # ------------------------------------------------------------ ABI mirror
@@ -268,6 +274,11 @@ class Config:
     # alignment form: None (end-to-end), "extension", or the ends-free lengths
     # (pattern_begin_free, pattern_end_free, text_begin_free, text_end_free)
     form: tuple | str | None = None
+    # any heuristic strategy set (overrides wfadaptive): a dict with
+    # "strategy" (WF_HEURISTIC_* bits) and the wavefront_heuristic_t fields it
+    # uses (min_wavefront_length, max_distance_threshold,
+    # steps_between_cutoffs, xdrop, zdrop, min_k, max_k)
+    heuristic: dict | None = None
 
     def attributes(self) -> AlignerAttr:
         a = default_attributes()
@@ -292,6 +303,9 @@ class Config:
             a.heuristic.strategy = WF_HEURISTIC_WFADAPTIVE
             (a.heuristic.min_wavefront_length, a.heuristic.max_distance_threshold,
              a.heuristic.steps_between_cutoffs) = self.wfadaptive
+        if self.heuristic:
+            for key, value in self.heuristic.items():
+                setattr(a.heuristic, key, value)
         a.memory_mode = self.memory_mode
         if self.max_steps > 0:
             a.system.max_alignment_steps = self.max_steps
