@@ -14,9 +14,8 @@ the cell, the reference takes back CIGAR operations it already wrote; the GPU
 records each cell's own source instead.  The CPU checker flags those pairs
 (FLAG_STALE_SOURCE); they are counted, not compared.
 
-Configurations the GPU does not compute yet (z-drop with a full alignment;
-gap-affine-2p with x-drop, z-drop or the adaptive band; the static band in
-score-only scope) must be refused: WF2G_ERR_CONFIG for a batch."""
+Configurations the GPU does not compute yet (z-drop with a full alignment,
+z-drop with gap-affine-2p) must be refused: WF2G_ERR_CONFIG for a batch."""
 import pytest
 
 import helpers
@@ -35,11 +34,7 @@ def _spec(name):
 
 def _served(metric, score_only, strategy):
     """The GPU's refusals (make_cfg in wfa2-lib_gb300/csrc/wfa_aligner.c)."""
-    if strategy & 0x20 and not score_only:
-        return False
-    if metric == 4 and strategy & (0x10 | 0x20 | 0x02):
-        return False
-    return not (strategy & 0x01 and score_only)
+    return not (strategy & 0x20 and (not score_only or metric == 4))
 
 
 def _gpu(W, cfg, b):
@@ -143,8 +138,8 @@ def test_heuristic_rejections(gpu_available, wfa):
     for cfg in [W.Config(metric=W.EDIT, heuristic=dict(strategy=0x10, xdrop=20)),
                 W.Config(metric=W.INDEL, heuristic=dict(strategy=0x20, zdrop=20)),
                 W.Config(heuristic=dict(strategy=0x20, zdrop=20)),
-                W.Config(metric=W.GAP_AFFINE_2P, heuristic=dict(strategy=0x10, xdrop=20)),
-                W.Config(score_only=True, heuristic=dict(strategy=0x01, min_k=-9, max_k=9)),
+                W.Config(metric=W.GAP_AFFINE_2P, score_only=True,
+                         heuristic=dict(strategy=0x20, zdrop=20)),
                 W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x01, min_k=-9,
                                                                     max_k=9))]:
         al = W.Aligner(cfg)

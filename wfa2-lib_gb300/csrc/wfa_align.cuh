@@ -908,14 +908,35 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
 
       // wavefront/wavefront_compute.c:40-87: output range
       int lo = INT32_MAX, hi = INT32_MIN;
-      if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
-      if (vMo1) { lo = min(lo, eMo1.x - 1); hi = max(hi, eMo1.y + 1); }
-      if (vI1) { lo = min(lo, eI1.x + 1); hi = max(hi, eI1.y + 1); }
-      if (vD1) { lo = min(lo, eD1.x - 1); hi = max(hi, eD1.y - 1); }
-      if (A2P) {
-        if (vMo2) { lo = min(lo, eMo2.x - 1); hi = max(hi, eMo2.y + 1); }
-        if (vI2) { lo = min(lo, eI2.x + 1); hi = max(hi, eI2.y + 1); }
-        if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
+      if (HEUR && !edit_like) {
+        // The reference widens the range by every input, a null one with the
+        // all-NULL wavefront's limits [1,-1] (wavefront/wavefront.c:110-117),
+        // so the range reaches diagonal 0.  Exact runs read only NULLs out
+        // there; under a cut-off the rows' windows can still hold cells.
+        const int2 nl = make_int2(1, -1);
+        const int2 lMx = vMx ? eMx : nl, lMo1 = vMo1 ? eMo1 : nl;
+        lo = min(lMx.x, lMo1.x - 1);
+        hi = max(lMx.y, lMo1.y + 1);
+        if (!lin) {  // gap-linear stops at the mismatch and open inputs
+          const int2 lI1 = vI1 ? eI1 : nl, lD1 = vD1 ? eD1 : nl;
+          lo = min(lo, min(lI1.x + 1, lD1.x - 1));
+          hi = max(hi, max(lI1.y + 1, lD1.y - 1));
+        }
+        if (A2P) {
+          const int2 lMo2 = vMo2 ? eMo2 : nl, lI2 = vI2 ? eI2 : nl, lD2 = vD2 ? eD2 : nl;
+          lo = min(lo, min(lMo2.x - 1, min(lI2.x + 1, lD2.x - 1)));
+          hi = max(hi, max(lMo2.y + 1, max(lI2.y + 1, lD2.y - 1)));
+        }
+      } else {
+        if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
+        if (vMo1) { lo = min(lo, eMo1.x - 1); hi = max(hi, eMo1.y + 1); }
+        if (vI1) { lo = min(lo, eI1.x + 1); hi = max(hi, eI1.y + 1); }
+        if (vD1) { lo = min(lo, eD1.x - 1); hi = max(hi, eD1.y - 1); }
+        if (A2P) {
+          if (vMo2) { lo = min(lo, eMo2.x - 1); hi = max(hi, eMo2.y + 1); }
+          if (vI2) { lo = min(lo, eI2.x + 1); hi = max(hi, eI2.y + 1); }
+          if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
+        }
       }
       const int width = hi - lo + 1;
       if (CIGAR && (s >= p.table_cap || (!pooled && cursor + width > p.bits_cap))) {
