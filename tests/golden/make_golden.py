@@ -187,6 +187,14 @@ HEURISTIC_SETS = {
     "w1_indel_wfmash_score": (1, 60, "indel", True, 0, 0, None,
                               _h(WM, min_wavefront_length=10, max_distance_threshold=50,
                                  steps_between_cutoffs=1)),
+    # null inputs widen the range to diagonal 0 (wavefront/wavefront.c:110-117):
+    # cases where that regrows cut cells
+    "w5_affine_p4_bstatic_score_6k": (5, 16, "affine.p4", True, 6000, 300, None,
+                                      _h(BS, min_k=-40, max_k=40)),
+    "w1_affine2p_xdrop_full": (1, 120, "affine2p", False, 0, 0, None,
+                               _h(XD, xdrop=80, steps_between_cutoffs=1)),
+    "w6_affine2p_badapt_full": (6, 60, "affine2p", False, 0, 0, None,
+                                _h(BA, min_k=-25, max_k=25, steps_between_cutoffs=2)),
 }
 
 
