@@ -1340,6 +1340,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     bool bad = false;
     bool items_full = false;  // walk items did not fit the back-trace slice
     int k_begin = 0;          // diagonal of the score-0 cell the walk reaches
+    // z-drop: the walk starts at the best cell's diagonal from the current
+    // score, where the current wavefront may hold no cell; the reference then
+    // reads the sources' windows (wavefront/wavefront_backtrace.c:62-219), or,
+    // finding none, writes the beginning as matches and gaps (:490-505)
+    bool zfirst = zdrop, znosrc = false;
     if (G == 32 || wig == 0) {
       int st = ce;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
       int ss = s, kk = end_k;
@@ -1362,6 +1367,52 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         }
         if (!CHK(ss < p.table_cap, 34, ss)) { bad = true; break; }
         const BtRow te = table[ss];
+        if (zfirst) {
+          zfirst = false;
+          if (te.width <= 0 || kk < te.lo || kk - te.lo >= te.width) {
+            // candidates as the reference packs them: (offset << 4) | type,
+            // larger wins (wavefront/wavefront_backtrace.c:36-59)
+            auto cand = [&](int back, int r, int k, int add, int type) -> int64_t {
+              if (ss - back < 0) return (int64_t)kNull;
+              const int2 w = imeta[r];
+              if (k < w.x || k > w.y) return (int64_t)kNull;
+              return ((int64_t)(RING_LD(row(r), k) + add) << 4) | type;
+            };
+            int64_t best = has_x ? cand(pen.x, ring_back(curM, pen.x, pen.R), kk, 1, 9) : kNull;
+            const int rMo1 = ring_back(curM, pen.o1 + pen.e1, pen.R);
+            best = max(best, cand(pen.o1 + pen.e1, rMo1, kk - 1, 1, 1));
+            best = max(best, cand(pen.o1 + pen.e1, rMo1, kk + 1, 0, 5));
+            if (!lin) {
+              const int s1 = ring_back(cur1, pen.e1, pen.RI1);
+              best = max(best, cand(pen.e1, rowI1 + s1, kk - 1, 1, 2));
+              best = max(best, cand(pen.e1, rowD1 + s1, kk + 1, 0, 6));
+            }
+            if (A2P) {
+              const int rMo2 = ring_back(curM, pen.o2 + pen.e2, pen.R);
+              const int s2 = ring_back(cur2, pen.e2, pen.RI2);
+              best = max(best, cand(pen.o2 + pen.e2, rMo2, kk - 1, 1, 3));
+              best = max(best, cand(pen.o2 + pen.e2, rMo2, kk + 1, 0, 7));
+              best = max(best, cand(pen.e2, rowI2 + s2, kk - 1, 1, 4));
+              best = max(best, cand(pen.e2, rowD2 + s2, kk + 1, 0, 8));
+            }
+            if (best < 0) { znosrc = true; break; }
+            char op;
+            switch ((int)(best & 15)) {
+              case 9: op = 'X'; ss -= pen.x; break;
+              case 1: op = 'I'; kk -= 1; ss -= pen.o1 + pen.e1; break;
+              case 2: op = 'I'; kk -= 1; ss -= pen.e1; st = 1; break;
+              case 3: op = 'I'; kk -= 1; ss -= pen.o2 + pen.e2; break;
+              case 4: op = 'I'; kk -= 1; ss -= pen.e2; st = 3; break;
+              case 5: op = 'D'; kk += 1; ss -= pen.o1 + pen.e1; break;
+              case 6: op = 'D'; kk += 1; ss -= pen.e1; st = 2; break;
+              case 7: op = 'D'; kk += 1; ss -= pen.o2 + pen.e2; break;
+              default: op = 'D'; kk += 1; ss -= pen.e2; st = 4; break;
+            }
+            if (lane == 0 && CHK(n < items_cap, 36, n)) items[n] = (uint8_t)op;
+            ++n;
+            continue;
+          }
+        }
         if (te.width <= 0 || kk < te.lo || kk - te.lo >= te.width) { bad = true; break; }
         const int64_t bi = te.pos + (kk - te.lo);
         if (!CHK(pooled || (bi >= 0 && bi < p.bits_cap), 35, bi)) { bad = true; break; }
@@ -1428,7 +1479,17 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         h = max(0, k_begin);
       }
       int pops = 0;  // z-drop: trailing gaps the first match count takes back
-      for (int64_t i = n - 1; i >= 0; --i) {
+      if (znosrc) {
+        // no source at the best cell: insertions, deletions, then the
+        // matches up to it (wavefront/wavefront_backtrace.c:490-505)
+        const int mn = min(end_v, end_h), ni0 = end_h - mn, nd0 = end_v - mn;
+        for (int j = lane; j < ni0 + nd0 + mn; j += 32)
+          if (CHK(j < plen + tlen, 41, j)) out[j] = j < ni0 ? 'I' : (j < ni0 + nd0 ? 'D' : 'M');
+        out_n = ni0 + nd0 + mn;
+        v = end_v;
+        h = end_h;
+      }
+      for (int64_t i = znosrc ? -1 : n - 1; i >= 0; --i) {
         const uint8_t it = items[i];
         if (it == 'E') {
           int L;
@@ -1441,8 +1502,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
             L = max(0, end_h - h);
             pops = max(0, h - end_h);
           } else {
-            L = lcp<ENC>(P, T, v, h, min(plen - v, tlen - h), nwords, g_pair);
+            // a z-dropped trace can run past an end (the reference does not
+            // check): no matches there
+            L = lcp<ENC>(P, T, v, h, max(0, min(plen - v, tlen - h)), nwords, g_pair);
           }
+          if (out_n + L > plen + tlen) { bad = true; break; }
           for (int j = lane; j < L; j += 32)
             if (CHK(out_n + j < plen + tlen, 37, out_n + j)) out[out_n + j] = 'M';
           out_n += L;
@@ -1452,6 +1516,9 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           if (it == 'X') { bad = (v >= plen || h >= tlen); ++v; ++h; }
           else if (it == 'I') { bad = (h >= tlen); ++h; }
           else { bad = (v >= plen); ++v; }
+          // the reference writes a z-dropped trace's operations past an end
+          // as they come; its trim decides
+          if (zdrop) bad = out_n >= plen + tlen;
           if (bad) break;
           if (lane == 0 && CHK(out_n < plen + tlen, 38, out_n)) out[out_n] = it;
           ++out_n;
