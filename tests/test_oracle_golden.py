@@ -176,3 +176,64 @@ def test_oracle_edge_cases(oracle_mod):
     assert [r.cigar(i) for i in range(b.n)] == ["", "D", "III", "MMMM", "M" * 40, "XXXX"]
     rs = O.align(b, O.Penalties(), max_steps=5)
     assert int(rs.status[5]) == -100 and int(rs.score[5]) == -5
+
+
+def _mixed_pairs(O, seed, n):
+    """Seeded pairs of four kinds: similar, a similar prefix then an unrelated
+    tail, one long indel, unrelated."""
+    import random
+    rng = random.Random(seed)
+
+    def mutate(s, rate):
+        out = []
+        for c in s:
+            r = rng.random()
+            if r < rate / 3:
+                out.append(rng.choice("ACGT"))
+            elif r < 2 * rate / 3:
+                pass
+            elif r < rate:
+                out += [c, rng.choice("ACGT")]
+            else:
+                out.append(c)
+        return "".join(out)
+
+    pats, txts = [], []
+    for i in range(n):
+        length = rng.randint(50, 700)
+        p = "".join(rng.choice("ACGT") for _ in range(length))
+        kind = i % 4
+        if kind == 0:
+            t = mutate(p, rng.uniform(0, 0.2))
+        elif kind == 1:
+            cut = rng.randint(length // 4, length)
+            t = mutate(p[:cut], 0.05) + "".join(rng.choice("ACGT") for _ in range(rng.randint(0, length)))
+        elif kind == 2:
+            a = rng.randint(0, length)
+            t = mutate(p[:a] + p[min(length, a + rng.randint(10, 150)):], 0.03)
+        else:
+            t = "".join(rng.choice("ACGT") for _ in range(rng.randint(0, 300)))
+        pats.append(p.encode())
+        txts.append(t.encode())
+    return O.PairBatch.from_lists(pats, txts)
+
+
+def test_oracle_flags(oracle_mod, wfa):
+    """The checker marks the pairs its GPU comparison leaves out: back-traces
+    through a wavefront a cut emptied (common under a wide x-drop on unrelated
+    sequences, absent on the generator's workloads) and runs past the
+    reference's per-pair wavefront table (x-drop with match 0)."""
+    O, W = oracle_mod, wfa
+    mixed = _mixed_pairs(O, 1, 200)
+    r = O.align(mixed, O.Penalties(), heuristic=O.Heuristic(O.HS_XDROP, xdrop=100,
+                                                            steps_between_cutoffs=2))
+    assert ((r.flags & O.FLAG_STALE_SOURCE) > 0).sum() > 50
+    assert ((r.flags & O.FLAG_OVER_BOUND) > 0).sum() > 10
+    r = O.align(mixed, O.Penalties(), heuristic=O.Heuristic(O.HS_WFADAPTIVE, 10, 50, 1))
+    assert not (r.flags & O.FLAG_OVER_BOUND).any()
+    for wl in (1, 6):
+        p = W.generate(wl, 120)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        r = O.align(b, O.Penalties(O.GAP_AFFINE, -2, 3, 1, 4),
+                    heuristic=O.Heuristic(O.HS_XDROP, xdrop=80, steps_between_cutoffs=1))
+        assert not r.flags.any()
