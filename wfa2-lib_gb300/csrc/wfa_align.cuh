@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           mhi = nhi;
           if (t == 0) {
             meta[curM] = make_int2(nlo, nhi);
-            if (!lin) {  // one component: nothing to intersect (:540-541)
+            if (!lin) {  // one component: nothing to intersect (:549)
               const int nr = A2P ? 4 : 2;
               for (int j = 0; j < nr; ++j) {
                 const int r = j == 0 ? rowI1 + cur1 : j == 1 ? rowD1 + cur1 : j == 2 ? rowI2 + cur2 : rowD2 + cur2;
@@ -1343,7 +1343,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
     // z-drop: the walk starts at the best cell's diagonal from the current
     // score, where the current wavefront may hold no cell; the reference then
     // reads the sources' windows (wavefront/wavefront_backtrace.c:62-219), or,
-    // finding none, writes the beginning as matches and gaps (:490-505)
+    // finding none, writes the beginning as matches and gaps (:505-516)
     bool zfirst = zdrop, znosrc = false;
     if (G == 32 || wig == 0) {
       int st = ce;  // 0 M, 1 I1, 2 D1, 3 I2, 4 D2
@@ -1481,7 +1481,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       int pops = 0;  // z-drop: trailing gaps the first match count takes back
       if (znosrc) {
         // no source at the best cell: insertions, deletions, then the
-        // matches up to it (wavefront/wavefront_backtrace.c:490-505)
+        // matches up to it (wavefront/wavefront_backtrace.c:505-516)
         const int mn = min(end_v, end_h), ni0 = end_h - mn, nd0 = end_v - mn;
         for (int j = lane; j < ni0 + nd0 + mn; j += 32)
           if (CHK(j < plen + tlen, 41, j)) out[j] = j < ni0 ? 'I' : (j < ni0 + nd0 ? 'D' : 'M');
