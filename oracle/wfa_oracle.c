@@ -124,9 +124,6 @@ common:
   p->tef = cfg[18];
   p->extension = p->endsfree && cfg[19] != 0;
   if (p->endsfree && (p->pbf < 0 || p->pef < 0 || p->tbf < 0 || p->tef < 0)) return -1;
-  /* with match < 0 a begin-free run also re-enters at every score that is a
-   * multiple of -match (wavefront/wavefront_compute.c:124-262): not restated */
-  if (p->endsfree && !p->extension && p->match != 0 && (p->pbf > 0 || p->tbf > 0)) return -1;
   /* edit and indel never widen the score-0 wavefront's initialised window
    * [0,0] (wavefront/wavefront_compute_edit.c:321-374), so their back-trace
    * reads begin-free diagonals as sourceless: not restated */
@@ -236,6 +233,65 @@ static void init_ends(orow_t* r, int lo, int hi) {
   }
 }
 
+/* Ends-free with match < 0: the begin-free diagonals enter one at a time, at
+ * the scores that are multiples of -match (wavefront/wavefront_compute.c:
+ * 124-145).  Returns that diagonal (and which sides are free), or -1. */
+static int endsfree_k_of(const pen_t* p, int endsfree, int s, int* text_free,
+                         int* pattern_free) {
+  if (!endsfree || p->match == 0 || p->extension) return -1;
+  if (p->pbf == 0 && p->tbf == 0) return -1;
+  if (s % (-p->match) != 0) return -1;
+  const int ek = s / (-p->match);
+  *text_free = p->tbf >= ek;
+  *pattern_free = p->pbf >= ek;
+  return (*text_free || *pattern_free) ? ek : -1;
+}
+
+/* The begin cells (0,ek) and (ek,0) enter the computed M wavefront when they
+ * lie ahead of it (wavefront/wavefront_compute.c:173-215), before trimming. */
+static void endsfree_init(orow_t* r, int ek, int text_free, int pattern_free) {
+  const int lo = r->lo, hi = r->hi;
+  if (text_free) {
+    if (hi >= ek) {
+      if (r->off[ek] <= ek) r->off[ek] = ek;
+    } else {
+      for (int k = hi + 1; k < ek; ++k) r->off[k] = WF_NULL;
+      r->off[ek] = ek;
+      r->hi = ek;
+    }
+  }
+  if (pattern_free) {
+    const int k0 = -ek;
+    if (lo <= k0) {
+      if (r->off[k0] <= 0) r->off[k0] = 0;
+    } else {
+      r->off[k0] = 0;
+      for (int k = k0 + 1; k < lo; ++k) r->off[k] = WF_NULL;
+      r->lo = k0;
+    }
+  }
+}
+
+/* A null step that still holds begin cells: an M wavefront of only those
+ * (wavefront/wavefront_compute.c:217-262), untrimmed. */
+static void endsfree_null_row(oracle_ws_t* ws, const pen_t* p, int s, int ek, int text_free,
+                              int pattern_free) {
+  const int lo = pattern_free ? -ek : ek, hi = text_free ? ek : -ek;
+  ws->hlo = imin(ws->hlo, lo - (p->scope + 1));
+  ws->hhi = imax(ws->hhi, hi + (p->scope + 1));
+  kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
+  kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
+  orow_t* r = row_at(ws, s, C_M);
+  r->off = row_storage(ws, s, C_M, ws->hlo, ws->hhi);
+  r->exists = 1;
+  r->null = 0;
+  r->lo = r->ilo = lo;
+  r->hi = r->ihi = hi;
+  for (int k = lo; k <= hi; ++k) r->off[k] = WF_NULL;
+  if (text_free) r->off[ek] = ek;
+  if (pattern_free) r->off[-ek] = 0;
+}
+
 /* wavefront/wavefront_compute.c:579-613 */
 static void trim_row(orow_t* r, int plen, int tlen) {
   int k;
@@ -320,14 +376,21 @@ static int64_t compute_step_linear(oracle_ws_t* ws, const pen_t* p, int s, int p
   } else {
     if (mx->null && mo->null) {
       (*null_steps)++;
+      int tf, pf;
+      const int ek = endsfree_k_of(p, endsfree, s, &tf, &pf);
+      if (ek >= 0) endsfree_null_row(ws, p, s, ek, tf, pf);
       return 0;
     }
     *null_steps = 0;
     lo = imin(mx->lo, mo->lo - 1);
     hi = imax(mx->hi, mo->hi + 1);
   }
-  ws->hlo = imin(ws->hlo, lo - (p->scope + 1));
-  ws->hhi = imax(ws->hhi, hi + (p->scope + 1));
+  int tf = 0, pf = 0;
+  const int ek = editlike ? -1 : endsfree_k_of(p, endsfree, s, &tf, &pf);
+  /* the allocation also covers the begin cells (wavefront/wavefront_compute.c:419-428) */
+  const int alo = (ek >= 0 && pf) ? imin(lo, -ek) : lo, ahi = (ek >= 0 && tf) ? imax(hi, ek) : hi;
+  ws->hlo = imin(ws->hlo, alo - (p->scope + 1));
+  ws->hhi = imax(ws->hhi, ahi + (p->scope + 1));
   kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
   kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
   nullrow.off = kbuf_at0(&ws->nullbuf);
@@ -363,6 +426,7 @@ static int64_t compute_step_linear(oracle_ws_t* ws, const pen_t* p, int s, int p
     if ((uint32_t)(mmax - k) > (uint32_t)plen) mmax = WF_NULL;
     o_m[k] = mmax;
   }
+  if (ek >= 0) endsfree_init(r, ek, tf, pf);
   trim_row(r, plen, tlen);
   if (editlike) {
     if (r->null) *null_steps = INT_MAX / 2;
@@ -394,6 +458,9 @@ static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, in
   for (int c = 0; c < NCOMP; ++c) memset(row_at(ws, s, c), 0, sizeof(orow_t));
   if (mx->null && mo1->null && i1e->null && d1e->null && mo2->null && i2e->null && d2e->null) {
     (*null_steps)++;
+    int tf, pf;
+    const int ek = endsfree_k_of(p, endsfree, s, &tf, &pf);
+    if (ek >= 0) endsfree_null_row(ws, p, s, ek, tf, pf);
     return 0;
   }
   *null_steps = 0;
@@ -414,9 +481,13 @@ static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, in
     hi = imax(hi, d2e->hi - 1);
   }
   /* wavefront/wavefront_compute.c:88-104: allocation padded by scope+1 and
-   * never narrower than any earlier allocation of the alignment */
-  ws->hlo = imin(ws->hlo, lo - (p->scope + 1));
-  ws->hhi = imax(ws->hhi, hi + (p->scope + 1));
+   * never narrower than any earlier allocation of the alignment; it also
+   * covers ends-free begin cells (:419-428) */
+  int tf = 0, pf = 0;
+  const int ek = endsfree_k_of(p, endsfree, s, &tf, &pf);
+  const int elo = (ek >= 0 && pf) ? imin(lo, -ek) : lo, ehi = (ek >= 0 && tf) ? imax(hi, ek) : hi;
+  ws->hlo = imin(ws->hlo, elo - (p->scope + 1));
+  ws->hhi = imax(ws->hhi, ehi + (p->scope + 1));
   kbuf_cover(&ws->nullbuf, ws->hlo, ws->hhi, 1);
   kbuf_cover(&ws->victim, ws->hlo, ws->hhi, 0);
   nullrow.off = kbuf_at0(&ws->nullbuf);
@@ -499,6 +570,8 @@ static int64_t compute_step(oracle_ws_t* ws, const pen_t* p, int s, int plen, in
       o_m[k] = mmax;
     }
   }
+  /* wavefront/wavefront_compute.c:614-633: begin cells, then trimming */
+  if (ek >= 0) endsfree_init(row_at(ws, s, C_M), ek, tf, pf);
   for (int c = 0; c < NCOMP; ++c) {
     orow_t* r = row_at(ws, s, c);
     if (r->exists) trim_row(r, plen, tlen);

@@ -27,7 +27,7 @@ sources are available; the fixtures themselves travel with the repo).
    (it faults in alignment scope and loops in score-only scope).  Each set
    lists the pair indices it keeps.
 
-Usage:  python tests/golden/make_golden.py [/path/to/WFA2-lib] [--only=heuristics]
+Usage:  python tests/golden/make_golden.py [/path/to/WFA2-lib] [--only=endsfree|heuristics]
 """
 import gzip
 import json
@@ -135,6 +135,14 @@ ENDSFREE = {
     "w1_linear_ef": (1, 200, "linear", False, 0, 0, (20, 20, 20, 20), None),
     "w1_linear_ext": (1, 200, "linear.m1", False, 0, 0, "extension", None),
     "w5_indel_endonly": (5, 60, "indel", False, 500, 100, (0, 40, 0, 40), None),
+    # begin-free lengths with match < 0: the free diagonals enter at the scores
+    # that are multiples of -match (wavefront/wavefront_compute.c:124-262)
+    "w1_affine_p4_ef_begin": (1, 200, "affine.p4", False, 0, 0, (20, 20, 20, 20), None),
+    "w1_affine_p4_ef_begin_score": (1, 200, "affine.p4", True, 0, 0, (20, 20, 20, 20), None),
+    "w5_affine_p3_ef_text": (5, 100, "affine.p3", False, 300, 150, (0, 0, 60, 60), None),
+    "w1_linear_m1_ef_begin": (1, 150, "linear.m1", False, 0, 0, (30, 10, 30, 10), None),
+    "w1_affine_p4_ef_begin_wfapt": (1, 150, "affine.p4", False, 0, 0, (15, 15, 15, 15),
+                                    (10, 50, 1)),
 }
 
 
@@ -213,6 +221,8 @@ def main():
     only = [a[len("--only="):] for a in sys.argv[1:] if a.startswith("--only=")]
     if only == ["heuristics"]:
         return heuristics_fixtures()
+    if only == ["endsfree"]:
+        return endsfree_fixtures()
     ref = args[0] if args else "/root/reference"
     with open(os.path.join(ref, "tests", "wfa.utest.seq"), "rb") as f:
         raw = f.read()
@@ -259,6 +269,15 @@ def main():
     with open(os.path.join(HERE, "synthetic_expected.json"), "w") as f:
         json.dump(synth, f, separators=(",", ":"))
 
+    endsfree_fixtures()
+    heuristics_fixtures()
+
+
+def endsfree_fixtures():
+    from oracle import oracle as O
+    import wfa2gpu as W
+    O.build(ref=True)
+    W.build()
     ends = {}
     for name, (wl, n, pset, so, param, param2, form, heur) in ENDSFREE.items():
         m, mi, mm_, o1, e1, o2, e2 = {**PENALTY_SETS, **EXTRA_SETS}[pset]
@@ -275,8 +294,6 @@ def main():
         print(name, "done")
     with open(os.path.join(HERE, "endsfree_expected.json"), "w") as f:
         json.dump(ends, f, separators=(",", ":"))
-
-    heuristics_fixtures()
 
 
 def heuristics_fixtures():
