@@ -859,8 +859,21 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
       const int2 oldI2 = A2P ? imeta[rowI2 + cur2] : kEmpty;
       const int2 oldD2 = A2P ? imeta[rowD2 + cur2] : kEmpty;
 
-      // wavefront/wavefront_compute_affine.c:236-243: all inputs null -> null step
-      if (!(vMx | vMo1 | vI1 | vD1 | vMo2 | vI2 | vD2)) {
+      // ends-free with match < 0: the begin cells (0,ek) and (ek,0) enter at
+      // the scores that are multiples of -match, ek = s / -match
+      // (wavefront/wavefront_compute.c:124-262); INT32_MIN: none
+      int ekT = INT32_MIN, ekP = INT32_MIN;
+      if (EF && pen.match != 0 && cb == 0 && (pbf > 0 || tbf > 0) && s % (-pen.match) == 0) {
+        const int ek = s / (-pen.match);
+        if (tbf >= ek) ekT = ek;
+        if (pbf >= ek) ekP = -ek;
+      }
+      const bool inject = EF && (ekT != INT32_MIN || ekP != INT32_MIN);
+      const bool all_null = !(vMx | vMo1 | vI1 | vD1 | vMo2 | vI2 | vD2);
+
+      // wavefront/wavefront_compute_affine.c:236-243: all inputs null -> null
+      // step (with begin cells to enter, an M wavefront of those)
+      if (all_null && !inject) {
         ++null_steps;
         // Exact runs read a row only within its limits, so a null step just
         // empties the limits of the slots it takes over; they keep their old
@@ -904,7 +917,8 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         }
         continue;
       }
-      null_steps = 0;
+      if (all_null) ++null_steps;  // the begin cells alone (:382-407)
+      else null_steps = 0;
 
       // wavefront/wavefront_compute.c:40-87: output range
       int lo = INT32_MAX, hi = INT32_MIN;
@@ -936,6 +950,19 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           if (vMo2) { lo = min(lo, eMo2.x - 1); hi = max(hi, eMo2.y + 1); }
           if (vI2) { lo = min(lo, eI2.x + 1); hi = max(hi, eI2.y + 1); }
           if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
+        }
+      }
+      // begin cells beyond the computed range [lo0,hi0] widen it on their
+      // side, with NULL cells between (wavefront/wavefront_compute.c:173-262);
+      // a step whose inputs are all null computes no cell
+      const int lo0 = all_null ? INT32_MAX : lo, hi0 = all_null ? INT32_MIN : hi;
+      if (inject) {
+        if (all_null) {
+          lo = min(ekP != INT32_MIN ? ekP : ekT, ekT != INT32_MIN ? ekT : ekP);
+          hi = max(ekP != INT32_MIN ? ekP : ekT, ekT != INT32_MIN ? ekT : ekP);
+        } else {
+          if (ekP != INT32_MIN) lo = min(lo, ekP);
+          if (ekT != INT32_MIN) hi = max(hi, ekT);
         }
       }
       const int width = hi - lo + 1;
@@ -1057,7 +1084,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (k + G <= hi) load_inputs(k + G);
         // wavefront/wavefront_compute_affine.c:66-84
         int32_t i1 = max(mo1_m, i1_e) + 1;
-        const int32_t d1 = max(mo1_p, d1_e);
+        int32_t d1 = max(mo1_p, d1_e);
         const int32_t mis = mx + 1;
         int32_t ins = i1, del = d1;
         int32_t i2 = kNull, d2 = kNull;
@@ -1068,8 +1095,21 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           ins = max(i1, i2);
           del = max(d1, d2);
         }
-        const int32_t best = max(del, max(mis, ins));
-        const bool okM = in_bounds(best, k, plen, tlen);
+        int32_t best = max(del, max(mis, ins));
+        if (inject && (k < lo0 || k > hi0)) {  // not computed: NULL
+          i1 = d1 = i2 = d2 = best = null_of<OffT>();
+        }
+        bool okM = in_bounds(best, k, plen, tlen);
+        // a begin cell replaces a computed one that does not lie ahead of it
+        bool begin_cell = false;
+        if (inject && (k == ekT || k == ekP)) {
+          const int32_t bo = k > 0 ? k : 0;  // offset of (0,k) or (-k,0)
+          if ((okM ? best : kNull) <= bo) {
+            best = bo;
+            okM = true;
+            begin_cell = true;
+          }
+        }
         // Trim tests (wavefront/wavefront_compute.c:579-613), simplified: a
         // non-NULL insertion keeps its source's v <= plen, a deletion its h <= tlen
         const bool okI1 = (uint32_t)i1 <= (uint32_t)tlen;
@@ -1150,6 +1190,7 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
               c |= (uint8_t)(wd2e >= gmo2p) << 6;
             }
           }
+          if (EF && begin_cell) c = kBegin;  // the walk stops here
           if (CHK(pooled || cursor + (k - lo) < p.bits_cap, 30, cursor + (k - lo))) brow[k] = c;
         }
       }
@@ -1418,6 +1459,12 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         if (!CHK(pooled || (bi >= 0 && bi < p.bits_cap), 35, bi)) { bad = true; break; }
         const uint8_t c = bt[bi];
         char op = 0;
+        if (EF && st == 0 && c == kBegin) {
+          // a begin cell entered at this score (ends-free, match < 0): the
+          // free beginning is written by the replay
+          k_begin = kk;
+          break;
+        }
         if (st == 0) {
           const int src = c & 7;
           if (src == kSrcX) { op = 'X'; ss -= pen.x; }

@@ -36,6 +36,8 @@ constexpr int kStInvalidForm = -400;
 //   bit 3     I1 extends (else opens)    bit 4  D1 extends
 //   bit 5     I2 extends                 bit 6  D2 extends
 enum : uint8_t { kSrcX = 0, kSrcD1 = 1, kSrcI1 = 2, kSrcD2 = 3, kSrcI2 = 4 };
+// choice byte of an ends-free begin cell entered after score 0 (match < 0)
+constexpr uint8_t kBegin = 0x80;
 
 // Back-trace row table entry, one per score: choice bytes of the row's cells
 // [lo, lo+width) start at byte `pos` of the back-trace store (the warp's slice,
