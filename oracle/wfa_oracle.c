@@ -1450,11 +1450,7 @@ int oracle_align_batch_flags(const int* cfg, int num_pairs, const char* sequence
       int32_t* end = out_end ? &out_end[2 * i] : NULL;
       if (ultralow) {
         oracle_bialign(&p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i], &ws,
-                       &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext);
-        if (end) {
-          end[0] = out_status[i] == ST_COMPLETED ? p_len[i] : -1;
-          end[1] = out_status[i] == ST_COMPLETED ? t_len[i] : -1;
-        }
+                       &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext, end);
       } else {
         oracle_align_one(&ws, &p, sequences + p_off[i], p_len[i], sequences + t_off[i], t_len[i],
                          &out_score[i], &out_status[i], ops, &out_ops_len[i], cells, ext, end,

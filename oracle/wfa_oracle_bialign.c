@@ -43,6 +43,7 @@ typedef struct {
   char* ops;
   int nops;
   int score; /* cigar->score */
+  int split0; /* the top level split at a breakpoint (it alone sets the CIGAR's end) */
   int64_t cells, ext; /* work counters: wavefront cells computed, bases matched */
 } bi_t;
 
@@ -260,7 +261,10 @@ static int bi_alignment(bi_t* b, int pb, int pe, int tb, int te, int cb, int ce,
   if (st != ST_OK) return st;
   st = bi_alignment(b, pb + bv, pe, tb + bh, te, bp.comp, ce, bp.score_r, level + 1);
   if (st != ST_OK) return st;
-  if (level == 0) b->score = oracle_classic_score(b->p, plen, tlen, bp.score);
+  if (level == 0) {
+    b->score = oracle_classic_score(b->p, plen, tlen, bp.score);
+    b->split0 = 1;
+  }
   return ST_OK;
 }
 
@@ -272,7 +276,7 @@ static char* reversed(const char* s, int n) {
 
 void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int tlen,
                     oracle_ws_t* ws, int32_t* out_score, int32_t* out_status, char* ops,
-                    int32_t* ops_len, int64_t* cells, int64_t* ext) {
+                    int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end) {
   (void)ws;
   bi_t b;
   memset(&b, 0, sizeof(b));
@@ -312,6 +316,16 @@ void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int 
     }
     *out_score = b.score;
     free(buf);
+  }
+  /* cigar->end_v/end_h: the score-only path sets the sequence lengths
+   * (wavefront/wavefront_bialign.c:1248-1257), a full alignment only when its
+   * top level split at a breakpoint (:1214-1220); a top level that went to the
+   * base case appends that CIGAR and keeps the cleared end
+   * (:159-194, alignment/cigar.c:79-90) */
+  if (end) {
+    const int set = (st == ST_OK) && (p->score_only || ops == NULL || b.split0);
+    end[0] = set ? plen : -1;
+    end[1] = set ? tlen : -1;
   }
   /* wavefront/wavefront_bialign.c:1286-1293 */
   if (st == ST_OK) *out_status = ST_COMPLETED;

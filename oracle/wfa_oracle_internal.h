@@ -135,6 +135,6 @@ void oracle_align_one(oracle_ws_t* ws, const pen_t* p, const char* P, int plen, 
 /* BiWFA (ultralow memory mode). */
 void oracle_bialign(const pen_t* p, const char* P, int plen, const char* T, int tlen,
                     oracle_ws_t* ws, int32_t* out_score, int32_t* out_status, char* ops,
-                    int32_t* ops_len, int64_t* cells, int64_t* ext);
+                    int32_t* ops_len, int64_t* cells, int64_t* ext, int32_t* end);
 
 #endif /* WFA_ORACLE_INTERNAL_H_ */

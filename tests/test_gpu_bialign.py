@@ -141,3 +141,26 @@ def test_bialign_per_pair_and_device_entry_points(gpu_available, wfa, oracle_mod
     for i in range(p.n):
         assert ops_h[ops_off[i]:ops_off[i] + ol[i]].tobytes().decode() == cig[i], i
     al.close()
+
+
+def test_biwfa_cigar_end_position(gpu_available, wfa, oracle_mod):
+    """wavefront_align() in ultralow mode leaves cigar->end_v/end_h where the
+    reference does: the sequence lengths after a score-only search or a
+    top-level split, (-1,-1) when the whole pair went to the base case
+    (wavefront/wavefront_bialign.c:159-194, :1214-1220, :1248-1257)."""
+    W, O = wfa, oracle_mod
+    for wl, n, pa, pb in [(0, 40, 0, 0), (1, 30, 0, 0)]:
+        p = W.generate(wl, n, param=pa, param2=pb)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        for metric in (W.GAP_AFFINE, W.GAP_AFFINE_2P):
+            for so in (False, True):
+                pen = O.Penalties(metric)
+                r = O.align(b, pen, memory_mode=O.MEM_ULTRALOW, score_only=so)
+                al = W.Aligner(W.Config(metric=metric, memory_mode=W.MEM_ULTRALOW, score_only=so))
+                for i in range(b.n):
+                    st, score, _ = al.align(b.pattern(i), b.text(i))
+                    cg = al._h.contents.cigar.contents
+                    assert (st, score, cg.end_v, cg.end_h) == (
+                        int(r.status[i]), int(r.score[i]), int(r.end[i][0]), int(r.end[i][1])), \
+                        (wl, metric, so, i)
+                al.close()

@@ -434,7 +434,7 @@ static int align_one(wavefront_aligner_t* const wf, const char* seqbuf, int plen
   const int rc = wf2g_engine_align(wf->engine, &cfg, 1, 0, seqbuf, &p_off, &plen, &t_off, &tlen,
                                    0, &score, &status, score_only ? NULL : cigar->operations,
                                    score_only ? NULL : &ops_off, score_only ? NULL : &ops_len,
-                                   cfg.ultralow ? NULL : end_info, NULL);
+                                   end_info, NULL);
   if (rc != 0) {
     wf->align_status.status = WF_STATUS_UNATTAINABLE;
     return WF_STATUS_UNATTAINABLE;
@@ -443,8 +443,10 @@ static int align_one(wavefront_aligner_t* const wf, const char* seqbuf, int plen
   if (status == WF_STATUS_ALG_COMPLETED || status == WF_STATUS_ALG_PARTIAL) {
     cigar->score = score;
     if (cfg.ultralow) {
-      cigar->end_v = plen;
-      cigar->end_h = tlen;
+      /* the lengths where the reference sets them (a score-only search, or a
+       * full alignment whose top level split at a breakpoint), else -1 */
+      cigar->end_v = end_info[0];
+      cigar->end_h = end_info[1];
       wf->align_status.score = wf_score_of(wf, score, plen, tlen);
     } else {
       cigar->end_v = end_info[0];

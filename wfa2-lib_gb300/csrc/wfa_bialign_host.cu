@@ -205,7 +205,7 @@ int search_nodes(Ctx& C, std::vector<Node>& nodes, std::vector<int>& ids,
 int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const char* seqs,
                 const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
                 const int32_t* t_len, int32_t* scores, int32_t* status, char* ops,
-                const int64_t* ops_off, int32_t* ops_len, cudaStream_t st) {
+                const int64_t* ops_off, int32_t* ops_len, int32_t* end_info, cudaStream_t st) {
   if (!E->bi) {
     E->bi = new (std::nothrow) BiState();
     if (!E->bi) return WF2G_ERR_OOM_;
@@ -299,6 +299,11 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
   }
 
   std::vector<int32_t> r_score(n), r_status(n), r_len(n, 0);
+  // cigar->end_v/end_h: the sequence lengths when the score-only search
+  // completes (wavefront/wavefront_bialign.c:1248-1257), or when a full
+  // alignment's top level splits at a breakpoint (:1214-1220); a top level
+  // that went to the base case keeps the cleared end (:159-194)
+  std::vector<int32_t> r_end((size_t)3 * n, -1);
   if (C.verbose) {
     BI_CUDA(cudaStreamSynchronize(st));
     fprintf(stderr, "[wfa2gpu] BiWFA inputs + packing: %.3f ms\n", C.ms_since_mark());
@@ -322,6 +327,8 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
         r_score[i] = classic_score(cfg, C.h_plen[i], C.h_tlen[i],
                                    o.status == kBiOk ? o.score : o.reached);
         r_status[i] = kStCompleted;
+        r_end[3 * (size_t)i] = C.h_plen[i];
+        r_end[3 * (size_t)i + 1] = C.h_tlen[i];
       } else {
         r_score[i] = INT32_MIN;  // cigar_clear()
         r_status[i] = o.status == kBiMaxSteps ? kStMaxSteps : kStUnattainable;
@@ -509,6 +516,10 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
                          ? classic_score(cfg, C.h_plen[i], C.h_tlen[i], nodes[i].bp_score)
                          : last_score;
         r_len[i] = (int32_t)len;
+        if (nodes[i].kind == kSplit) {
+          r_end[3 * (size_t)i] = C.h_plen[i];
+          r_end[3 * (size_t)i + 1] = C.h_tlen[i];
+        }
       }
     }
 
@@ -544,16 +555,20 @@ int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const ch
     BI_CUDA(cudaStreamSynchronize(st));
     fprintf(stderr, "[wfa2gpu] assembly: %.3f ms\n", C.ms_since_mark());
   }
+  for (int i = 0; i < n; ++i) r_end[3 * (size_t)i + 2] = 0;
   if (on_device) {
     BI_CUDA(cudaMemcpyAsync(scores, r_score.data(), n4, cudaMemcpyHostToDevice, st));
     BI_CUDA(cudaMemcpyAsync(status, r_status.data(), n4, cudaMemcpyHostToDevice, st));
     if (cigar) BI_CUDA(cudaMemcpyAsync(ops_len, r_len.data(), n4, cudaMemcpyHostToDevice, st));
+    if (end_info)
+      BI_CUDA(cudaMemcpyAsync(end_info, r_end.data(), 3 * n4, cudaMemcpyHostToDevice, st));
     BI_CUDA(cudaStreamSynchronize(st));
   } else {
     BI_CUDA(cudaStreamSynchronize(st));
     memcpy(scores, r_score.data(), n4);
     memcpy(status, r_status.data(), n4);
     if (cigar) memcpy(ops_len, r_len.data(), n4);
+    if (end_info) memcpy(end_info, r_end.data(), 3 * n4);
   }
   return WF2G_OK_;
 }

@@ -359,7 +359,7 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
 
   if (cfg->ultralow)
     return bialign_run(E, *cfg, n, on_device, seqs, p_off, p_len, t_off, t_len, scores, status,
-                       ops, ops_off, ops_len, st);
+                       ops, ops_off, ops_len, end_info, st);
   if (on_device) {
     return plan_and_run(E, *cfg, n, seqs, p_off, p_len, t_off, t_len, max_len, scores, status,
                         ops, ops_off, ops_len, nullptr, nullptr, 0, end_info, st);

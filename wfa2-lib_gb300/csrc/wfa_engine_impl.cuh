@@ -139,11 +139,12 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
                  const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st);
 
-// BiWFA batch (wfa_bialign_host.cu); synchronises `st`.
+// BiWFA batch (wfa_bialign_host.cu); synchronises `st`.  end_info (may be
+// null): per pair cigar->end_v, cigar->end_h and 0.
 int bialign_run(Engine* E, const wf2g_cfg_t& cfg, int n, int on_device, const char* seqs,
                 const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
                 const int32_t* t_len, int32_t* scores, int32_t* status, char* ops,
-                const int64_t* ops_off, int32_t* ops_len, cudaStream_t st);
+                const int64_t* ops_off, int32_t* ops_len, int32_t* end_info, cudaStream_t st);
 
 }  // namespace eng
 }  // namespace wf2g
