@@ -1431,8 +1431,9 @@ int oracle_align_batch_flags(const int* cfg, int num_pairs, const char* sequence
   const int ultralow = (cfg[7] == 3);
   /* BiWFA has no ends-free or extension form (wavefront/wavefront_align.c:67-82) */
   if (ultralow && p.endsfree) return -1;
-  /* BiWFA is restated with the wf-adaptive heuristic or none */
-  if (ultralow && (p.heur & ~HS_WFADAPTIVE)) return -1;
+  /* BiWFA is restated with every heuristic but z-drop (whose drop inside a
+   * breakpoint search is not restated) */
+  if (ultralow && (p.heur & HS_ZDROP)) return -1;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel num_threads(nthreads)

@@ -203,6 +203,16 @@ HEURISTIC_SETS = {
                                _h(XD, xdrop=80, steps_between_cutoffs=1)),
     "w6_affine2p_badapt_full": (6, 60, "affine2p", False, 0, 0, None,
                                 _h(BA, min_k=-25, max_k=25, steps_between_cutoffs=2)),
+    # BiWFA (ultralow memory, the optional ninth field): the breakpoint
+    # searches take the heuristic, the base cases do not
+    # (wavefront/wavefront_bialigner.c:52-71)
+    "w1_affine_biwfa_bstatic": (1, 60, "affine", False, 0, 0, None,
+                                _h(BS, min_k=-30, max_k=30), 3),
+    "w1_affine2p_biwfa_xdrop": (1, 60, "affine2p", False, 0, 0, None,
+                                _h(XD, xdrop=80, steps_between_cutoffs=1), 3),
+    "w1_affine_p4_biwfa_wfmash_score": (1, 60, "affine.p4", True, 0, 0, None,
+                                        _h(WM, min_wavefront_length=10, max_distance_threshold=50,
+                                           steps_between_cutoffs=1), 3),
 }
 
 
@@ -302,23 +312,26 @@ def heuristics_fixtures():
     O.build(ref=True)
     W.build()
     heur = {}
-    for name, (wl, n, pset, so, param, param2, form, hspec) in HEURISTIC_SETS.items():
+    for name, spec in HEURISTIC_SETS.items():
+        wl, n, pset, so, param, param2, form, hspec = spec[:8]
+        mm = spec[8] if len(spec) > 8 else 0
         m, mi, mm_, o1, e1, o2, e2 = {**PENALTY_SETS, **EXTRA_SETS}[pset]
         pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
                           gap_opening2=o2, gap_extension2=e2)
         h = heuristic_of(hspec)
         p = W.generate(wl, n, param=param, param2=param2)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-        a = O.align(b, pen, score_only=so, kind="port", form=form, heuristic=h)
+        a = O.align(b, pen, score_only=so, kind="port", form=form, heuristic=h, memory_mode=mm)
         keep = [i for i in range(n) if not (a.flags[i] & O.FLAG_OVER_BOUND)
                 and not (m <= 1 and a.status[i] == 1)]
         sub = O.PairBatch.from_lists([b.pattern(i) for i in keep], [b.text(i) for i in keep])
-        r = O.align(sub, pen, score_only=so, kind="reference_scalar", form=form, heuristic=h)
+        r = O.align(sub, pen, score_only=so, kind="reference_scalar", form=form, heuristic=h,
+                    memory_mode=mm)
         rows = [[int(r.score[j]), int(r.status[j]), crc(r.cigar(j)), int(r.end[j][0]),
                  int(r.end[j][1])] for j in range(sub.n)]
         heur[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
                       "penalties": pset, "score_only": so, "form": form, "heuristic": hspec,
-                      "keep": keep, "rows": rows}
+                      "memory_mode": mm, "keep": keep, "rows": rows}
         print(name, "done", len(keep), "of", n)
     with open(os.path.join(HERE, "heuristics_expected.json"), "w") as f:
         json.dump(heur, f, separators=(",", ":"))

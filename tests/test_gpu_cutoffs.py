@@ -32,8 +32,10 @@ def _spec(name):
                 gap_opening2=o2, gap_extension2=e2)
 
 
-def _served(metric, score_only, strategy):
+def _served(metric, score_only, strategy, memory_mode=0):
     """The GPU's refusals (make_cfg in wfa2-lib_gb300/csrc/wfa_aligner.c)."""
+    if memory_mode == 3 and strategy & ~0x04:  # BiWFA: wf-adaptive or none
+        return False
     return not (strategy & 0x20 and (not score_only or metric == 4))
 
 
@@ -42,7 +44,7 @@ def _gpu(W, cfg, b):
     rc, scores, status, ops, ops_len, ops_off, end = al.align_batch_ends(
         b.seqs, b.p_off, b.p_len, b.t_off, b.t_len)
     al.close()
-    if not _served(cfg.metric, cfg.score_only, cfg.heuristic["strategy"]):
+    if not _served(cfg.metric, cfg.score_only, cfg.heuristic["strategy"], cfg.memory_mode):
         assert rc == -2  # WF2G_ERR_CONFIG: refused, no answer
         return None
     assert rc == 0
@@ -71,7 +73,8 @@ def test_heuristics_match_reference_fixtures(gpu_available, wfa, oracle_mod, nam
     b = helpers.heuristic_pairs(O, W, fx)
     ref = _oracle_flags(O, spec, b, fx["score_only"], fx["form"], fx["heuristic"])
     got = _gpu(W, W.Config(**spec, score_only=fx["score_only"], form=fx["form"],
-                           heuristic=fx["heuristic"]), b)
+                           heuristic=fx["heuristic"],
+                           memory_mode=fx.get("memory_mode", 0)), b)
     if got is None:
         return
     compared = 0

@@ -112,7 +112,7 @@ def test_oracle_matches_reference_heuristics(oracle_mod, wfa, name):
     pen = _pen(O, UT["penalty_sets"][fx["penalties"]])
     b = helpers.heuristic_pairs(O, W, fx)
     r = O.align(b, pen, score_only=fx["score_only"], form=fx["form"],
-                heuristic=O.Heuristic(**fx["heuristic"]))
+                heuristic=O.Heuristic(**fx["heuristic"]), memory_mode=fx.get("memory_mode", 0))
     assert len(fx["rows"]) == b.n
     for i, (score, status, c, ev, eh) in enumerate(fx["rows"]):
         got = (int(r.score[i]), int(r.status[i]), helpers.crc(r.cigar(i)), int(r.end[i][0]),
@@ -122,7 +122,7 @@ def test_oracle_matches_reference_heuristics(oracle_mod, wfa, name):
 
 def test_oracle_heuristic_rejections(oracle_mod, wfa):
     """Drops with edit/indel (the reference exits, wavefront/wavefront_align.c:
-    83-89) and BiWFA with heuristics other than wf-adaptive fail loudly."""
+    83-89) and BiWFA with z-drop fail loudly."""
     O, W = oracle_mod, wfa
     p = W.generate(1, 4, first=3)
     b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
@@ -132,7 +132,7 @@ def test_oracle_heuristic_rejections(oracle_mod, wfa):
                 O.align(b, O.Penalties(metric), heuristic=O.Heuristic(st, xdrop=10, zdrop=10))
     with pytest.raises(ValueError):
         O.align(b, O.Penalties(), memory_mode=O.MEM_ULTRALOW,
-                heuristic=O.Heuristic(O.HS_BANDED_STATIC, min_k=-5, max_k=5))
+                heuristic=O.Heuristic(O.HS_ZDROP, zdrop=50))
     O.align(b, O.Penalties(), memory_mode=O.MEM_ULTRALOW,
             heuristic=O.Heuristic(O.HS_WFADAPTIVE, 10, 50, 1))
 
