@@ -467,8 +467,53 @@ def main():
         d2h = n * 8 + ((n * 4 + int(ops_off[-1])) if cigar else 0)
         e2e = {"value": world * n * args.steps / e2e_s, "unit": "pairs/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-        # every result of the e2e path equals the device-resident path
-        assert np.array_equal(h_scores, d_scores.cpu().numpy())
+
+    # ------------------------------------------------------------ parity
+    # The timed batch's results, every pair: scores, statuses and CIGARs
+    # against the CPU checker, every CIGAR replayed and rescored
+    # (oracle/wfa_check.c).  The checker's run over the whole batch, with all
+    # host threads, is also the CPU baseline and gives the exact work units.
+    pen = O.Penalties(metric=args.metric)
+    g_scores, g_status = d_scores.cpu().numpy(), d_status.cpu().numpy()
+    g_ops = d_ops.cpu().numpy() if cigar else None
+    g_opslen = d_opslen.cpu().numpy() if cigar else None
+    full_check = args.config in (0, 1)
+    threads = os.cpu_count() or 1
+    parity, r_full, cpu_full_s = None, None, None
+    if full_check:
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        r_full = O.align(b, pen, memory_mode=args.memory, score_only=args.score_only,
+                         nthreads=threads)
+        cpu_full_s = time.perf_counter() - t0
+        parity = O.compare(b, pen, g_scores, g_status, g_ops, ops_off[:n], g_opslen, r_full,
+                           score_only=args.score_only, nthreads=threads)
+        if e2e is not None:
+            # the host-API results equal the device-resident ones, pair by pair
+            pe = O.compare(b, pen, h_scores, h_status, h_ops, ops_off[:n], h_opslen,
+                           O.AlignResult(g_scores, g_status, g_ops, ops_off[:n], g_opslen,
+                                         None, None),
+                           score_only=args.score_only, nthreads=threads)
+            parity["e2e_vs_device_mismatch"] = (pe["score_mismatch"] + pe["status_mismatch"] +
+                                                pe["cigar_mismatch"])
+        counts = [parity[k] for k in ("score_mismatch", "status_mismatch", "cigar_mismatch",
+                                      "cigar_invalid", "rescore_mismatch")]
+        counts.append(parity.get("e2e_vs_device_mismatch", 0))
+        if dist:
+            t = torch.tensor(counts + [n], dtype=torch.int64, device=dev)
+            dist.all_reduce(t)
+            counts, checked = t.tolist()[:-1], int(t.tolist()[-1])
+            parity.update(dict(zip(("score_mismatch", "status_mismatch", "cigar_mismatch",
+                                    "cigar_invalid", "rescore_mismatch"), counts[:5])))
+            parity["pairs_checked"] = checked
+        parity["checker"] = "oracle port (C restatement), all pairs of the timed batch"
+        if any(counts):
+            print(json.dumps({"parity_failed": parity}), flush=True)
+            raise SystemExit(f"parity failure: {parity}")
+    elif e2e is not None:
+        assert np.array_equal(h_scores, g_scores)
 
     if rank != 0:
         if dist:
@@ -496,12 +541,32 @@ def main():
     per_pair = k / per_pair_s
     assert np.array_equal(ps, d_scores[:k].cpu().numpy())
 
-    # CPU baseline (bounded sample) and work units (WFA cells, extend chars)
-    cpu_v, cpu_n, cpu_threads, r, sp, _ = cpu_sample(O, W, args, args.cpu_seconds, 0, "port")
-    # the bounded sample doubles as a parity spot-check of the timed results
-    if rank == 0 and first == 0:
-        m = min(cpu_n, n)
-        assert np.array_equal(r.score[:m], d_scores[:m].cpu().numpy())
+    # CPU baseline and work units (WFA cells, extend chars): the checker's run
+    # over the whole batch where it ran, else a bounded sample of the workload
+    if r_full is not None and world == 1:
+        r, cpu_n, cpu_threads = r_full, n, threads
+        cpu_v = n / cpu_full_s
+        cpu_desc = f"all {n} pairs of the timed batch, all host threads (also the parity check)"
+    else:
+        cpu_v, cpu_n, cpu_threads, r, sp, _ = cpu_sample(O, W, args, args.cpu_seconds, 0, "port")
+        cpu_desc = f"first {cpu_n} pairs of the workload, all host threads"
+        if r_full is not None:
+            r = r_full
+        # the bounded sample is a parity check of the timed results' first pairs
+        if parity is None and first == 0:
+            m = min(cpu_n, n)
+            sb = O.PairBatch(p.seqs, p.p_off[:m], p.p_len[:m], p.t_off[:m], p.t_len[:m])
+            ref = O.AlignResult(r.score[:m], r.status[:m], r.ops, r.ops_off[:m], r.ops_len[:m],
+                                None, None)
+            parity = O.compare(sb, pen, g_scores[:m], g_status[:m], g_ops, ops_off[:m],
+                               g_opslen[:m] if cigar else None, ref,
+                               score_only=args.score_only, nthreads=cpu_threads)
+            parity["checker"] = "oracle port (C restatement), the bounded CPU sample"
+            bad = sum(parity[k] for k in ("score_mismatch", "status_mismatch", "cigar_mismatch",
+                                          "cigar_invalid", "rescore_mismatch"))
+            if bad:
+                print(json.dumps({"parity_failed": parity}), flush=True)
+                raise SystemExit(f"parity failure: {parity}")
     cells_pp = float(r.cells.mean())
     ext_words_pp = float(np.ceil(r.ext / 32.0).mean())
     ops_pp = INT_OPS_PER_CELL[args.metric] * cells_pp + INT_OPS_PER_EXT_WORD * ext_words_pp
@@ -534,8 +599,9 @@ def main():
                              "frac": alg_bytes / step_s / 1e9 / hbm_peak,
                              "peak_basis": "MEASURED_PEAKS.json hbm_gbs (of measured)"}},
         "cpu_baseline": {"value": cpu_v, "unit": "pairs/s", "cores": cpu_threads, "kind": "port",
-                         "sample": f"first {cpu_n} pairs of the workload, all host threads"},
+                         "sample": cpu_desc},
         "e2e": e2e,
+        "parity": parity,
         "gpu_launches": launches,
         "clocks": clk,
         "per_pair_dropin": {"value": per_pair, "unit": "pairs/s",

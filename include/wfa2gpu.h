@@ -456,7 +456,8 @@ int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const in
  * GPU that loads the library holds until the process exits.  The caller passes
  * inputs and outputs in device memory of the CURRENT device, as for
  * wavefront_align_batch_device(), and the work is queued on `cuda_stream`
- * (NULL: the legacy default stream).
+ * (NULL: the legacy default stream).  The current device must be the one the
+ * aligner was created on, else the call returns WF2G_ERR_ARGS.
  *
  * Limits: memory mode ultralow (BiWFA) is not served (WF2G_ERR_CONFIG); every
  * pattern and text at most 2048 characters (max_sequence_length
@@ -467,6 +468,9 @@ int wavefront_align_batch_device(wavefront_aligner_t* const wf_aligner, const in
  *
  * The first call on a device looks up that device's address of the array
  * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is kept per CUDA context and looked up again when the current
+ * context changes (after cudaDeviceReset, for instance), so make the first
+ * call after such a reset before any stream capture too.
  * All calls share the array and it keeps the last call's contents (the work
  * queue head is cleared at the start of each call): calls whose GPU work
  * overlaps -- on different streams, or from different threads -- race on it

@@ -94,7 +94,8 @@ class Heuristic:
 
 def build(ref: bool = False) -> None:
     targets = ["oracle"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    extra = [f"WFA_REF={os.environ['WFA_REF']}"] if os.environ.get("WFA_REF") else []
+    subprocess.run(["make", "-s", "-C", HERE] + targets + extra, check=True)
 
 
 _LIBS = {}
@@ -117,6 +118,26 @@ def _lib(kind: str):
     fn.restype = ctypes.c_int
     _LIBS[kind] = fn
     return fn
+
+
+def reference_dir() -> str:
+    """The reference's source tree: $WFA_REF, else the location this
+    directory's Makefile builds the reference library from.  It exists only
+    where the reference sources are present (not on the GPU hosts)."""
+    env = os.environ.get("WFA_REF")
+    if env:
+        return env
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True,
+                             text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+    return out
+
+
+def have_reference_sources() -> bool:
+    d = reference_dir()
+    return bool(d) and os.path.isdir(os.path.join(d, "wavefront"))
 
 
 def have_reference() -> bool:
@@ -219,6 +240,41 @@ def align(batch: PairBatch, pen: Penalties, memory_mode=MEM_HIGH, score_only=Fal
     if rc != 0:
         raise ValueError("invalid configuration for the CPU checker")
     return AlignResult(score, status, ops, ops_off, ops_len, cells, ext, end, flags)
+
+
+def compare(batch: PairBatch, pen: Penalties, scores, status, ops, ops_off, ops_len,
+            ref: "AlignResult", score_only=False, nthreads=0) -> dict:
+    """Pair-by-pair comparison of results under test (scores, status and, in
+    full-CIGAR runs, ops/ops_off/ops_len) with the checker's `ref`, replaying
+    and rescoring every CIGAR under test (oracle/wfa_check.c).  Returns the
+    mismatch counts and the first differing pair (-1: none)."""
+    lib = ctypes.CDLL(PORT_LIB) if os.path.exists(PORT_LIB) else None
+    if lib is None:
+        build()
+        lib = ctypes.CDLL(PORT_LIB)
+    fn = lib.oracle_compare_batch
+    P = ctypes.c_void_p
+    fn.argtypes = [P, ctypes.c_int] + [P] * 15 + [ctypes.c_int, P]
+    fn.restype = ctypes.c_int
+    cfg = pen.cfg(score_only=score_only)
+    out = np.zeros(6, np.int64)
+
+    def ptr(a):
+        return None if a is None else np.ascontiguousarray(a).ctypes.data_as(P)
+    keep = [np.ascontiguousarray(x) for x in (scores, status)]
+    full = not score_only
+    a_ops = np.ascontiguousarray(ops) if full else None
+    a_off = np.ascontiguousarray(ops_off, dtype=np.int64) if full else None
+    a_len = np.ascontiguousarray(ops_len, dtype=np.int32) if full else None
+    fn(ptr(cfg), batch.n, ptr(batch.seqs), ptr(batch.p_off), ptr(batch.p_len), ptr(batch.t_off),
+       ptr(batch.t_len), ptr(keep[0]), ptr(keep[1]), ptr(a_ops), ptr(a_off), ptr(a_len),
+       ptr(ref.score), ptr(ref.status), ptr(ref.ops) if full else None,
+       ptr(ref.ops_off) if full else None, ptr(ref.ops_len) if full else None, int(nthreads),
+       ptr(out))
+    return {"pairs_checked": int(batch.n), "score_mismatch": int(out[0]),
+            "status_mismatch": int(out[1]), "cigar_mismatch": int(out[2]),
+            "cigar_invalid": int(out[3]), "rescore_mismatch": int(out[4]),
+            "first_bad_pair": int(out[5])}
 
 
 # ---------------------------------------------------------------- formats

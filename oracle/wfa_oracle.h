@@ -85,6 +85,21 @@ int oracle_align_batch_flags(
     char* out_ops, const int64_t* ops_off, int32_t* out_ops_len,
     int64_t* out_cells, int64_t* out_ext, int32_t* out_end, int32_t* out_flags, int nthreads);
 
+/* Compares batch a (the results under test) with batch b (the checker's)
+ * pair by pair, and replays and rescores every CIGAR of a whose status is 0
+ * (wfa_check.c).  a_ops/b_ops may both be NULL (score-only).  out[0..5]:
+ * score mismatches, status mismatches, CIGAR mismatches, CIGARs of a that do
+ * not align their pair, CIGARs of a whose rescored score differs from a's
+ * score, and the first differing pair (-1: none). */
+int oracle_compare_batch(const int* cfg, int num_pairs, const char* sequences,
+                         const int64_t* p_off, const int32_t* p_len,
+                         const int64_t* t_off, const int32_t* t_len,
+                         const int32_t* a_score, const int32_t* a_status, const char* a_ops,
+                         const int64_t* a_ops_off, const int32_t* a_ops_len,
+                         const int32_t* b_score, const int32_t* b_status, const char* b_ops,
+                         const int64_t* b_ops_off, const int32_t* b_ops_len, int nthreads,
+                         int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

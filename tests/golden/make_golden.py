@@ -233,7 +233,8 @@ def main():
         return heuristics_fixtures()
     if only == ["endsfree"]:
         return endsfree_fixtures()
-    ref = args[0] if args else "/root/reference"
+    from oracle import oracle as O
+    ref = args[0] if args else O.reference_dir()
     with open(os.path.join(ref, "tests", "wfa.utest.seq"), "rb") as f:
         raw = f.read()
     with open(os.path.join(HERE, "utest.seq.gz"), "wb") as fo:

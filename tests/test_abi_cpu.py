@@ -46,11 +46,11 @@ def test_attribute_defaults_match_reference(wfa):
     assert a.system.probe_interval_global == 3000 and a.system.min_offsets_per_thread == 500
 
 
-def test_attribute_layout_matches_reference(wfa, tmp_path):
+def test_attribute_layout_matches_reference(wfa, oracle_mod, tmp_path):
     """Field offsets of wavefront_aligner_attr_t equal the reference's (probe
     compiled against the reference headers where they exist)."""
-    ref = "/root/reference"
-    if not os.path.isdir(os.path.join(ref, "wavefront")):
+    ref = oracle_mod.reference_dir()
+    if not ref or not os.path.isdir(os.path.join(ref, "wavefront")):
         pytest.skip("reference headers not present on this host")
     fields = [f[0] for f in wfa.AlignerAttr._fields_]
     probe = tmp_path / "probe.c"

@@ -8,6 +8,7 @@
 import os
 import shutil
 import subprocess
+import sys
 
 import pytest
 
@@ -15,7 +16,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 INC = os.path.join(ROOT, "include")
 LIB = os.path.join(ROOT, "wfa2-lib_gb300", "lib")
-REF_CPP = "/root/reference/bindings/cpp"
+sys.path.insert(0, ROOT)
+from oracle import oracle as _oracle  # noqa: E402
+
+# the reference's C++ binding, where the reference sources are present
+REF_CPP = os.path.join(_oracle.reference_dir() or "/nonexistent", "bindings", "cpp")
 
 
 def _have_gxx():

@@ -56,18 +56,27 @@ def _host(o, ops_off, n, score_only):
     return scores, status, cig
 
 
+# (label, configuration keywords, generator workload): the exact gap-affine
+# default, gap-affine-2p and the wf-adaptive heuristic -- the kernel choices
+# this entry point serves.  Gap-affine-2p runs on 100 bp pairs: on 1 kbp pairs
+# its back-trace can pass the 512 KiB per warp (a documented OOM).
+CONFIGS = [("affine", {}, 1), ("affine2p", {"metric": 4}, 0),
+           ("wfadaptive", {"wfadaptive": (10, 50, 1)}, 1)]
+
+
 @pytest.mark.parametrize("score_only", [False, True])
-def test_noalloc_matches_batch_device_twice(score_only):
+@pytest.mark.parametrize("label,kw,workload", CONFIGS, ids=[c[0] for c in CONFIGS])
+def test_noalloc_matches_batch_device_twice(score_only, label, kw, workload):
     torch = pytest.importorskip("torch")
     import wfa2gpu as W
     W.build()
     assert torch.cuda.is_available(), "GPU test needs a CUDA device"
-    p = W.generate(1, 600, first=4242)
+    p = W.generate(workload, 600 if label == "affine" else 200, first=4242)
     assert p.max_len <= 2048
     n = p.n
     d, ops_off = _device_batch(torch, W, p)
     stream = torch.cuda.Stream()
-    al = W.Aligner(W.Config(score_only=score_only))
+    al = W.Aligner(W.Config(score_only=score_only, **kw))
 
     ref = _outputs(torch, n, int(ops_off[-1]))
     assert _run(al, False, n, d, ref, p.max_len, score_only, stream.cuda_stream) == 0
@@ -86,6 +95,42 @@ def test_noalloc_matches_batch_device_twice(score_only):
         if not score_only:
             bad = [i for i in range(n) if got[2][i] != exp[2][i]]
             assert not bad, f"CIGARs differ on call {call}: pairs {bad[:5]}"
+    al.close()
+
+
+def test_noalloc_backtrace_limit_reports_oom():
+    """A pair whose back-trace needs more than the 512 KiB per warp reports
+    WF_STATUS_OOM with no CIGAR; the other pairs of the batch are unaffected."""
+    torch = pytest.importorskip("torch")
+    import helpers
+    import wfa2gpu as W
+    W.build()
+    g = W.generate(1, 40, first=99)
+    pats = [g.pattern(i) for i in range(g.n)]
+    txts = [g.text(i) for i in range(g.n)]
+    rng = np.random.default_rng(7)
+    big = 20  # two unrelated 2 kbp sequences: millions of cells
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    pats.insert(big, rng.choice(acgt, 2000).tobytes())
+    txts.insert(big, rng.choice(acgt, 2000).tobytes())
+    seqs, po, pl, to, tl = helpers.pack(pats, txts)
+    p = W.Pairs(seqs, po, pl, to, tl)
+    n = len(pats)
+    d, ops_off = _device_batch(torch, W, p)
+    al = W.Aligner(W.Config())
+    ref = _outputs(torch, n, int(ops_off[-1]))
+    assert _run(al, False, n, d, ref, int(max(pl.max(), tl.max())), False, 0) == 0
+    out = _outputs(torch, n, int(ops_off[-1]))
+    assert _run(al, True, n, d, out, int(max(pl.max(), tl.max())), False, 0) == 0
+    torch.cuda.synchronize()
+    exp = _host(ref, ops_off, n, False)
+    got = _host(out, ops_off, n, False)
+    assert exp[1][big] == 0
+    assert got[1][big] == W.WF_STATUS_OOM and len(got[2][big]) == 0
+    others = [i for i in range(n) if i != big]
+    assert np.array_equal(got[0][others], exp[0][others])
+    assert np.array_equal(got[1][others], exp[1][others])
+    assert all(got[2][i] == exp[2][i] for i in others)
     al.close()
 
 

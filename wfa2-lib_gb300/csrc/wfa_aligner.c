@@ -574,7 +574,11 @@ int wavefront_align_batch_device_noalloc(wavefront_aligner_t* const wf_aligner,
                                          const int64_t* d_cigar_offsets, int32_t* d_cigar_lengths,
                                          void* cuda_stream) {
   if (!wf_aligner || num_pairs < 0) return WF2G_ERR_ARGS;
-  if (wf2g_engine_device() < 0) return WF2G_ERR_NO_GPU;
+  const int dev = wf2g_engine_device();
+  if (dev < 0) return WF2G_ERR_NO_GPU;
+  /* the call runs on the current device: it must be the aligner's */
+  if (wf_aligner->engine && wf2g_engine_owner_device(wf_aligner->engine) != dev)
+    return WF2G_ERR_ARGS;
   wf2g_cfg_t cfg;
   if (make_cfg(wf_aligner, &cfg) != 0) return WF2G_ERR_CONFIG;
   return wf2g_noalloc_align(&cfg, num_pairs, d_seqs, d_pattern_offsets, d_pattern_lengths,

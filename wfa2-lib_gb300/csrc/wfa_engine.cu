@@ -18,6 +18,9 @@
 //             WF_STATUS_OOM.
 // Score-only runs have no back-trace: pass 2 takes the non-ACGT pairs with
 // 8-bit sequences and is the last.
+// Before them, in the library's headline form (gap-affine, exact, end-to-end),
+// the shared-memory fast pass (wfa_fast.cu) runs over the whole batch; pass 1
+// then takes only the pairs it left in its retry list.
 // Each warp owns a global-memory slice holding its wavefront ring (every
 // diagonal the pair can reach, so rows never wrap) and back-trace bytes; the
 // slices stay L1/L2 resident.  On GB300 this measured 2x faster than a ring in
@@ -91,13 +94,17 @@ extern "C" void wf2g_engine_free(void* engine) {
   cudaSetDevice(E->device);
   DevBuf* bufs[] = {&E->seqs,   &E->poff,     &E->plen,  &E->toff,     &E->tlen,
                     &E->scores, &E->status,   &E->ops,   &E->opsoff,   &E->opslen,
-                    &E->counters, &E->retry,  &E->scratch1, &E->scratch2,
+                    &E->counters, &E->retry,  &E->scratch0, &E->scratch1, &E->scratch2,
                     &E->pool,   &E->poolctl,  &E->endinfo};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   bi_state_free(E->bi);
   if (E->stream) cudaStreamDestroy(E->stream);
   delete E;
+}
+
+extern "C" int wf2g_engine_owner_device(const void* engine) {
+  return engine ? ((const Engine*)engine)->device : -1;
 }
 
 extern "C" int64_t wf2g_engine_launches(const void* engine) {
@@ -192,6 +199,111 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   return 0;
 }
 
+// Upper bound of the batch's sequence lengths for the fast pass: offsets stay
+// int16 with room for NULL drift, and its staged sequences stay small.
+constexpr int kFastMaxLen = 4096;
+
+static int gcd_int(int a, int b) {
+  while (b) {
+    const int r = a % b;
+    a = b;
+    b = r;
+  }
+  return a;
+}
+
+// Whether the fast pass serves this configuration.
+static bool fast_eligible(const wf2g_cfg_t& cfg, int max_len, const int8_t* d_cb,
+                          const int8_t* d_ce, int score_cap) {
+  return env_int("WF2G_FAST", 1) != 0 && cfg.metric == 3 && cfg.heur == 0 && !cfg.endsfree &&
+         !cfg.extension && !cfg.ultralow && d_cb == nullptr && d_ce == nullptr && score_cap == 0 &&
+         max_len <= kFastMaxLen && cfg.x > 0 && cfg.o1 > 0 && cfg.e1 > 0;
+}
+
+// The fast pass over pairs [0, n): one pair per CTA of G threads, rows of W
+// diagonals in shared memory; pairs it leaves go to `retry` (count at
+// `retry_count`).
+static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
+                         const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
+                         const int32_t* d_tlen, int max_len, int32_t* d_scores,
+                         int32_t* d_status, char* d_ops, const int64_t* d_opsoff,
+                         int32_t* d_opslen, int32_t* d_end_info, int32_t* queue,
+                         int32_t* retry, int32_t* retry_count, cudaStream_t st) {
+  const bool cigar = !cfg.score_only;
+  const int G = env_int("WF2G_FAST_G", 64) == 32 ? 32 : 64;
+  int W = env_int("WF2G_FAST_W", 1024) >= 2048 ? 2048 : 1024;
+  if (G == 32) W = 1024;
+  void* fn = wf2g_fast_kernel_ptr(cigar, G, W);
+  if (!fn) return WF2G_ERR_CUDA_;
+  FastParams fp;
+  memset(&fp, 0, sizeof(fp));
+  const int g = gcd_int(gcd_int(cfg.x, cfg.o1 + cfg.e1), cfg.e1);
+  fp.x = cfg.x / g;
+  fp.oe = (cfg.o1 + cfg.e1) / g;
+  fp.e = cfg.e1 / g;
+  fp.g = g;
+  fp.match = cfg.match;
+  fp.R = std::max(fp.x, fp.oe) + 1;
+  fp.RI = fp.e + 1;
+  fp.max_steps = cfg.max_steps;
+  fp.seqs = (const uint8_t*)d_seqs;
+  fp.p_off = d_poff;
+  fp.p_len = d_plen;
+  fp.t_off = d_toff;
+  fp.t_len = d_tlen;
+  fp.n_items = n;
+  fp.queue = queue;
+  fp.retry_items = retry;
+  fp.retry_count = retry_count;
+  fp.scores = d_scores;
+  fp.status = d_status;
+  fp.ops = (uint8_t*)d_ops;
+  fp.ops_off = d_opsoff;
+  fp.ops_len = d_opslen;
+  fp.end_info = d_end_info;
+  fp.max_len = max_len;
+  fp.nq = (max_len >> 4) + 2;
+  const int nrows = fp.R + 2 * fp.RI;
+  const int nw = G / 32;
+  auto al16 = [](int64_t b) { return (b + 15) & ~int64_t(15); };
+  int64_t off = 0;
+  fp.rows_off = 0;
+  off = al16((int64_t)nrows * W * 2);
+  fp.q_off = (int)off;
+  off = al16(off + (int64_t)2 * fp.nq * 8);
+  fp.meta_off = (int)off;
+  off = al16(off + (int64_t)nw * nrows * 8);
+  fp.red_off = (int)off;
+  off = al16(off + (int64_t)(2 * nw * 8 + 4) * 4);
+  const size_t smem = (size_t)off;
+  if (smem > E->smem_optin) return 1;  // rows do not fit: the general passes take all
+  fp.s_cap = W;
+  fp.pair_cap = cigar && E->bits_cap > 0 ? E->bits_cap : 0;
+  fp.items_off = cigar ? (int64_t)fp.s_cap * W : 0;
+  fp.items_cap = cigar ? 4 * (int64_t)max_len + 64 : 0;
+  fp.slice_bytes = cigar ? ((fp.items_off + fp.items_cap + 255) & ~int64_t(255)) : 0;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  int bps = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, G, smem);
+  if (bps < 1) return 1;
+  int blocks = std::min(bps * E->num_sms, std::max(n, 1));
+  const int64_t budget =
+      E->scratch_budget >= 0 ? E->scratch_budget : (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
+  if (cigar && (int64_t)blocks * fp.slice_bytes > budget)
+    blocks = (int)std::max<int64_t>(1, budget / fp.slice_bytes);
+  if (ensure(E->scratch0, cigar ? (size_t)blocks * fp.slice_bytes : 16)) return WF2G_ERR_OOM_;
+  fp.scratch = (uint8_t*)E->scratch0.p;
+  void* args[] = {(void*)&fp};
+  cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(G), args, smem, st);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "[wfa2gpu] kernel launch failed: %s\n", cudaGetErrorString(e));
+    return WF2G_ERR_CUDA_;
+  }
+  E->launches++;
+  return 0;
+}
+
 int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                  const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
@@ -200,12 +312,28 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   const bool cigar = !cfg.score_only;
   if (max_len < 1) max_len = 1;
   // counters: [0..3] work queues of passes 1-4, [4..6] retry counts of passes 1-3
-  // (retry lists: pass q writes list q-1, at retry + (q-1) * n)
-  if (ensure(E->counters, 8 * sizeof(int32_t)) || ensure(E->retry, (size_t)3 * n * sizeof(int32_t)))
+  // (retry lists: pass q writes list q-1, at retry + (q-1) * n), [8] work
+  // queue and [9] retry count of the fast pass (its list at retry + 3 * n)
+  if (ensure(E->counters, 16 * sizeof(int32_t)) || ensure(E->retry, (size_t)4 * n * sizeof(int32_t)))
     return WF2G_ERR_OOM_;
   int32_t* counters = (int32_t*)E->counters.p;
   int32_t* retry = (int32_t*)E->retry.p;
-  if (cudaMemsetAsync(counters, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return WF2G_ERR_CUDA_;
+  if (cudaMemsetAsync(counters, 0, 16 * sizeof(int32_t), st) != cudaSuccess) return WF2G_ERR_CUDA_;
+  bool fast = false;
+  if (fast_eligible(cfg, max_len, d_cb, d_ce, score_cap)) {
+    const int rc = run_fast_pass(E, cfg, n, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len,
+                                 d_scores, d_status, d_ops, d_opsoff, d_opslen, d_end_info,
+                                 counters + 8, retry + (size_t)3 * n, counters + 9, st);
+    if (rc < 0) return rc;
+    fast = (rc == 0);
+    if (fast && env_int("WF2G_VERBOSE", 0)) {
+      // diagnostics: how many pairs the fast pass left (synchronises the stream)
+      int32_t left = 0;
+      cudaMemcpyAsync(&left, counters + 9, sizeof(left), cudaMemcpyDeviceToHost, st);
+      cudaStreamSynchronize(st);
+      fprintf(stderr, "[wfa2gpu] fast pass: %d of %d pairs left to the general kernel\n", left, n);
+    }
+  }
 
   KParams base;
   memset(&base, 0, sizeof(base));
@@ -256,9 +384,9 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   // pass 1: every pair, 2-bit sequences, 1 MB of back-trace bytes per warp;
   // pairs with non-ACGT bytes or a longer back-trace go to the next pass
   KParams k = base;
-  k.items = nullptr;
-  k.num_items_dev = nullptr;
-  k.n_items = n;
+  k.items = fast ? retry + (size_t)3 * n : nullptr;
+  k.num_items_dev = fast ? counters + 9 : nullptr;
+  k.n_items = fast ? 0 : n;
   k.queue = counters + 0;
   k.retry_items = retry;
   k.retry_count = counters + 4;

@@ -59,6 +59,8 @@ int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int num_pairs, const char* d_seqs,
                        const int32_t* d_t_len, int max_len, int32_t* d_scores, int32_t* d_status,
                        char* d_ops, const int64_t* d_ops_off, int32_t* d_ops_len, void* stream);
 int wf2g_engine_device(void);
+/* The device an engine was created on. */
+int wf2g_engine_owner_device(const void* engine);
 
 /* Serving loop (wfa_server.cu); the result type is wavefront_server_result_t
  * of include/wfa2gpu.h, passed as void* to keep this header self-contained. */

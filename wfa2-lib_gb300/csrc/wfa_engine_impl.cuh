@@ -29,6 +29,7 @@ extern "C" void* wf2g_bi_pack_ptr(void);
 extern "C" void* wf2g_bi_gather_ptr(void);
 extern "C" size_t wf2g_bi_smem_bytes(int a2p, int scope);
 extern "C" void* wf2g_pool_init_ptr(void);
+extern "C" void* wf2g_fast_kernel_ptr(int cigar, int group, int width);
 
 namespace eng {
 
@@ -70,9 +71,9 @@ struct Engine {
   // batch buffers (host-input path)
   DevBuf seqs, poff, plen, toff, tlen, scores, status, ops, opsoff, opslen, endinfo;
   // control
-  DevBuf counters;  // [0] queue pass 1, [1] queue pass 2, [2] retry count
+  DevBuf counters;  // work-queue heads and retry counts of the passes (wfa_engine.cu)
   DevBuf retry;
-  DevBuf scratch1, scratch2;
+  DevBuf scratch0, scratch1, scratch2;  // fast pass, general pass 1, passes 2-4
   DevBuf pool, poolctl;  // back-trace block pool; [count, lock, ..., stack]
   BiState* bi = nullptr;
   // device-memory limits of this engine (bytes; < 0: the WF2G_SCRATCH_GB /

@@ -1,0 +1,513 @@
+// wfa_fast.cu -- the shared-memory kernel of the GB300 wavefront aligner for
+// the library's headline form: gap-affine, exact (no heuristic), end-to-end,
+// A/C/G/T sequences.  It runs first over a batch; a pair it cannot finish
+// (non-ACGT bytes, a wavefront wider than its shared-memory rows, a score
+// beyond its back-trace rows, a step limit, an unreachable end) goes to a
+// retry list that the general kernel (wfa_align.cuh) takes in full, so every
+// pair's result is the general kernel's result or this kernel's identical one.
+//
+// Semantics are the reference's exact unidirectional WFA
+// (wavefront/wavefront_unialign.c:242-273):
+//   compute  wavefront/wavefront_compute_affine.c:44-86 (unsigned bounds test
+//            on M only), limits wavefront/wavefront_compute.c:40-87, trimming
+//            of the row ends wavefront/wavefront_compute.c:579-613;
+//   extend   wavefront/wavefront_extend.c:86-121 (exact LCP per diagonal);
+//   end      wavefront/wavefront_termination.c:37-60 (M[s][tlen-plen] >= tlen);
+//   score    wavefront/wavefront_compute.c:108-120 (classic score);
+//   CIGAR    wavefront/wavefront_backtrace.c:320-529, reproduced from one
+//            choice byte per cell: M takes mismatch > deletion > insertion on
+//            ties, a gap takes extension over opening (:49-59).
+//
+// GPU design (differs from the general kernel where it pays):
+//   * Scores are divided by g = gcd(x, o+e, e).  Every wavefront at a score
+//     that is not a multiple of g is null in the reference (its inputs lie at
+//     scores that are not multiples of g either, down to score 0), so the
+//     scaled recurrence visits exactly the non-null wavefronts; with the
+//     default (4,6,2) it halves the steps.
+//   * One group of G threads per pair (a warp, or two warps with one CTA
+//     barrier per step), threads striped over diagonals.  The wavefront ring
+//     -- max(x,o+e)/g+1 M rows and e/g+1 I and D rows -- lives in shared
+//     memory as int16 offsets over W diagonals [-W/2, W/2), so every input of
+//     a step is one LDS away and no step waits on L2.  Rows are NULL outside
+//     their trimmed limits; the cell loop reads k-1, k, k+1 without checks.
+//   * Sequences are staged 2 bits per base as 64-bit word pairs (word i and
+//     i+1 at every i): a 16-base window is one LDS.64 and one funnel shift.
+//   * Choice bytes go to a per-group global slice at a fixed stride of W
+//     bytes per scaled score, so the back-trace reads them without a row table.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "wfa_kernels.cuh"
+
+namespace wf2g {
+
+// Longest common prefix of P[v..] and T[h..], at most lim bases (lim >= 0,
+// v+lim <= plen, h+lim <= tlen): 16-base windows, XOR + count leading zeros
+// (wavefront/wavefront_extend_kernels.c:68-92).  Q[i] = {word i+1, word i}.
+__device__ __forceinline__ int fast_lcp(const uint2* __restrict__ QP, const uint2* __restrict__ QT,
+                                        int v, int h, int lim) {
+  int L = 0;
+  while (L < lim) {
+    const int pv = v + L, ph = h + L;
+    const uint2 a = QP[pv >> 4];
+    const uint2 b = QT[ph >> 4];
+    const uint32_t d = __funnelshift_l(a.x, a.y, (uint32_t)pv << 1) ^
+                       __funnelshift_l(b.x, b.y, (uint32_t)ph << 1);
+    if (d) {
+      L += __clz(d) >> 1;
+      break;
+    }
+    L += 16;
+  }
+  return L < lim ? L : lim;
+}
+
+template <int G>
+__device__ __forceinline__ void fast_sync() {
+  if (G == 32) __syncwarp();
+  else __syncthreads();
+}
+
+// Stages one sequence as word pairs: base i at bits [31-2(i%16), 30-2(i%16)]
+// of word i/16, Q[i] = {word i+1, word i} for i < nq (words past the
+// sequence are 0).  Returns false (group-uniform) if a byte is not A/C/G/T.
+template <int G>
+__device__ bool fast_stage(const uint8_t* __restrict__ src, int len, uint2* Q, int nq, int t) {
+  const int lane = t & 31;
+  bool ok = true;
+  // 32 bases per warp pass -> words 2b and 2b+1; words up to index nq are needed
+  const int nblk = (nq >> 1) + 1;
+  for (int b = t >> 5; b < nblk; b += G / 32) {
+    const int i = (b << 5) + lane;
+    uint32_t code = 0;
+    if (i < len) {
+      const uint8_t c = src[i];
+      ok &= (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
+      code = (c >> 1) & 3u;  // A0 C1 T2 G3: a bijection on ACGT
+    }
+    const int sh = 30 - 2 * (lane & 15);
+    const uint32_t w0 = __reduce_or_sync(kFull, lane < 16 ? code << sh : 0u);
+    const uint32_t w1 = __reduce_or_sync(kFull, lane >= 16 ? code << sh : 0u);
+    const int i0 = 2 * b, i1 = 2 * b + 1;
+    // word j goes to Q[j].y and Q[j-1].x
+    if (lane == 0) {
+      if (i0 < nq) Q[i0].y = w0;
+      if (i0 >= 1 && i0 - 1 < nq) Q[i0 - 1].x = w0;
+    } else if (lane == 1) {
+      if (i1 < nq) Q[i1].y = w1;
+      if (i1 - 1 < nq) Q[i1 - 1].x = w1;
+    }
+  }
+  if (G == 32) return __all_sync(kFull, ok);
+  return __syncthreads_and(ok);
+}
+
+// The fast kernel.  CIGAR: full alignment (choice bytes, back-trace, replay)
+// or score only.  G: threads per pair (32 or 64), one pair per CTA.  W:
+// diagonals per shared-memory row.
+template <bool CIGAR, int G, int W>
+__global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
+  static_assert(G == 32 || G == 64, "a warp or two warps per pair");
+  static_assert(W / G <= 32, "per-thread cell masks hold at most 32 cells per step");
+  constexpr int NW = G / 32;
+  constexpr int HALF = W / 2;
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int t = threadIdx.x;
+  const int lane = t & 31;
+  const int wig = t >> 5;
+  const int nrows = p.R + 2 * p.RI;
+  int16_t* const rows = reinterpret_cast<int16_t*>(smem + p.rows_off);
+  uint2* const QP = reinterpret_cast<uint2*>(smem + p.q_off);
+  uint2* const QT = QP + p.nq;
+  // per-warp copy of every row's trimmed limits (lo > hi: empty), so a warp
+  // writes its own copy after each step without a CTA barrier
+  int2* const meta = reinterpret_cast<int2*>(smem + p.meta_off) + wig * nrows;
+  // G == 64: per-warp partial reductions, double-buffered by step parity,
+  // and a broadcast slot
+  int32_t* const red = reinterpret_cast<int32_t*>(smem + p.red_off);
+  uint8_t* const slice = p.scratch + (int64_t)blockIdx.x * p.slice_bytes;
+  uint8_t* const items = slice + p.items_off;
+  const int rowI = p.R, rowD = p.R + p.RI;
+  auto row = [&](int r) -> int16_t* { return rows + r * W + HALF; };
+
+  // all rows NULL (two int16 NULLs per 32-bit word)
+  {
+    uint32_t* const r32 = reinterpret_cast<uint32_t*>(rows);
+    for (int i = t; i < nrows * W / 2; i += G) r32[i] = 0x80008000u;
+  }
+  // diagonals the previous pair touched in every row (cleared before the next)
+  int used_lo = 0, used_hi = -1;
+
+  while (true) {
+    // ---------------------------------------------------------- next pair
+    int item = 0;
+    if (G == 32) {
+      if (t == 0) item = atomicAdd(p.queue, 1);
+      item = __shfl_sync(kFull, item, 0);
+    } else {
+      if (t == 0) red[2 * NW * 8] = atomicAdd(p.queue, 1);
+      __syncthreads();
+      item = red[2 * NW * 8];
+    }
+    if (item >= p.n_items) break;
+    const int pair = item;
+    const int plen = p.p_len[pair];
+    const int tlen = p.t_len[pair];
+    auto punt = [&]() {
+      if (t == 0) p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
+    };
+
+    // ---------------------------------------------------------- reset
+    if (used_lo <= used_hi) {
+      // word-aligned span of the touched diagonals, in every row
+      const int a = (used_lo + HALF) >> 1, b = (used_hi + HALF) >> 1;
+      const int span = b - a + 1;
+      uint32_t* const r32 = reinterpret_cast<uint32_t*>(rows);
+      for (int i = t; i < nrows * span; i += G) {
+        const int r = i / span, j = i - r * span;
+        r32[r * (W / 2) + a + j] = 0x80008000u;
+      }
+    }
+    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
+    used_lo = 0;
+    used_hi = 0;
+    // (a sequence over the bound is not staged past nq words: it is punted below)
+    bool ok = fast_stage<G>(p.seqs + p.p_off[pair], min(plen, p.max_len), QP, p.nq, t);
+    ok &= fast_stage<G>(p.seqs + p.t_off[pair], min(tlen, p.max_len), QT, p.nq, t);
+    fast_sync<G>();
+    const int k_end = tlen - plen;
+    // longer than the batch's stated bound (the staged words would not hold
+    // it) or ending on a diagonal the rows do not hold: the general kernel
+    if (!ok || plen > p.max_len || tlen > p.max_len || k_end < 1 - HALF || k_end > HALF - 2) {
+      punt();
+      fast_sync<G>();
+      continue;
+    }
+
+    // ---------------------------------------------------------- score 0
+    // M[0][0] = 0, extended at once (wavefront/wavefront_aligner.c:311-382)
+    const int L0 = fast_lcp(QP, QT, 0, 0, min(plen, tlen));
+    if (t == 0) row(0)[0] = (int16_t)L0;
+    if (lane == 0) meta[0] = make_int2(0, 0);
+    fast_sync<G>();
+    int s = 0;            // scaled score of the last computed wavefront
+    int cM = 0, cI = 0;   // ring slots of score s
+    int null_steps = 0;
+    int result = 0;       // 1 done, -1 leave to the general kernel
+    bool done = (plen == tlen) && (L0 >= tlen);
+    int parity = 0;
+    int64_t bt_used = 0;  // choice bytes of the pair: the general kernel's measure
+
+    while (!done) {
+      // the reference computes score g*s+1 next and stops there at the step
+      // limit (wavefront/wavefront_unialign.c:102-107): the general kernel
+      // reports that
+      if ((int64_t)p.g * s + 1 >= (int64_t)p.max_steps || s + 1 >= p.s_cap) {
+        result = -1;
+        break;
+      }
+      ++s;
+      cM = (cM + 1 == p.R) ? 0 : cM + 1;
+      cI = (cI + 1 == p.RI) ? 0 : cI + 1;
+      const int sMx = cM - p.x < 0 ? cM - p.x + p.R : cM - p.x;
+      const int sMo = cM - p.oe < 0 ? cM - p.oe + p.R : cM - p.oe;
+      const int sIe = cI - p.e < 0 ? cI - p.e + p.RI : cI - p.e;
+      // input limits (wavefront/wavefront_compute.c:306-352; a score below 0
+      // is a null wavefront)
+      const int2 kEmpty = make_int2(1, 0);
+      const int2 eMx = s >= p.x ? meta[sMx] : kEmpty;
+      const int2 eMo = s >= p.oe ? meta[sMo] : kEmpty;
+      const int2 eI = s >= p.e ? meta[rowI + sIe] : kEmpty;
+      const int2 eD = s >= p.e ? meta[rowD + sIe] : kEmpty;
+      const bool vMx = eMx.x <= eMx.y, vMo = eMo.x <= eMo.y;
+      const bool vI = eI.x <= eI.y, vD = eD.x <= eD.y;
+      int16_t* const oM = row(cM);
+      int16_t* const oI = row(rowI + cI);
+      int16_t* const oD = row(rowD + cI);
+      const int2 oldM = meta[cM], oldI = meta[rowI + cI], oldD = meta[rowD + cI];
+      if (!(vMx | vMo | vI | vD)) {
+        // a null step (wavefront/wavefront_compute_affine.c:236-243): the
+        // slots taken over become empty and all-NULL
+        for (int k = oldM.x + t; k <= oldM.y; k += G) oM[k] = kNull16;
+        for (int k = oldI.x + t; k <= oldI.y; k += G) oI[k] = kNull16;
+        for (int k = oldD.x + t; k <= oldD.y; k += G) oD[k] = kNull16;
+        if (lane == 0) meta[cM] = meta[rowI + cI] = meta[rowD + cI] = kEmpty;
+        fast_sync<G>();
+        // more null steps than the scope: the end is unreachable
+        // (wavefront/wavefront_extend.c:95-101), left to the general kernel
+        if (++null_steps > p.R) {
+          result = -1;
+          break;
+        }
+        continue;
+      }
+      null_steps = 0;
+      // output range: union of the inputs' (wavefront/wavefront_compute.c:40-87)
+      int lo = INT_MAX, hi = INT_MIN;
+      if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
+      if (vMo) { lo = min(lo, eMo.x - 1); hi = max(hi, eMo.y + 1); }
+      if (vI) { lo = min(lo, eI.x + 1); hi = max(hi, eI.y + 1); }
+      if (vD) { lo = min(lo, eD.x - 1); hi = max(hi, eD.y - 1); }
+      if (lo < 1 - HALF || hi > HALF - 2) {  // wider than the rows
+        result = -1;
+        break;
+      }
+      used_lo = min(used_lo, lo);
+      used_hi = max(used_hi, hi);
+      bt_used += hi - lo + 1;
+      if (CIGAR && p.pair_cap > 0 && bt_used > p.pair_cap) {  // over the pair's budget
+        result = -1;
+        break;
+      }
+      // what the slots held outside [lo,hi] becomes NULL (disjoint from the
+      // cells written below, and no input row is an output row)
+      if (oldM.x <= oldM.y && (oldM.x < lo || oldM.y > hi)) {
+        for (int k = oldM.x + t; k <= min(oldM.y, lo - 1); k += G) oM[k] = kNull16;
+        for (int k = max(oldM.x, hi + 1) + t; k <= oldM.y; k += G) oM[k] = kNull16;
+      }
+      if (oldI.x <= oldI.y && (oldI.x < lo || oldI.y > hi)) {
+        for (int k = oldI.x + t; k <= min(oldI.y, lo - 1); k += G) oI[k] = kNull16;
+        for (int k = max(oldI.x, hi + 1) + t; k <= oldI.y; k += G) oI[k] = kNull16;
+      }
+      if (oldD.x <= oldD.y && (oldD.x < lo || oldD.y > hi)) {
+        for (int k = oldD.x + t; k <= min(oldD.y, lo - 1); k += G) oD[k] = kNull16;
+        for (int k = max(oldD.x, hi + 1) + t; k <= oldD.y; k += G) oD[k] = kNull16;
+      }
+
+      const int16_t* const rMx = row(sMx);
+      const int16_t* const rMo = row(sMo);
+      const int16_t* const rI = row(rowI + sIe);
+      const int16_t* const rD = row(rowD + sIe);
+      uint8_t* const brow = CIGAR ? slice + (int64_t)s * W + HALF : nullptr;
+
+      // ---------------------------------------------------- the cells
+      uint32_t mM = 0, mI = 0, mD = 0;  // bit j: cell lo+t+G*j in bounds
+      int k = lo + t;
+      int32_t n_mx = 0, n_mom = 0, n_mop = 0, n_ie = 0, n_de = 0;
+      if (k <= hi) {
+        n_mx = rMx[k]; n_mom = rMo[k - 1]; n_mop = rMo[k + 1]; n_ie = rI[k - 1]; n_de = rD[k + 1];
+      }
+      uint32_t bit = 1;
+      for (; k <= hi; k += G, bit <<= 1) {
+        const int32_t mx = n_mx, mom = n_mom, mop = n_mop, ie = n_ie, de = n_de;
+        const int kn = k + G;
+        if (kn <= hi) {
+          n_mx = rMx[kn]; n_mom = rMo[kn - 1]; n_mop = rMo[kn + 1]; n_ie = rI[kn - 1]; n_de = rD[kn + 1];
+        }
+        // wavefront/wavefront_compute_affine.c:66-84
+        const int32_t i1 = max(mom, ie) + 1;
+        const int32_t d1 = max(mop, de);
+        const int32_t mis = mx + 1;
+        const int32_t best = max(d1, max(mis, i1));
+        const int32_t v = best - k;
+        const bool okM = (uint32_t)best <= (uint32_t)tlen && (uint32_t)v <= (uint32_t)plen;
+        int32_t mext = kNull16;
+        if (okM) mext = best + fast_lcp(QP, QT, v, best, min(plen - v, tlen - best));
+        oM[k] = (int16_t)mext;
+        oI[k] = (int16_t)i1;
+        oD[k] = (int16_t)d1;
+        if (okM) mM |= bit;
+        if ((uint32_t)i1 <= (uint32_t)tlen) mI |= bit;
+        if ((uint32_t)(d1 - k) <= (uint32_t)plen) mD |= bit;
+        if (CIGAR) {
+          // source of M: mismatch > deletion > insertion; gaps: extend >= open
+          uint32_t c = (mis == best) ? 0u : (d1 == best ? 1u : 2u);
+          c |= (uint32_t)(ie >= mom) << 2;
+          c |= (uint32_t)(de >= mop) << 3;
+          brow[k] = (uint8_t)c;
+        }
+      }
+      __syncwarp();  // the warp's cell writes are visible to its lanes
+      // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
+      // 579-613): offsets lo + (G*j + t) reduced over the group
+      auto first_of = [&](uint32_t m) -> int { return m ? G * (__ffs(m) - 1) + t : INT_MAX; };
+      auto last_of = [&](uint32_t m) -> int { return m ? G * (31 - __clz(m)) + t : INT_MIN; };
+      int fM = __reduce_min_sync(kFull, first_of(mM));
+      int lM = __reduce_max_sync(kFull, last_of(mM));
+      int fI = __reduce_min_sync(kFull, first_of(mI));
+      int lI = __reduce_max_sync(kFull, last_of(mI));
+      int fD = __reduce_min_sync(kFull, first_of(mD));
+      int lD = __reduce_max_sync(kFull, last_of(mD));
+      if (G > 32) {
+        int32_t* const pr = red + (parity * NW + wig) * 8;
+        if (lane == 0) {
+          pr[0] = fM; pr[1] = lM; pr[2] = fI; pr[3] = lI; pr[4] = fD; pr[5] = lD;
+        }
+        __syncthreads();
+        const int32_t* const q = red + (parity * NW + (wig ^ 1)) * 8;
+        fM = min(fM, q[0]); lM = max(lM, q[1]);
+        fI = min(fI, q[2]); lI = max(lI, q[3]);
+        fD = min(fD, q[4]); lD = max(lD, q[5]);
+        parity ^= 1;
+      }
+      const int tloM = fM == INT_MAX ? 1 : lo + fM, thiM = fM == INT_MAX ? 0 : lo + lM;
+      const int tloI = fI == INT_MAX ? 1 : lo + fI, thiI = fI == INT_MAX ? 0 : lo + lI;
+      const int tloD = fD == INT_MAX ? 1 : lo + fD, thiD = fD == INT_MAX ? 0 : lo + lD;
+      // M cells out of bounds are stored NULL.  I and D keep their values;
+      // out-of-bounds ones at the trimmed ends become NULL as the reference's
+      // trim leaves them.  Each warp reads the ends itself (every cell is
+      // visible after the reduction) and decides alike, so the CTA barrier
+      // after a fill is group-uniform.
+      {
+        const int iL = fI == INT_MAX ? hi : tloI - 1, iR = fI == INT_MAX ? hi + 1 : thiI + 1;
+        const int dL = fD == INT_MAX ? hi : tloD - 1, dR = fD == INT_MAX ? hi + 1 : thiD + 1;
+        bool fill = false;
+        for (int kk = lo + lane; kk <= iL; kk += 32) fill |= oI[kk] >= 0;
+        for (int kk = iR + lane; kk <= hi; kk += 32) fill |= oI[kk] >= 0;
+        for (int kk = lo + lane; kk <= dL; kk += 32) fill |= oD[kk] >= 0;
+        for (int kk = dR + lane; kk <= hi; kk += 32) fill |= oD[kk] >= 0;
+        if (__any_sync(kFull, fill)) {
+          if (G > 32) __syncthreads();  // every warp has read before any writes
+          for (int kk = lo + t; kk <= iL; kk += G) oI[kk] = kNull16;
+          for (int kk = iR + t; kk <= hi; kk += G) oI[kk] = kNull16;
+          for (int kk = lo + t; kk <= dL; kk += G) oD[kk] = kNull16;
+          for (int kk = dR + t; kk <= hi; kk += G) oD[kk] = kNull16;
+          fast_sync<G>();
+        }
+      }
+      if (lane == 0) {
+        meta[cM] = make_int2(tloM, thiM);
+        meta[rowI + cI] = make_int2(tloI, thiI);
+        meta[rowD + cI] = make_int2(tloD, thiD);
+      }
+      // termination on M[s] at k_end (wavefront/wavefront_termination.c:37-60)
+      done = tloM <= k_end && k_end <= thiM && oM[k_end] >= tlen;
+      __syncwarp();
+    }
+
+    if (!done || result != 0) {
+      punt();
+      fast_sync<G>();
+      continue;
+    }
+    // classic score (wavefront/wavefront_compute.c:108-120) at WFA score g*s,
+    // in the reference's wrapping int arithmetic
+    const int S = p.g * s;
+    const int score = p.match == 0
+                          ? -S
+                          : (int)((uint32_t)(-p.match) * ((uint32_t)plen + (uint32_t)tlen) - (uint32_t)S) / 2;
+    if (!CIGAR) {
+      if (t == 0) {
+        p.scores[pair] = score;
+        p.status[pair] = kStCompleted;
+        if (p.end_info) {
+          p.end_info[3 * (int64_t)pair] = plen;
+          p.end_info[3 * (int64_t)pair + 1] = tlen;
+          p.end_info[3 * (int64_t)pair + 2] = S;
+        }
+      }
+      fast_sync<G>();
+      continue;
+    }
+
+    // ---------------------------------------------------------- back-trace
+    // Walk the choice bytes from (s, k_end) in M to (0, 0), recording the
+    // operations backwards with an 'E' at every M visit; then replay forwards
+    // re-extending each M visit with the same LCP.  The first warp works,
+    // every lane alike; lane 0 writes.
+    bool bad = false;
+    int64_t n = 0;
+    if (wig == 0) {
+      int ss = s, kk = k_end;
+      const uint8_t* const bt = slice + HALF;
+      while (true) {
+        // M state at (ss, kk)
+        if (n + 1 > p.items_cap) { bad = true; break; }
+        if (lane == 0) items[n] = 'E';
+        ++n;
+        if (ss == 0) {
+          bad = (kk != 0);
+          break;
+        }
+        if (ss < 0 || kk < -HALF || kk >= HALF) { bad = true; break; }
+        uint32_t c = bt[(int64_t)ss * W + kk];
+        const uint32_t src = c & 3u;
+        if (src == 0) {
+          if (n + 1 > p.items_cap) { bad = true; break; }
+          if (lane == 0) items[n] = 'X';
+          ++n;
+          ss -= p.x;
+          continue;
+        }
+        // a gap chain: deletions move to k+1, insertions to k-1; each cell's
+        // extend bit says whether its gap continues (score - e) or was opened
+        // from M (score - (o+e))
+        const bool del = (src == 1);
+        const uint32_t ebit = del ? 8u : 4u;
+        const uint8_t op = del ? 'D' : 'I';
+        while (true) {
+          if (n + 1 > p.items_cap) { bad = true; break; }
+          if (lane == 0) items[n] = op;
+          ++n;
+          kk += del ? 1 : -1;
+          if (!(c & ebit)) {
+            ss -= p.oe;
+            break;
+          }
+          ss -= p.e;
+          if (ss <= 0 || kk < -HALF || kk >= HALF) { bad = true; break; }
+          c = bt[(int64_t)ss * W + kk];
+        }
+        if (bad) break;
+      }
+      __syncwarp();
+      // forward replay
+      int out_n = 0, v = 0, h = 0;
+      uint8_t* const out = p.ops + p.ops_off[pair];
+      const int cap = plen + tlen;
+      for (int64_t base = n - 1; base >= 0 && !bad; base -= 32) {
+        const uint32_t mine = (base - lane >= 0) ? items[base - lane] : 0u;
+        const int cnt = base + 1 < 32 ? (int)base + 1 : 32;
+        for (int j = 0; j < cnt; ++j) {
+          const uint32_t it = __shfl_sync(kFull, mine, j);
+          if (it == 'E') {
+            const int L = fast_lcp(QP, QT, v, h, min(plen - v, tlen - h));
+            if (out_n + L > cap) { bad = true; break; }
+            for (int q = lane; q < L; q += 32) out[out_n + q] = 'M';
+            out_n += L;
+            v += L;
+            h += L;
+          } else {
+            if (it == 'X') { bad = (v >= plen) || (h >= tlen); ++v; ++h; }
+            else if (it == 'I') { bad = h >= tlen; ++h; }
+            else { bad = v >= plen; ++v; }
+            if (bad || out_n >= cap) { bad = true; break; }
+            if (lane == 0) out[out_n] = (uint8_t)it;
+            ++out_n;
+          }
+        }
+      }
+      if (v != plen || h != tlen) bad = true;
+      if (t == 0 && !bad) {
+        p.scores[pair] = score;
+        p.status[pair] = kStCompleted;
+        p.ops_len[pair] = out_n;
+        if (p.end_info) {
+          p.end_info[3 * (int64_t)pair] = plen;
+          p.end_info[3 * (int64_t)pair + 1] = tlen;
+          p.end_info[3 * (int64_t)pair + 2] = S;
+        }
+      }
+      if (bad) punt();
+    }
+    fast_sync<G>();
+  }
+}
+
+}  // namespace wf2g
+
+// Kernel of the fast pass for (full CIGAR?, threads per pair, row width).
+extern "C" void* wf2g_fast_kernel_ptr(int cigar, int group, int width) {
+  using namespace wf2g;
+  if (group == 32 && width == 1024)
+    return cigar ? (void*)wfa_fast_kernel<true, 32, 1024> : (void*)wfa_fast_kernel<false, 32, 1024>;
+  if (group == 64 && width == 1024)
+    return cigar ? (void*)wfa_fast_kernel<true, 64, 1024> : (void*)wfa_fast_kernel<false, 64, 1024>;
+  if (group == 64 && width == 2048)
+    return cigar ? (void*)wfa_fast_kernel<true, 64, 2048> : (void*)wfa_fast_kernel<false, 64, 2048>;
+  if (group == 32 && width == 512)
+    return cigar ? (void*)wfa_fast_kernel<true, 32, 512> : (void*)wfa_fast_kernel<false, 32, 512>;
+  return nullptr;
+}

@@ -137,4 +137,43 @@ struct KParams {
   int32_t* end_info;
 };
 
+// int16 NULL of the shared-memory rows (offsets stay below 32,000)
+constexpr int kNull16 = -32768;
+
+// Launch parameters of the shared-memory fast pass (wfa_fast.cu), filled by
+// the engine (wfa_engine.cu).
+struct FastParams {
+  int x, oe, e;   // penalties divided by g: mismatch, gap open+extend, gap extend
+  int g;          // gcd(x, o+e, e)
+  int match;      // the user's match (<= 0), for the classic score
+  int R, RI;      // ring depths: max(x, oe) + 1 M rows, e + 1 I and D rows
+  int max_steps;  // unscaled step limit (INT32_MAX: none)
+  const uint8_t* seqs;
+  const int64_t* p_off;
+  const int32_t* p_len;
+  const int64_t* t_off;
+  const int32_t* t_len;
+  int n_items;
+  int32_t* queue;        // work-queue head (zeroed before launch)
+  int32_t* retry_items;  // pairs left to the general kernel
+  int32_t* retry_count;
+  int32_t* scores;
+  int32_t* status;
+  uint8_t* ops;
+  const int64_t* ops_off;
+  int32_t* ops_len;
+  int32_t* end_info;  // optional {end_v, end_h, WFA score} per pair
+  int max_len;        // longest sequence of the batch (a longer pair is punted)
+  int nq;             // 64-bit word pairs staged per sequence
+  int rows_off, q_off, meta_off, red_off;  // byte offsets of the parts of a group's shared memory
+  uint8_t* scratch;     // per-group global slices
+  int64_t slice_bytes;  // [choice bytes: s_cap rows of W bytes][walk items]
+  int s_cap;            // scaled scores a slice holds
+  int64_t pair_cap;     // back-trace bytes one pair may use (0: no cap); a pair
+                        // over it is left to the general kernel, which reports
+                        // WF_STATUS_OOM for it
+  int64_t items_off;
+  int64_t items_cap;
+};
+
 }  // namespace wf2g

@@ -9,6 +9,7 @@
 // queue) carved out of one fixed array in device memory that is part of this
 // library image.  Every GPU that loads the library holds that array until the
 // process exits.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,10 +39,43 @@ static constexpr int kNoAllocMaxLen = 2048;
 static constexpr int64_t kNoAllocBitsPerWarp = int64_t(512) << 10;
 static constexpr int kMaxDevices = 64;
 
-// Host code cannot use the array's name as a device address: resolve it once
-// per device, with that device current.
+// Host code cannot use the array's name as a device address: resolve it with
+// cudaGetSymbolAddress, with the device current.  The address belongs to the
+// CUDA context that loaded the module: after cudaDeviceReset (or any reset of
+// the primary context) the module is loaded again and the array may move, so
+// the cached address is keyed by the context's unique id (cuCtxGetId) and
+// resolved again when that id changes.
 static std::mutex g_setup_mutex;
 static uint8_t* g_scratch_ptr[kMaxDevices];
+static unsigned long long g_scratch_ctx[kMaxDevices];
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+static PfnCtxGetCurrent g_ctx_get_current = nullptr;
+static PfnCtxGetId g_ctx_get_id = nullptr;
+static std::once_flag g_driver_once;
+
+// Unique id of the calling thread's current context: 0 on success, 1 when no
+// context is current yet, -1 when the driver entry points are unavailable.
+static int current_context_id(unsigned long long* id) {
+  std::call_once(g_driver_once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_ctx_get_id = (PfnCtxGetId)f;
+    cudaGetLastError();
+  });
+  if (!g_ctx_get_current || !g_ctx_get_id) return -1;
+  CUcontext c = nullptr;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS) return -1;
+  if (!c) return 1;
+  return g_ctx_get_id(c, id) == CUDA_SUCCESS ? 0 : -1;
+}
 
 static uint8_t* scratch_for_current_device(int* err) {
   int dev = -1;
@@ -51,19 +85,24 @@ static uint8_t* scratch_for_current_device(int* err) {
     return nullptr;
   }
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* ptr = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || ptr == nullptr) {
-      fprintf(stderr, "[wfa2gpu] no-alloc scratch: cudaGetSymbolAddress failed: %s\n",
-              cudaGetErrorString(e));
-      cudaGetLastError();
-      *err = -4;  // WF2G_ERR_CUDA
-      return nullptr;
-    }
-    g_scratch_ptr[dev] = (uint8_t*)ptr;
+  unsigned long long id = 0;
+  int have_id = current_context_id(&id);
+  if (have_id == 0 && g_scratch_ptr[dev] && g_scratch_ctx[dev] == id) return g_scratch_ptr[dev];
+  void* ptr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || ptr == nullptr) {
+    fprintf(stderr, "[wfa2gpu] no-alloc scratch: cudaGetSymbolAddress failed: %s\n",
+            cudaGetErrorString(e));
+    cudaGetLastError();
+    *err = -4;  // WF2G_ERR_CUDA
+    return nullptr;
   }
-  return g_scratch_ptr[dev];
+  // the lookup initialises the runtime's context if none was current
+  if (have_id == 1) have_id = current_context_id(&id);
+  // without a context id nothing is cached: the address is looked up per call
+  g_scratch_ptr[dev] = have_id == 0 ? (uint8_t*)ptr : nullptr;
+  g_scratch_ctx[dev] = id;
+  return (uint8_t*)ptr;
 }
 
 extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_seqs,
@@ -160,14 +199,18 @@ extern "C" int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int n, const char* d_se
   kp.queue = queue;
   kp.gscratch = base + 256;
   // calls share the array: clear the queue head left by the previous call
-  if (cudaMemsetAsync(queue, 0, sizeof(int32_t), st) != cudaSuccess) return -4;
+  if (cudaMemsetAsync(queue, 0, sizeof(int32_t), st) != cudaSuccess) {
+    cudaGetLastError();
+    return -4;
+  }
   void* fn = wf2g_kernel_ptr(cfg->metric == 4, cigar, 8, 2, cfg->heur, 0, 0, 0);
   void* args[] = {(void*)&kp};
   const cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(32 * wpc), args,
                                          (size_t)kp.smem_per_group * wpc, st);
   if (e != cudaSuccess) {
     fprintf(stderr, "[wfa2gpu] no-alloc launch failed: %s\n", cudaGetErrorString(e));
-    return -4;  // WF2G_ERR_CUDA
+    cudaGetLastError();  // the failure is reported here, not left pending for the caller
+    return -4;           // WF2G_ERR_CUDA
   }
   return 0;
 }
