@@ -52,12 +52,7 @@ extern "C" int wf2g_engine_device(void) {
   return d;
 }
 
-extern "C" void* wf2g_engine_new(int* err) {
-  const int dev = wf2g_engine_device();
-  if (dev < 0) {
-    if (err) *err = WF2G_ERR_NO_GPU_;
-    return nullptr;
-  }
+static Engine* create_engine(int dev, int* err) {
   Engine* E = new (std::nothrow) Engine();
   if (!E) {
     if (err) *err = WF2G_ERR_OOM_;
@@ -88,18 +83,30 @@ extern "C" void* wf2g_engine_new(int* err) {
   return E;
 }
 
+extern "C" void* wf2g_engine_new(int* err) {
+  const int dev = wf2g_engine_device();
+  if (dev < 0) {
+    if (err) *err = WF2G_ERR_NO_GPU_;
+    return nullptr;
+  }
+  return create_engine(dev, err);
+}
+
 extern "C" void wf2g_engine_free(void* engine) {
   Engine* E = (Engine*)engine;
   if (!E) return;
   cudaSetDevice(E->device);
   DevBuf* bufs[] = {&E->seqs,   &E->poff,     &E->plen,  &E->toff,     &E->tlen,
                     &E->scores, &E->status,   &E->ops,   &E->opsoff,   &E->opslen,
-                    &E->counters, &E->retry,  &E->scratch0, &E->scratch1, &E->scratch2,
+                    &E->counters, &E->retry,  &E->scratch0, &E->scratch0b, &E->scratch1,
+                    &E->scratch2, &E->dstage, &E->dout,
                     &E->pool,   &E->poolctl,  &E->endinfo};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
+  if (E->hstage) cudaFreeHost(E->hstage);
   bi_state_free(E->bi);
   if (E->stream) cudaStreamDestroy(E->stream);
+  if (E->twin) wf2g_engine_free(E->twin);
   delete E;
 }
 
@@ -158,9 +165,7 @@ static int run_pass(Engine* E, const wf2g_cfg_t& cfg, const KParams& base, const
   const int want_blocks = ps.wide ? 8 : std::max(1, 64 / wpc);
   int carve = (int)((smem * want_blocks * 100 + 228 * 1024 - 1) / (228 * 1024)) + 1;
   carve = std::max(1, std::min(carve, 100));
-  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
-  int bps = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, tpg * wpc, smem);
+  int bps = blocks_per_sm(E, fn, tpg * wpc, smem, carve);
   bps = std::max(1, std::min(bps, ps.max_blocks_per_sm));
   const int need = (n_upper + wpc - 1) / wpc;
   int blocks = std::min(bps * E->num_sms, std::max(need, 1));
@@ -220,19 +225,18 @@ static bool fast_eligible(const wf2g_cfg_t& cfg, int max_len, const int8_t* d_cb
          max_len <= kFastMaxLen && cfg.x > 0 && cfg.o1 > 0 && cfg.e1 > 0;
 }
 
-// The fast pass over pairs [0, n): one pair per CTA of G threads, rows of W
-// diagonals in shared memory; pairs it leaves go to `retry` (count at
-// `retry_count`).
-static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
+// A fast pass over pairs [0, n) (items == nullptr) or over the list `items`
+// (its length at num_items_dev, at most n): one pair per CTA of G threads,
+// rows of W diagonals in shared memory; pairs it leaves go to `retry` (count
+// at `retry_count`).  Returns 1 when the configuration does not fit.
+static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
+                         const int32_t* items, const int32_t* num_items_dev, const char* d_seqs,
                          const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                          const int32_t* d_tlen, int max_len, int32_t* d_scores,
                          int32_t* d_status, char* d_ops, const int64_t* d_opsoff,
                          int32_t* d_opslen, int32_t* d_end_info, int32_t* queue,
-                         int32_t* retry, int32_t* retry_count, cudaStream_t st) {
+                         int32_t* retry, int32_t* retry_count, DevBuf& scratch, cudaStream_t st) {
   const bool cigar = !cfg.score_only;
-  const int G = env_int("WF2G_FAST_G", 64) == 32 ? 32 : 64;
-  int W = env_int("WF2G_FAST_W", 1024) >= 2048 ? 2048 : 1024;
-  if (G == 32) W = 1024;
   void* fn = wf2g_fast_kernel_ptr(cigar, G, W);
   if (!fn) return WF2G_ERR_CUDA_;
   FastParams fp;
@@ -243,14 +247,18 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_
   fp.e = cfg.e1 / g;
   fp.g = g;
   fp.match = cfg.match;
-  fp.R = std::max(fp.x, fp.oe) + 1;
-  fp.RI = fp.e + 1;
+  // one warp per pair updates the rows in place (one slot fewer per ring)
+  const int inplace = (G == 32);
+  fp.R = std::max(fp.x, fp.oe) + 1 - inplace;
+  fp.RI = fp.e + 1 - inplace;
   fp.max_steps = cfg.max_steps;
   fp.seqs = (const uint8_t*)d_seqs;
   fp.p_off = d_poff;
   fp.p_len = d_plen;
   fp.t_off = d_toff;
   fp.t_len = d_tlen;
+  fp.items = items;
+  fp.num_items_dev = num_items_dev;
   fp.n_items = n;
   fp.queue = queue;
   fp.retry_items = retry;
@@ -274,26 +282,28 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_
   fp.meta_off = (int)off;
   off = al16(off + (int64_t)nw * nrows * 8);
   fp.red_off = (int)off;
-  off = al16(off + (int64_t)(2 * nw * 8 + 4) * 4);
+  // two step-parameter buffers, the per-warp partial reductions, a broadcast slot
+  off = al16(off + 256 + (int64_t)nw * 8 * 4 + 16);
   const size_t smem = (size_t)off;
   if (smem > E->smem_optin) return 1;  // rows do not fit: the general passes take all
   fp.s_cap = W;
   fp.pair_cap = cigar && E->bits_cap > 0 ? E->bits_cap : 0;
-  fp.items_off = cigar ? (int64_t)fp.s_cap * W : 0;
+  // per step: 4-bit choice codes in 32-bit words, 8 iterations of a thread
+  // per word, and the row's limits (4 bytes)
+  const int iters = (W + G - 1) / G;
+  const int64_t rw = (int64_t)((iters + 7) / 8) * G;
+  fp.items_off = cigar ? (int64_t)fp.s_cap * (rw * 4 + 4) : 0;
   fp.items_cap = cigar ? 4 * (int64_t)max_len + 64 : 0;
   fp.slice_bytes = cigar ? ((fp.items_off + fp.items_cap + 255) & ~int64_t(255)) : 0;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  int bps = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, G, smem);
+  const int bps = blocks_per_sm(E, fn, G, smem, 100);
   if (bps < 1) return 1;
   int blocks = std::min(bps * E->num_sms, std::max(n, 1));
   const int64_t budget =
       E->scratch_budget >= 0 ? E->scratch_budget : (int64_t)env_int("WF2G_SCRATCH_GB", 24) << 30;
   if (cigar && (int64_t)blocks * fp.slice_bytes > budget)
     blocks = (int)std::max<int64_t>(1, budget / fp.slice_bytes);
-  if (ensure(E->scratch0, cigar ? (size_t)blocks * fp.slice_bytes : 16)) return WF2G_ERR_OOM_;
-  fp.scratch = (uint8_t*)E->scratch0.p;
+  if (ensure(scratch, cigar ? (size_t)blocks * fp.slice_bytes : 16)) return WF2G_ERR_OOM_;
+  fp.scratch = (uint8_t*)scratch.p;
   void* args[] = {(void*)&fp};
   cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(G), args, smem, st);
   if (e != cudaSuccess) {
@@ -308,30 +318,55 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                  const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
                  char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
-                 const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st) {
+                 const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st,
+                 bool skip_empty) {
   const bool cigar = !cfg.score_only;
   if (max_len < 1) max_len = 1;
   // counters: [0..3] work queues of passes 1-4, [4..6] retry counts of passes 1-3
-  // (retry lists: pass q writes list q-1, at retry + (q-1) * n), [8] work
-  // queue and [9] retry count of the fast pass (its list at retry + 3 * n)
-  if (ensure(E->counters, 16 * sizeof(int32_t)) || ensure(E->retry, (size_t)4 * n * sizeof(int32_t)))
+  // (retry lists: pass q writes list q-1, at retry + (q-1) * n), [8]/[9] work
+  // queue and retry count of the first fast pass (its list at retry + 3 * n),
+  // [10]/[11] those of the second (its list at retry + 4 * n)
+  if (ensure(E->counters, 16 * sizeof(int32_t)) || ensure(E->retry, (size_t)5 * n * sizeof(int32_t)))
     return WF2G_ERR_OOM_;
   int32_t* counters = (int32_t*)E->counters.p;
   int32_t* retry = (int32_t*)E->retry.p;
   if (cudaMemsetAsync(counters, 0, 16 * sizeof(int32_t), st) != cudaSuccess) return WF2G_ERR_CUDA_;
   bool fast = false;
+  // what the fast passes leave: the list the general pass 1 takes
+  const int32_t* fast_left = retry + (size_t)3 * n;
+  const int32_t* fast_left_n = counters + 9;
   if (fast_eligible(cfg, max_len, d_cb, d_ce, score_cap)) {
-    const int rc = run_fast_pass(E, cfg, n, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len,
-                                 d_scores, d_status, d_ops, d_opsoff, d_opslen, d_end_info,
-                                 counters + 8, retry + (size_t)3 * n, counters + 9, st);
+    // the first pass: a warp per pair, rows of 1024 diagonals updated in
+    // place; the second, over what the first left: rows of 2048
+    int rc = run_fast_pass(E, cfg, 32, 1024, n, nullptr, nullptr, d_seqs, d_poff, d_plen, d_toff,
+                           d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff, d_opslen,
+                           d_end_info, counters + 8, retry + (size_t)3 * n, counters + 9,
+                           E->scratch0, st);
     if (rc < 0) return rc;
     fast = (rc == 0);
-    if (fast && env_int("WF2G_VERBOSE", 0)) {
-      // diagnostics: how many pairs the fast pass left (synchronises the stream)
+    if (fast && env_int("WF2G_FAST_WIDE", 1)) {
+      const int g2 = env_int("WF2G_FAST_WIDE_G", 64) >= 128 ? 128 : 64;
+      rc = run_fast_pass(E, cfg, g2, 2048, n, retry + (size_t)3 * n, counters + 9, d_seqs, d_poff,
+                         d_plen, d_toff, d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff,
+                         d_opslen, d_end_info, counters + 10, retry + (size_t)4 * n,
+                         counters + 11, E->scratch0b, st);
+      if (rc < 0) return rc;
+      if (rc == 0) {
+        fast_left = retry + (size_t)4 * n;
+        fast_left_n = counters + 11;
+      }
+    }
+    const bool verbose = env_int("WF2G_VERBOSE", 0) != 0;
+    if (fast && (skip_empty || verbose)) {
+      // how many pairs the fast passes left (waits for them)
       int32_t left = 0;
-      cudaMemcpyAsync(&left, counters + 9, sizeof(left), cudaMemcpyDeviceToHost, st);
-      cudaStreamSynchronize(st);
-      fprintf(stderr, "[wfa2gpu] fast pass: %d of %d pairs left to the general kernel\n", left, n);
+      if (cudaMemcpyAsync(&left, fast_left_n, sizeof(left), cudaMemcpyDeviceToHost, st) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return WF2G_ERR_CUDA_;
+      if (verbose)
+        fprintf(stderr, "[wfa2gpu] fast passes: %d of %d pairs left to the general kernel\n", left, n);
+      if (skip_empty && left == 0) return WF2G_OK_;
     }
   }
 
@@ -384,8 +419,8 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   // pass 1: every pair, 2-bit sequences, 1 MB of back-trace bytes per warp;
   // pairs with non-ACGT bytes or a longer back-trace go to the next pass
   KParams k = base;
-  k.items = fast ? retry + (size_t)3 * n : nullptr;
-  k.num_items_dev = fast ? counters + 9 : nullptr;
+  k.items = fast ? fast_left : nullptr;
+  k.num_items_dev = fast ? fast_left_n : nullptr;
   k.n_items = fast ? 0 : n;
   k.queue = counters + 0;
   k.retry_items = retry;
@@ -469,6 +504,180 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   return WF2G_OK_;
 }
 
+// ---------------------------------------------------------------- host batches
+// Small batches (the per-pair drop-in wavefront_align() is one pair): every
+// input goes to the GPU in one pinned staging copy and every output comes
+// back in one, and the general passes are skipped when the fast passes left
+// nothing.
+constexpr int kSmallBatch = 64;
+constexpr int64_t kSmallBytes = int64_t(4) << 20;
+
+static int ensure_hstage(Engine* E, size_t bytes) {
+  if (bytes <= E->hstage_cap) return 0;
+  if (E->hstage) cudaFreeHost(E->hstage);
+  E->hstage = nullptr;
+  E->hstage_cap = 0;
+  const size_t want = bytes + bytes / 4;
+  if (cudaHostAlloc(&E->hstage, want, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  E->hstage_cap = want;
+  return 0;
+}
+
+static size_t al16z(size_t b) { return (b + 15) & ~size_t(15); }
+
+static int host_small(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seqs,
+                      const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
+                      const int32_t* t_len, int32_t* scores, int32_t* status, char* ops,
+                      const int64_t* ops_off, int32_t* ops_len, int32_t* end_info,
+                      int64_t seq_end, int64_t ops_end, int mlen, cudaStream_t st) {
+  const bool cigar = !cfg.score_only;
+  const size_t n4 = (size_t)n * 4, n8 = (size_t)n * 8;
+  // inputs: [p_off][t_off][ops_off][p_len][t_len][sequences]
+  const size_t i_toff = n8, i_opsoff = 2 * n8, i_plen = 3 * n8, i_tlen = 3 * n8 + n4;
+  const size_t i_seqs = al16z(3 * n8 + 2 * n4);
+  const size_t in_bytes = al16z(i_seqs + (size_t)seq_end + 16);
+  // outputs: [scores][status][ops_len][end_info][operations]
+  const size_t o_status = n4, o_opslen = 2 * n4, o_end = 3 * n4, o_ops = al16z(6 * n4);
+  const size_t out_bytes = o_ops + (cigar ? (size_t)ops_end : 0) + 16;
+  if (ensure_hstage(E, in_bytes + out_bytes) || ensure(E->dstage, in_bytes) ||
+      ensure(E->dout, out_bytes))
+    return WF2G_ERR_OOM_;
+  uint8_t* const h = (uint8_t*)E->hstage;
+  memcpy(h, p_off, n8);
+  memcpy(h + i_toff, t_off, n8);
+  if (cigar) memcpy(h + i_opsoff, ops_off, n8);
+  memcpy(h + i_plen, p_len, n4);
+  memcpy(h + i_tlen, t_len, n4);
+  memcpy(h + i_seqs, seqs, (size_t)seq_end);
+  uint8_t* const d = (uint8_t*)E->dstage.p;
+  uint8_t* const q = (uint8_t*)E->dout.p;
+  if (cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return WF2G_ERR_CUDA_;
+  const int rc = plan_and_run(
+      E, cfg, n, (const char*)(d + i_seqs), (const int64_t*)d, (const int32_t*)(d + i_plen),
+      (const int64_t*)(d + i_toff), (const int32_t*)(d + i_tlen), mlen, (int32_t*)q,
+      (int32_t*)(q + o_status), cigar ? (char*)(q + o_ops) : nullptr,
+      cigar ? (const int64_t*)(d + i_opsoff) : nullptr, cigar ? (int32_t*)(q + o_opslen) : nullptr,
+      nullptr, nullptr, 0, end_info ? (int32_t*)(q + o_end) : nullptr, st, true);
+  if (rc) return rc;
+  uint8_t* const ho = h + in_bytes;
+  cudaError_t e = cudaMemcpyAsync(ho, q, out_bytes - 16, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "[wfa2gpu] CUDA error: %s\n", cudaGetErrorString(e));
+    return WF2G_ERR_CUDA_;
+  }
+  memcpy(scores, ho, n4);
+  memcpy(status, ho + o_status, n4);
+  if (end_info) memcpy(end_info, ho + o_end, 3 * n4);
+  if (cigar) {
+    memcpy(ops_len, ho + o_opslen, n4);
+    for (int i = 0; i < n; ++i)
+      if (ops_len[i] > 0) memcpy(ops + ops_off[i], ho + o_ops + ops_off[i], (size_t)ops_len[i]);
+  }
+  return WF2G_OK_;
+}
+
+// Large batches run in chunks of pairs on two streams (this engine's, and a
+// second engine's with its own scratch), so the copies of one chunk overlap
+// the kernels of the next.  Each chunk's copies move only its pairs' bytes;
+// the device arrays mirror the caller's layout, so offsets stay valid.
+static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seqs,
+                        const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
+                        const int32_t* t_len, int32_t* scores, int32_t* status, char* ops,
+                        const int64_t* ops_off, int32_t* ops_len, int32_t* end_info,
+                        int64_t seq_end, int64_t ops_end, bool ops_ordered, cudaStream_t st) {
+  const bool cigar = !cfg.score_only;
+  const size_t n4 = (size_t)n * 4, n8 = (size_t)n * 8;
+  if (ensure(E->seqs, (size_t)seq_end + 16) || ensure(E->poff, n8) || ensure(E->plen, n4) ||
+      ensure(E->toff, n8) || ensure(E->tlen, n4) || ensure(E->scores, n4) ||
+      ensure(E->status, n4))
+    return WF2G_ERR_OOM_;
+  if (cigar && (ensure(E->ops, (size_t)ops_end + 16) || ensure(E->opsoff, n8) || ensure(E->opslen, n4)))
+    return WF2G_ERR_OOM_;
+  if (end_info && ensure(E->endinfo, 3 * n4)) return WF2G_ERR_OOM_;
+  // chunks of at least 16k pairs, at most 8; one chunk when the CIGAR regions
+  // are not in pair order (the chunks' copies back could overlap)
+  const int64_t chunk = std::max<int64_t>(16384, ((int64_t)n + 7) / 8);
+  int nchunks = (int)(((int64_t)n + chunk - 1) / chunk);
+  if (cigar && !ops_ordered) nchunks = 1;
+  if (nchunks > 1 && !E->twin) {
+    int err = 0;
+    E->twin = create_engine(E->device, &err);
+    if (!E->twin) nchunks = 1;
+  }
+  if (E->twin) {
+    E->twin->scratch_budget = E->scratch_budget;
+    E->twin->pool_budget = E->pool_budget;
+    E->twin->bits_cap = E->bits_cap;
+  }
+  const int64_t twin0 = E->twin ? E->twin->launches : 0;
+  const int64_t per = ((int64_t)n + nchunks - 1) / nchunks;
+  uint8_t* const dseq = (uint8_t*)E->seqs.p;
+  for (int c = 0; c < nchunks; ++c) {
+    const int a = (int)(c * per), b = (int)std::min<int64_t>(n, (c + 1) * per);
+    if (a >= b) break;
+    Engine* const Ec = (c & 1) ? E->twin : E;
+    const cudaStream_t sc = (c & 1) ? E->twin->stream : st;
+    const int m = b - a;
+    int64_t smin = INT64_MAX, smax = 0;
+    int ml = 0;
+    for (int i = a; i < b; ++i) {
+      smin = std::min(smin, std::min(p_off[i], t_off[i]));
+      smax = std::max(smax, std::max(p_off[i] + p_len[i], t_off[i] + t_len[i]));
+      ml = std::max(ml, std::max(p_len[i], t_len[i]));
+    }
+    if (smin > smax) smin = smax;
+    const size_t m4 = (size_t)m * 4, m8 = (size_t)m * 8;
+    cudaError_t e = cudaSuccess;
+    if (smax > smin)
+      e = cudaMemcpyAsync(dseq + smin, seqs + smin, (size_t)(smax - smin), cudaMemcpyHostToDevice, sc);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->poff.p + a, p_off + a, m8, cudaMemcpyHostToDevice, sc);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int32_t*)E->plen.p + a, p_len + a, m4, cudaMemcpyHostToDevice, sc);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->toff.p + a, t_off + a, m8, cudaMemcpyHostToDevice, sc);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int32_t*)E->tlen.p + a, t_len + a, m4, cudaMemcpyHostToDevice, sc);
+    if (cigar && e == cudaSuccess)
+      e = cudaMemcpyAsync((int64_t*)E->opsoff.p + a, ops_off + a, m8, cudaMemcpyHostToDevice, sc);
+    if (e != cudaSuccess) return WF2G_ERR_CUDA_;
+    const int rc = plan_and_run(
+        Ec, cfg, m, (const char*)dseq, (const int64_t*)E->poff.p + a, (const int32_t*)E->plen.p + a,
+        (const int64_t*)E->toff.p + a, (const int32_t*)E->tlen.p + a, ml,
+        (int32_t*)E->scores.p + a, (int32_t*)E->status.p + a, cigar ? (char*)E->ops.p : nullptr,
+        cigar ? (const int64_t*)E->opsoff.p + a : nullptr,
+        cigar ? (int32_t*)E->opslen.p + a : nullptr, nullptr, nullptr, 0,
+        end_info ? (int32_t*)E->endinfo.p + 3 * (size_t)a : nullptr, sc);
+    if (rc) return rc;
+    e = cudaMemcpyAsync(scores + a, (int32_t*)E->scores.p + a, m4, cudaMemcpyDeviceToHost, sc);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(status + a, (int32_t*)E->status.p + a, m4, cudaMemcpyDeviceToHost, sc);
+    if (end_info && e == cudaSuccess)
+      e = cudaMemcpyAsync(end_info + 3 * (size_t)a, (int32_t*)E->endinfo.p + 3 * (size_t)a, 3 * m4,
+                          cudaMemcpyDeviceToHost, sc);
+    if (cigar && e == cudaSuccess) {
+      e = cudaMemcpyAsync(ops_len + a, (int32_t*)E->opslen.p + a, m4, cudaMemcpyDeviceToHost, sc);
+      // the chunk's CIGAR regions (the whole buffer when there is one chunk)
+      const int64_t omin = nchunks == 1 ? 0 : ops_off[a];
+      const int64_t omax =
+          nchunks == 1 ? ops_end : ops_off[b - 1] + (int64_t)p_len[b - 1] + t_len[b - 1];
+      if (e == cudaSuccess && omax > omin)
+        e = cudaMemcpyAsync(ops + omin, (char*)E->ops.p + omin, (size_t)(omax - omin),
+                            cudaMemcpyDeviceToHost, sc);
+    }
+    if (e != cudaSuccess) return WF2G_ERR_CUDA_;
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && nchunks > 1) e = cudaStreamSynchronize(E->twin->stream);
+  if (E->twin) E->launches += E->twin->launches - twin0;
+  if (e != cudaSuccess) {
+    fprintf(stderr, "[wfa2gpu] CUDA error: %s\n", cudaGetErrorString(e));
+    return WF2G_ERR_CUDA_;
+  }
+  return WF2G_OK_;
+}
+
 extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int on_device,
                                  const char* seqs, const int64_t* p_off, const int32_t* p_len,
                                  const int64_t* t_off, const int32_t* t_len, int max_len,
@@ -492,52 +701,26 @@ extern "C" int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int n, int
     return plan_and_run(E, *cfg, n, seqs, p_off, p_len, t_off, t_len, max_len, scores, status,
                         ops, ops_off, ops_len, nullptr, nullptr, 0, end_info, st);
   }
-  // ---- host path: stage inputs, run, copy results back
+  // ---- host path
   int64_t seq_end = 0, ops_end = 0;
   int mlen = 0;
+  bool ops_ordered = true;  // each pair's CIGAR region after the previous one's
   for (int i = 0; i < n; ++i) {
     if (p_len[i] < 0 || t_len[i] < 0) return WF2G_ERR_ARGS_;
     seq_end = std::max(seq_end, p_off[i] + p_len[i]);
     seq_end = std::max(seq_end, t_off[i] + t_len[i]);
     mlen = std::max(mlen, std::max(p_len[i], t_len[i]));
-    if (cigar) ops_end = std::max(ops_end, ops_off[i] + (int64_t)p_len[i] + t_len[i]);
+    if (cigar) {
+      ops_end = std::max(ops_end, ops_off[i] + (int64_t)p_len[i] + t_len[i]);
+      if (i > 0 && ops_off[i] < ops_off[i - 1] + (int64_t)p_len[i - 1] + t_len[i - 1])
+        ops_ordered = false;
+    }
   }
-  const size_t n4 = (size_t)n * 4, n8 = (size_t)n * 8;
-  if (ensure(E->seqs, (size_t)seq_end + 16) || ensure(E->poff, n8) || ensure(E->plen, n4) ||
-      ensure(E->toff, n8) || ensure(E->tlen, n4) || ensure(E->scores, n4) ||
-      ensure(E->status, n4))
-    return WF2G_ERR_OOM_;
-  if (cigar && (ensure(E->ops, (size_t)ops_end + 16) || ensure(E->opsoff, n8) || ensure(E->opslen, n4)))
-    return WF2G_ERR_OOM_;
-  if (end_info && ensure(E->endinfo, 3 * n4)) return WF2G_ERR_OOM_;
-  cudaError_t e = cudaSuccess;
-  e = cudaMemcpyAsync(E->seqs.p, seqs, (size_t)seq_end, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(E->poff.p, p_off, n8, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(E->plen.p, p_len, n4, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(E->toff.p, t_off, n8, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(E->tlen.p, t_len, n4, cudaMemcpyHostToDevice, st);
-  if (cigar && e == cudaSuccess) e = cudaMemcpyAsync(E->opsoff.p, ops_off, n8, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return WF2G_ERR_CUDA_;
-  int rc = plan_and_run(E, *cfg, n, (const char*)E->seqs.p, (const int64_t*)E->poff.p,
-                        (const int32_t*)E->plen.p, (const int64_t*)E->toff.p,
-                        (const int32_t*)E->tlen.p, mlen, (int32_t*)E->scores.p,
-                        (int32_t*)E->status.p, cigar ? (char*)E->ops.p : nullptr,
-                        cigar ? (const int64_t*)E->opsoff.p : nullptr,
-                        cigar ? (int32_t*)E->opslen.p : nullptr, nullptr, nullptr, 0,
-                        end_info ? (int32_t*)E->endinfo.p : nullptr, st);
-  if (rc) return rc;
-  e = cudaMemcpyAsync(scores, E->scores.p, n4, cudaMemcpyDeviceToHost, st);
-  if (end_info && e == cudaSuccess)
-    e = cudaMemcpyAsync(end_info, E->endinfo.p, 3 * n4, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(status, E->status.p, n4, cudaMemcpyDeviceToHost, st);
-  if (cigar && e == cudaSuccess) e = cudaMemcpyAsync(ops_len, E->opslen.p, n4, cudaMemcpyDeviceToHost, st);
-  if (cigar && e == cudaSuccess) e = cudaMemcpyAsync(ops, E->ops.p, (size_t)ops_end, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) {
-    fprintf(stderr, "[wfa2gpu] CUDA error: %s\n", cudaGetErrorString(e));
-    return WF2G_ERR_CUDA_;
-  }
-  return WF2G_OK_;
+  if (n <= kSmallBatch && seq_end <= kSmallBytes && ops_end <= kSmallBytes)
+    return host_small(E, *cfg, n, seqs, p_off, p_len, t_off, t_len, scores, status, ops, ops_off,
+                      ops_len, end_info, seq_end, ops_end, mlen, st);
+  return host_chunked(E, *cfg, n, seqs, p_off, p_len, t_off, t_len, scores, status, ops, ops_off,
+                      ops_len, end_info, seq_end, ops_end, ops_ordered, st);
 }
 
 }  // namespace eng

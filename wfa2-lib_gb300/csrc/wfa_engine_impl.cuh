@@ -62,6 +62,16 @@ inline void release(DevBuf& b) {
 struct BiState;  // BiWFA buffers (wfa_bialign_host.cu)
 void bi_state_free(BiState* b);
 
+// Occupancy of one kernel configuration, looked up once per engine (the
+// attribute calls and the occupancy query cost more than a launch).
+struct OccEntry {
+  const void* fn;
+  int block;
+  size_t smem;
+  int carve;
+  int bps;
+};
+
 struct Engine {
   int device = -1;
   int num_sms = 0;
@@ -73,7 +83,7 @@ struct Engine {
   // control
   DevBuf counters;  // work-queue heads and retry counts of the passes (wfa_engine.cu)
   DevBuf retry;
-  DevBuf scratch0, scratch1, scratch2;  // fast pass, general pass 1, passes 2-4
+  DevBuf scratch0, scratch0b, scratch1, scratch2;  // fast passes, general pass 1, passes 2-4
   DevBuf pool, poolctl;  // back-trace block pool; [count, lock, ..., stack]
   BiState* bi = nullptr;
   // device-memory limits of this engine (bytes; < 0: the WF2G_SCRATCH_GB /
@@ -84,7 +94,37 @@ struct Engine {
   int64_t bi_scratch_budget = -1;
   int64_t pool_budget = -1;  // back-trace block pool (< 0: WF2G_POOL_GB, default 32)
   int64_t bits_cap = 0;
+  OccEntry occ[48];
+  int n_occ = 0;
+  // host batches: pinned staging of small batches, and the second engine
+  // that runs every other chunk of a large batch on its own stream
+  void* hstage = nullptr;
+  size_t hstage_cap = 0;
+  DevBuf dstage, dout;
+  Engine* twin = nullptr;
 };
+
+// Blocks of `fn` per SM for `block` threads and `smem` dynamic shared memory
+// (carve >= 0: the preferred shared-memory carveout, set with it).
+inline int blocks_per_sm(Engine* E, const void* fn, int block, size_t smem, int carve) {
+  for (int i = 0; i < E->n_occ; ++i) {
+    const OccEntry& o = E->occ[i];
+    if (o.fn == fn && o.block == block && o.smem == smem && o.carve == carve) return o.bps;
+  }
+  // the opt-in maximum, not this size: the attribute is per function and
+  // process-wide, shared by every engine's launches
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_optin);
+  if (carve >= 0) cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, block, smem) != cudaSuccess) {
+    cudaGetLastError();
+    bps = 0;
+  }
+  if (E->n_occ < (int)(sizeof(E->occ) / sizeof(E->occ[0])))
+    E->occ[E->n_occ++] = OccEntry{fn, block, smem, carve, bps};
+  return bps;
+}
 
 inline int env_int(const char* name, int dflt) {
   const char* v = getenv(name);
@@ -134,11 +174,14 @@ inline int score_bound(const wf2g_cfg_t& c, int max_len) {
 // Unidirectional batch over device arrays (two passes; see wfa_engine.cu).
 // d_cb/d_ce: begin/end component per pair (nullptr: M).  score_cap > 0
 // replaces the score bound derived from max_len (back-trace table size).
+// skip_empty: after the fast passes, wait for them and skip the general
+// passes when they left no pair (small host batches, which wait anyway).
 int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
                  const int64_t* d_poff, const int32_t* d_plen, const int64_t* d_toff,
                  const int32_t* d_tlen, int max_len, int32_t* d_scores, int32_t* d_status,
                  char* d_ops, const int64_t* d_opsoff, int32_t* d_opslen, const int8_t* d_cb,
-                 const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st);
+                 const int8_t* d_ce, int score_cap, int32_t* d_end_info, cudaStream_t st,
+                 bool skip_empty = false);
 
 // BiWFA batch (wfa_bialign_host.cu); synchronises `st`.  end_info (may be
 // null): per pair cigar->end_v, cigar->end_h and 0.

@@ -153,9 +153,13 @@ struct FastParams {
   const int32_t* p_len;
   const int64_t* t_off;
   const int32_t* t_len;
+  // work list: items[i] is a pair index (items == nullptr: identity, n_items
+  // pairs); num_items_dev, if non-null, holds the list's length
+  const int32_t* items;
+  const int32_t* num_items_dev;
   int n_items;
   int32_t* queue;        // work-queue head (zeroed before launch)
-  int32_t* retry_items;  // pairs left to the general kernel
+  int32_t* retry_items;  // pairs left to the next pass
   int32_t* retry_count;
   int32_t* scores;
   int32_t* status;
@@ -167,7 +171,7 @@ struct FastParams {
   int nq;             // 64-bit word pairs staged per sequence
   int rows_off, q_off, meta_off, red_off;  // byte offsets of the parts of a group's shared memory
   uint8_t* scratch;     // per-group global slices
-  int64_t slice_bytes;  // [choice bytes: s_cap rows of W bytes][walk items]
+  int64_t slice_bytes;  // [choice codes: s_cap rows][row limits: s_cap][walk items]
   int s_cap;            // scaled scores a slice holds
   int64_t pair_cap;     // back-trace bytes one pair may use (0: no cap); a pair
                         // over it is left to the general kernel, which reports
