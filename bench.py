@@ -35,6 +35,11 @@ METRIC = "pairs/s bit-exact score+CIGAR, batched vs per-pair on 1 GB300; p50/p99
 INT_OPS_PER_CELL = {3: 20, 4: 25}  # int32 ops per WFA cell: gap-affine, gap-affine-2p
 INT_OPS_PER_EXT_WORD = 8   # per additional 32-base extend word
 MEM_HIGH, MEM_ULTRALOW = 0, 3
+# DRAM bytes (read + write) per pair of the dominant kernel, from one ncu
+# capture of a 20,000-pair launch of the first fast pass on the headline
+# workload (dram__bytes_read.sum + dram__bytes_write.sum = 0.1223 + 0.7793 GB;
+# profiles/wfa_fast_kernel_workload1.md), scaled to a launch by its pairs
+TRAFFIC_BYTES_PER_PAIR = {(1, False): 901.58e6 / 20000}
 
 # The benchmark configurations: workload of the seeded generator, pairs per
 # GPU, distance metric, memory mode, pairs of the per-pair drop-in sample and
@@ -69,6 +74,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="target wall time of the bounded CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serve-sweep", action="store_true",
+                    help="config 4: skip the latency-against-load sweep")
     ap.add_argument("--fixed", default="",
                     help="L:D -- instead of the config's pairs, pairs of fixed length L with "
                          "D per-mille uniform edits (generator workload 5; small profiling cases)")
@@ -284,10 +291,32 @@ def run_serving(args, rank, world, local):
         assert (st == 0).all(), f"{int((st != 0).sum())} requests failed"
     launches = srv.launches - l0
     clk = clocks.stop()
-    srv.close()
     wall = statistics.median(walls)
     value = n / wall
     L = np.concatenate(lats) / 1000.0
+    # Latency against load: the offered rate above is far beyond what the GPU
+    # completes, so its latencies are the queue's drain time.  Here Poisson
+    # streams at fractions of the completed rate just measured, each about
+    # six seconds long (at least 2,000 requests).
+    sweep = []
+    if not args.no_serve_sweep:
+        srng = np.random.default_rng(4321 + rank)
+        for frac in (0.25, 0.5, 0.8, 1.0):
+            rate = frac * value
+            m = int(min(n, max(2000, rate * 6.0)))
+            arr = np.ascontiguousarray(np.cumsum(srng.exponential(1e6 / rate, m)))
+            w = serve(m, arr)
+            assert (st[:m] == 0).all(), f"{int((st[:m] != 0).sum())} requests failed"
+            Lm = lat[:m] / 1000.0
+            sweep.append({"offered_fraction_of_capacity": frac, "offered_rate": rate,
+                          "requests": m, "completed_pairs_per_s": m / w,
+                          "latency_ms": {"p50": float(np.percentile(Lm, 50)),
+                                         "p99": float(np.percentile(Lm, 99)),
+                                         "max": float(Lm.max())}})
+        # the last sweep run overwrote the first m results: the parity check
+        # below needs the main run's, so serve the main stream once more
+        serve(n, arrivals)
+    srv.close()
     # offline batched form on the same pairs (host API, all pairs in one call)
     al = W.Aligner(cfg)
     al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
@@ -327,6 +356,9 @@ def run_serving(args, rank, world, local):
                     "latency_ms": {"p50": float(np.percentile(L, 50)),
                                    "p99": float(np.percentile(L, 99)),
                                    "max": float(L.max())},
+                    "note": "offered 200k pairs/s is beyond capacity: these latencies are "
+                            "queue drain; see sweep for latency at sustainable load",
+                    "sweep": sweep,
                     "biwfa_fallback_pairs": int(len(fb)),
                     "offline_batched_pairs_per_s": n / t_batch,
                     "lanes": 2, "hbm_budget_gb": 80},
@@ -567,6 +599,14 @@ def main():
             if bad:
                 print(json.dumps({"parity_failed": parity}), flush=True)
                 raise SystemExit(f"parity failure: {parity}")
+    unit_note = "WFA cells of the exact unidirectional reference (heuristic none)"
+    if args.memory == MEM_ULTRALOW:
+        # BiWFA's work is counted in the unidirectional unit, so its extra
+        # (forward, reverse and base-case) cells count against the fraction:
+        # the same sample, score-only, memory high, for the cell count only
+        ub = O.PairBatch(sp.seqs, sp.p_off, sp.p_len, sp.t_off, sp.t_len)
+        r = O.align(ub, pen, memory_mode=MEM_HIGH, score_only=True, nthreads=cpu_threads)
+        unit_note += " (BiWFA's own cells count as overhead)"
     cells_pp = float(r.cells.mean())
     ext_words_pp = float(np.ceil(r.ext / 32.0).mean())
     ops_pp = INT_OPS_PER_CELL[args.metric] * cells_pp + INT_OPS_PER_EXT_WORD * ext_words_pp
@@ -589,7 +629,13 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded SplitMix64 generator)", "config": workload_config(args),
         "roofline": {"bound": "int32", "achieved": achieved_tops, "peak": peak_tops,
-                     "unit": "Tops/s", "frac": achieved_tops / peak_tops, "traffic": None,
+                     "unit": "Tops/s", "frac": achieved_tops / peak_tops,
+                     "traffic": (TRAFFIC_BYTES_PER_PAIR[(args.config, args.score_only)] * n
+                                 if (args.config, args.score_only) in TRAFFIC_BYTES_PER_PAIR
+                                 and not args.fixed else None),
+                     "traffic_basis": "DRAM read+write bytes per launch of the first fast pass, "
+                                      "ncu capture of 20,000 pairs scaled by pairs",
+                     "unit": unit_note,
                      "units_per_launch": {"wfa_cells": n * cells_pp,
                                           "ops_per_cell": INT_OPS_PER_CELL[args.metric],
                                           "ext_words": n * ext_words_pp},

@@ -34,6 +34,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <ctime>
 
 #include "wfa_engine_impl.cuh"
 
@@ -345,7 +346,8 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
     if (rc < 0) return rc;
     fast = (rc == 0);
     if (fast && env_int("WF2G_FAST_WIDE", 1)) {
-      const int g2 = env_int("WF2G_FAST_WIDE_G", 64) >= 128 ? 128 : 64;
+      const int gw = env_int("WF2G_FAST_WIDE_G", 32);
+      const int g2 = gw <= 32 ? 32 : gw <= 64 ? 64 : 128;
       rc = run_fast_pass(E, cfg, g2, 2048, n, retry + (size_t)3 * n, counters + 9, d_seqs, d_poff,
                          d_plen, d_toff, d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff,
                          d_opslen, d_end_info, counters + 10, retry + (size_t)4 * n,
@@ -356,6 +358,8 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
         fast_left_n = counters + 11;
       }
     }
+    // (diagnostics: WF2G_VERBOSE=1 reads the count too, which waits for the
+    // fast passes before the general ones are queued)
     const bool verbose = env_int("WF2G_VERBOSE", 0) != 0;
     if (fast && (skip_empty || verbose)) {
       // how many pairs the fast passes left (waits for them)
@@ -528,6 +532,12 @@ static int ensure_hstage(Engine* E, size_t bytes) {
 
 static size_t al16z(size_t b) { return (b + 15) & ~size_t(15); }
 
+static double wall_s() {
+  timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 static int host_small(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seqs,
                       const int64_t* p_off, const int32_t* p_len, const int64_t* t_off,
                       const int32_t* t_len, int32_t* scores, int32_t* status, char* ops,
@@ -591,6 +601,7 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
                         const int64_t* ops_off, int32_t* ops_len, int32_t* end_info,
                         int64_t seq_end, int64_t ops_end, bool ops_ordered, cudaStream_t st) {
   const bool cigar = !cfg.score_only;
+  const double t_start = (env_int("WF2G_VERBOSE", 0) || env_int("WF2G_TIMING", 0)) ? wall_s() : 0.0;
   const size_t n4 = (size_t)n * 4, n8 = (size_t)n * 8;
   if (ensure(E->seqs, (size_t)seq_end + 16) || ensure(E->poff, n8) || ensure(E->plen, n4) ||
       ensure(E->toff, n8) || ensure(E->tlen, n4) || ensure(E->scores, n4) ||
@@ -601,7 +612,8 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
   if (end_info && ensure(E->endinfo, 3 * n4)) return WF2G_ERR_OOM_;
   // chunks of at least 16k pairs, at most 8; one chunk when the CIGAR regions
   // are not in pair order (the chunks' copies back could overlap)
-  const int64_t chunk = std::max<int64_t>(16384, ((int64_t)n + 7) / 8);
+  const int want_chunks = std::max(1, std::min(env_int("WF2G_CHUNKS", 8), 64));
+  const int64_t chunk = std::max<int64_t>(16384, ((int64_t)n + want_chunks - 1) / want_chunks);
   int nchunks = (int)(((int64_t)n + chunk - 1) / chunk);
   if (cigar && !ops_ordered) nchunks = 1;
   if (nchunks > 1 && !E->twin) {
@@ -617,6 +629,11 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
   const int64_t twin0 = E->twin ? E->twin->launches : 0;
   const int64_t per = ((int64_t)n + nchunks - 1) / nchunks;
   uint8_t* const dseq = (uint8_t*)E->seqs.p;
+  // diagnostics: WF2G_TIMING=1 times the first chunk's copies and kernels
+  const bool timing = env_int("WF2G_TIMING", 0) != 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (timing)
+    for (auto& x : ev) cudaEventCreate(&x);
   for (int c = 0; c < nchunks; ++c) {
     const int a = (int)(c * per), b = (int)std::min<int64_t>(n, (c + 1) * per);
     if (a >= b) break;
@@ -633,6 +650,7 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
     if (smin > smax) smin = smax;
     const size_t m4 = (size_t)m * 4, m8 = (size_t)m * 8;
     cudaError_t e = cudaSuccess;
+    if (timing && c == 0) cudaEventRecord(ev[0], sc);
     if (smax > smin)
       e = cudaMemcpyAsync(dseq + smin, seqs + smin, (size_t)(smax - smin), cudaMemcpyHostToDevice, sc);
     if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->poff.p + a, p_off + a, m8, cudaMemcpyHostToDevice, sc);
@@ -642,6 +660,7 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
     if (cigar && e == cudaSuccess)
       e = cudaMemcpyAsync((int64_t*)E->opsoff.p + a, ops_off + a, m8, cudaMemcpyHostToDevice, sc);
     if (e != cudaSuccess) return WF2G_ERR_CUDA_;
+    if (timing && c == 0) cudaEventRecord(ev[1], sc);
     const int rc = plan_and_run(
         Ec, cfg, m, (const char*)dseq, (const int64_t*)E->poff.p + a, (const int32_t*)E->plen.p + a,
         (const int64_t*)E->toff.p + a, (const int32_t*)E->tlen.p + a, ml,
@@ -650,6 +669,7 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
         cigar ? (int32_t*)E->opslen.p + a : nullptr, nullptr, nullptr, 0,
         end_info ? (int32_t*)E->endinfo.p + 3 * (size_t)a : nullptr, sc);
     if (rc) return rc;
+    if (timing && c == 0) cudaEventRecord(ev[2], sc);
     e = cudaMemcpyAsync(scores + a, (int32_t*)E->scores.p + a, m4, cudaMemcpyDeviceToHost, sc);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(status + a, (int32_t*)E->status.p + a, m4, cudaMemcpyDeviceToHost, sc);
@@ -666,11 +686,24 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
         e = cudaMemcpyAsync(ops + omin, (char*)E->ops.p + omin, (size_t)(omax - omin),
                             cudaMemcpyDeviceToHost, sc);
     }
+    if (timing && c == 0) cudaEventRecord(ev[3], sc);
     if (e != cudaSuccess) return WF2G_ERR_CUDA_;
   }
+  const double t_enq = (env_int("WF2G_VERBOSE", 0) || env_int("WF2G_TIMING", 0)) ? wall_s() : 0.0;
   cudaError_t e = cudaStreamSynchronize(st);
   if (e == cudaSuccess && nchunks > 1) e = cudaStreamSynchronize(E->twin->stream);
+  if (env_int("WF2G_VERBOSE", 0) || env_int("WF2G_TIMING", 0))
+    fprintf(stderr, "[wfa2gpu] host batch: %d chunks, enqueue %.1f ms, wait %.1f ms\n", nchunks,
+            1e3 * (t_enq - t_start), 1e3 * (wall_s() - t_enq));
   if (E->twin) E->launches += E->twin->launches - twin0;
+  if (timing) {
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&b, ev[1], ev[2]);
+    cudaEventElapsedTime(&c, ev[2], ev[3]);
+    fprintf(stderr, "[wfa2gpu] first chunk: copies in %.1f ms, kernels %.1f ms, copies out %.1f ms\n", a, b, c);
+    for (auto& x : ev) cudaEventDestroy(x);
+  }
   if (e != cudaSuccess) {
     fprintf(stderr, "[wfa2gpu] CUDA error: %s\n", cudaGetErrorString(e));
     return WF2G_ERR_CUDA_;

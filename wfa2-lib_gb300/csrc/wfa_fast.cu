@@ -41,6 +41,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <type_traits>
 
 #include "wfa_kernels.cuh"
 
@@ -129,7 +130,7 @@ static_assert(2 * sizeof(FastStep) <= 256, "the engine reserves 256 bytes for th
 template <bool CIGAR, int G, int W>
 __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
   static_assert(G == 32 || G == 64 || G == 128, "one to four warps per pair");
-  static_assert(W / G <= 32, "per-thread cell masks hold at most 32 cells per step");
+  static_assert(W / G <= 64, "per-thread cell masks hold at most 64 cells per step");
   // One warp per pair updates the rows in place: the M ring holds
   // max(x, o+e) rows and I and D e rows each (the engine sizes it so); a
   // step's output rows are the slots of its oldest inputs.
@@ -138,6 +139,8 @@ __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
   constexpr int HALF = W / 2;
   constexpr int J = (W + G - 1) / G;     // most iterations of a step
   constexpr int RW = ((J + 7) / 8) * G;  // 32-bit choice words per step (8 cells each)
+  // per-thread cell masks: bit j for the thread's cell of iteration j
+  typedef typename std::conditional<(J > 32), unsigned long long, uint32_t>::type Mask;
   extern __shared__ __align__(16) uint8_t smem[];
   const int t = threadIdx.x;
   const int lane = t & 31;
@@ -359,7 +362,7 @@ __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
       int16_t* const oI = rows + st.oI;
       int16_t* const oD = rows + st.oD;
       uint32_t* const crow = CIGAR ? codes + (int64_t)st.s * RW + t : nullptr;
-      uint32_t mM = 0, mI = 0, mD = 0;  // bit j: cell lo+t+G*j in bounds
+      Mask mM = 0, mI = 0, mD = 0;  // bit j: cell lo+t+G*j in bounds
       uint32_t acc = 0;                 // 4-bit choice codes of 8 iterations
       int32_t n_mx = 0, n_mom = 0, n_mop = 0, n_ie = 0, n_de = 0;
       if (lo + t <= hi) {
@@ -403,7 +406,7 @@ __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
         oM[k] = (int16_t)mext;
         oI[k] = (int16_t)i1;
         oD[k] = (int16_t)d1;
-        const uint32_t bit = 1u << j;
+        const Mask bit = Mask(1) << j;
         if (okM) mM |= bit;
         if ((uint32_t)i1 <= (uint32_t)tlen) mI |= bit;
         if ((uint32_t)(d1 - k) <= (uint32_t)plen) mD |= bit;
@@ -439,8 +442,14 @@ __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
       }
       // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
       // 579-613), as offsets G*j + t from lo
-      auto first_of = [&](uint32_t m) -> int { return m ? G * (__ffs(m) - 1) + t : INT_MAX; };
-      auto last_of = [&](uint32_t m) -> int { return m ? G * (31 - __clz(m)) + t : INT_MIN; };
+      auto first_of = [&](Mask m) -> int {
+        if (!m) return INT_MAX;
+        return G * (sizeof(Mask) == 8 ? __ffsll((long long)m) - 1 : __ffs((int)m) - 1) + t;
+      };
+      auto last_of = [&](Mask m) -> int {
+        if (!m) return INT_MIN;
+        return G * (sizeof(Mask) == 8 ? 63 - __clzll((long long)m) : 31 - __clz((int)m)) + t;
+      };
       int fM = __reduce_min_sync(kFull, first_of(mM));
       int lM = __reduce_max_sync(kFull, last_of(mM));
       int fI = __reduce_min_sync(kFull, first_of(mI));
@@ -552,48 +561,83 @@ __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
         };
         bool bad = false;
         int64_t n = 0;
-        int ss = s, kk = k_end;
-        while (true) {
-          // M state at (ss, kk)
-          if (n + 1 > p.items_cap) { bad = true; break; }
-          if (lane == 0) items[n] = 'E';
+        auto emit = [&](uint8_t op) -> bool {
+          if (n + 1 > p.items_cap) return false;
+          if (lane == 0) items[n] = op;
           ++n;
-          if (ss == 0) {
-            bad = (kk != 0);
+          return true;
+        };
+        // One cell of the walk: (ss, kk) entered in state st (0 M, 1 D, 2 I)
+        // with its code c.  Emits its operations and moves to the next cell,
+        // which is successor l of this one: 1 mismatch (ss-x, kk), 2 deletion
+        // extended (ss-e, kk+1), 3 deletion opened (ss-(o+e), kk+1), 4
+        // insertion extended (ss-e, kk-1), 5 insertion opened (ss-(o+e),
+        // kk-1).  Returns 0 (moved), 1 (reached score 0) or -1 (inconsistent).
+        auto resolve = [&](int& ss, int& kk, int& st, uint32_t c, bool cbad, int& l) -> int {
+          if (st == 0) {
+            if (!emit('E')) return -1;
+            if (ss == 0) return kk == 0 ? 1 : -1;
+            if (cbad) return -1;
+            const uint32_t src = c & 3u;
+            if (src == 0) {
+              if (!emit('X')) return -1;
+              ss -= p.x;
+              l = 1;
+              return ss >= 0 ? 0 : -1;
+            }
+            st = (src == 1) ? 1 : 2;  // a gap chain starts in this cell
+          } else if (cbad) {
+            return -1;
+          }
+          // a gap cell: deletions move to k+1, insertions to k-1; the extend
+          // bit says whether the gap continues (score - e) or was opened from
+          // M (score - (o+e))
+          const bool del = (st == 1);
+          if (!emit(del ? 'D' : 'I')) return -1;
+          kk += del ? 1 : -1;
+          if (c & (del ? 8u : 4u)) {
+            ss -= p.e;
+            l = del ? 2 : 4;
+            return ss > 0 ? 0 : -1;  // a gap cannot begin the alignment
+          }
+          ss -= p.oe;
+          st = 0;
+          l = del ? 3 : 5;
+          return ss >= 0 ? 0 : -1;
+        };
+        // Walk from (s, k_end) in M to (0, 0), two cells per round trip to
+        // memory: knowing the code of the cell being left, lanes 0-5 load the
+        // code of the next cell and of the five cells reachable from it;
+        // resolving the next cell then finds its successor's code loaded.
+        int ss = s, kk = k_end, st = 0;
+        bool cbad = false;
+        uint32_t c = ss > 0 ? code_at(ss, kk, cbad) : 0u;
+        while (true) {
+          int l = 0;
+          int r = resolve(ss, kk, st, c, cbad, l);
+          if (r != 0) {
+            bad = (r < 0);
             break;
           }
-          if (ss < 0) { bad = true; break; }
-          uint32_t c = code_at(ss, kk, bad);
-          if (bad) break;
-          const uint32_t src = c & 3u;
-          if (src == 0) {
-            if (n + 1 > p.items_cap) { bad = true; break; }
-            if (lane == 0) items[n] = 'X';
-            ++n;
-            ss -= p.x;
-            continue;
+          // the cell entered, (ss, kk), and its successors
+          int qs = ss, qk = kk;
+          if (lane == 1) { qs = ss - p.x; }
+          else if (lane == 2) { qs = ss - p.e; qk = kk + 1; }
+          else if (lane == 3) { qs = ss - p.oe; qk = kk + 1; }
+          else if (lane == 4) { qs = ss - p.e; qk = kk - 1; }
+          else if (lane == 5) { qs = ss - p.oe; qk = kk - 1; }
+          bool qbad = false;
+          uint32_t qc = 0u;
+          if (lane < 6 && qs > 0) qc = code_at(qs, qk, qbad);
+          c = __shfl_sync(kFull, qc, 0);
+          cbad = __shfl_sync(kFull, (int)qbad, 0) != 0;
+          r = resolve(ss, kk, st, c, cbad, l);
+          if (r != 0) {
+            bad = (r < 0);
+            break;
           }
-          // a gap chain: deletions move to k+1, insertions to k-1; each cell's
-          // extend bit says whether its gap continues (score - e) or was
-          // opened from M (score - (o+e))
-          const bool del = (src == 1);
-          const uint32_t ebit = del ? 8u : 4u;
-          const uint8_t op = del ? 'D' : 'I';
-          while (true) {
-            if (n + 1 > p.items_cap) { bad = true; break; }
-            if (lane == 0) items[n] = op;
-            ++n;
-            kk += del ? 1 : -1;
-            if (!(c & ebit)) {
-              ss -= p.oe;
-              break;
-            }
-            ss -= p.e;
-            if (ss <= 0) { bad = true; break; }
-            c = code_at(ss, kk, bad);
-            if (bad) break;
-          }
-          if (bad) break;
+          c = __shfl_sync(kFull, qc, l);
+          cbad = __shfl_sync(kFull, (int)qbad, l) != 0;
         }
         __syncwarp();
         // forward replay
@@ -657,6 +701,7 @@ extern "C" void* wf2g_fast_kernel_ptr(int cigar, int group, int width) {
   if (group == G && width == W) \
     return cigar ? (void*)wfa_fast_kernel<true, G, W> : (void*)wfa_fast_kernel<false, G, W>;
   WF2G_FAST_CASE(32, 1024)
+  WF2G_FAST_CASE(32, 2048)
   WF2G_FAST_CASE(64, 1024)
   WF2G_FAST_CASE(64, 2048)
   WF2G_FAST_CASE(128, 2048)
