@@ -573,6 +573,58 @@ def main():
     per_pair = k / per_pair_s
     assert np.array_equal(ps, d_scores[:k].cpu().numpy())
 
+    # Secondary lines of the headline run (cheap, same box, same process):
+    # the drop-in on the configuration the reference names for it (100 bp
+    # pairs), and the headline batch score-only (checked against the
+    # checker's scores of the full run).
+    secondary = {}
+    if args.config == 1 and not args.fixed and not args.score_only:
+        p0 = W.generate(0, 2000, first=0)
+        r0 = O.align(O.PairBatch(p0.seqs, p0.p_off, p0.p_len, p0.t_off, p0.t_len),
+                     O.Penalties(), nthreads=os.cpu_count() or 1)
+        k0 = p0.n
+        s0, t0s, l0s = (np.zeros(k0, np.int32) for _ in range(3))
+        pa0 = W.Aligner(cfg)
+        bl.wf2g_bench_per_pair(C.cast(pa0._h, P), 100, ptr(p0.seqs), ptr(p0.p_off), ptr(p0.p_len),
+                               ptr(p0.t_off), ptr(p0.t_len), ptr(s0), ptr(t0s), ptr(l0s))
+        w0 = bl.wf2g_bench_per_pair(C.cast(pa0._h, P), k0, ptr(p0.seqs), ptr(p0.p_off),
+                                    ptr(p0.p_len), ptr(p0.t_off), ptr(p0.t_len), ptr(s0), ptr(t0s),
+                                    ptr(l0s))
+        pa0.close()
+        assert np.array_equal(s0, r0.score) and (t0s == 0).all(), "config 0 drop-in parity"
+        secondary["config0_per_pair_dropin"] = {
+            "value": k0 / w0, "unit": "pairs/s",
+            "sample": f"{k0} wavefront_align() calls on 100 bp pairs (5 edits each), "
+                      "scores checked against the checker"}
+        so = W.Aligner(W.Config(metric=args.metric, score_only=True, memory_mode=args.memory))
+
+        def step_score_only():
+            rc = so.align_batch_device(n, d_seqs.data_ptr(), d_poff.data_ptr(), d_plen.data_ptr(),
+                                       d_toff.data_ptr(), d_tlen.data_ptr(), max_len,
+                                       d_scores.data_ptr(), d_status.data_ptr(), 0, 0, 0,
+                                       stream.cuda_stream)
+            if rc != 0:
+                raise RuntimeError(f"score-only batch failed: {rc}")
+        for _ in range(max(args.warmup, 3)):
+            step_score_only()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_score_only()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        so.close()
+        so_s = e0.elapsed_time(e1) / 1000.0
+        so_scores = d_scores.cpu().numpy()
+        so_ok = bool(r_full is not None and np.array_equal(so_scores, r_full.score) and
+                     (d_status.cpu().numpy() == 0).all())
+        assert so_ok, "score-only parity"
+        secondary["config1_score_only"] = {
+            "value": n * args.steps / so_s, "unit": "pairs/s", "ms_per_step": 1000 * so_s / args.steps,
+            "parity": f"all {n} scores equal the checker's"}
+
     # CPU baseline and work units (WFA cells, extend chars): the checker's run
     # over the whole batch where it ran, else a bounded sample of the workload
     if r_full is not None and world == 1:
@@ -635,7 +687,7 @@ def main():
                                  and not args.fixed else None),
                      "traffic_basis": "DRAM read+write bytes per launch of the first fast pass, "
                                       "ncu capture of 20,000 pairs scaled by pairs",
-                     "unit": unit_note,
+                     "work_unit": unit_note,
                      "units_per_launch": {"wfa_cells": n * cells_pp,
                                           "ops_per_cell": INT_OPS_PER_CELL[args.metric],
                                           "ext_words": n * ext_words_pp},
@@ -652,6 +704,7 @@ def main():
         "clocks": clk,
         "per_pair_dropin": {"value": per_pair, "unit": "pairs/s",
                             "sample": f"{k} wavefront_align() calls"},
+        "secondary": secondary,
         "batched_over_per_pair": value / world / per_pair,
         "cells_per_s": world * n * cells_pp * args.steps / dev_s,
         "dp_cell_updates_per_s": float(np.sum(p.p_len.astype(np.float64) * p.t_len)) * world *

@@ -338,15 +338,19 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   const int32_t* fast_left_n = counters + 9;
   if (fast_eligible(cfg, max_len, d_cb, d_ce, score_cap)) {
     // the first pass: a warp per pair, rows of 1024 diagonals updated in
-    // place; the second, over what the first left: rows of 2048
-    int rc = run_fast_pass(E, cfg, 32, 1024, n, nullptr, nullptr, d_seqs, d_poff, d_plen, d_toff,
+    // place; the second, over what the first left: rows of 2048.  A batch
+    // too small to fill the GPU (the drop-in's single pair) takes four warps
+    // per pair instead, which shortens each pair's steps.
+    const int small_n = env_int("WF2G_FAST_SMALL_N", 2 * E->num_sms);
+    const int g1 = n <= small_n ? 128 : 32;
+    int rc = run_fast_pass(E, cfg, g1, 1024, n, nullptr, nullptr, d_seqs, d_poff, d_plen, d_toff,
                            d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff, d_opslen,
                            d_end_info, counters + 8, retry + (size_t)3 * n, counters + 9,
                            E->scratch0, st);
     if (rc < 0) return rc;
     fast = (rc == 0);
     if (fast && env_int("WF2G_FAST_WIDE", 1)) {
-      const int gw = env_int("WF2G_FAST_WIDE_G", 32);
+      const int gw = n <= small_n ? 128 : env_int("WF2G_FAST_WIDE_G", 32);
       const int g2 = gw <= 32 ? 32 : gw <= 64 ? 64 : 128;
       rc = run_fast_pass(E, cfg, g2, 2048, n, retry + (size_t)3 * n, counters + 9, d_seqs, d_poff,
                          d_plen, d_toff, d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff,
@@ -701,7 +705,13 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
     cudaEventElapsedTime(&a, ev[0], ev[1]);
     cudaEventElapsedTime(&b, ev[1], ev[2]);
     cudaEventElapsedTime(&c, ev[2], ev[3]);
-    fprintf(stderr, "[wfa2gpu] first chunk: copies in %.1f ms, kernels %.1f ms, copies out %.1f ms\n", a, b, c);
+    cudaPointerAttributes pa, pb;
+    const int ta = cudaPointerGetAttributes(&pa, seqs) == cudaSuccess ? (int)pa.type : -1;
+    const int tb = (cigar && cudaPointerGetAttributes(&pb, ops) == cudaSuccess) ? (int)pb.type : -1;
+    cudaGetLastError();
+    fprintf(stderr,
+            "[wfa2gpu] first chunk: copies in %.1f ms, kernels %.1f ms, copies out %.1f ms "
+            "(memory type of sequences %d, of operations %d)\n", a, b, c, ta, tb);
     for (auto& x : ev) cudaEventDestroy(x);
   }
   if (e != cudaSuccess) {

@@ -704,6 +704,7 @@ extern "C" void* wf2g_fast_kernel_ptr(int cigar, int group, int width) {
   WF2G_FAST_CASE(32, 2048)
   WF2G_FAST_CASE(64, 1024)
   WF2G_FAST_CASE(64, 2048)
+  WF2G_FAST_CASE(128, 1024)
   WF2G_FAST_CASE(128, 2048)
 #undef WF2G_FAST_CASE
   return nullptr;
