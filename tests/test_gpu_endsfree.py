@@ -51,14 +51,6 @@ def test_endsfree_matches_reference_fixtures(gpu_available, wfa, name):
     p = W.generate(fx["workload"], fx["n"], param=fx["param"], param2=fx["param2"])
     cfg = W.Config(**_spec(fx["penalties"]), score_only=fx["score_only"], form=fx["form"],
                    wfadaptive=fx["wfadaptive"])
-    if cfg.match != 0 and fx["form"] != "extension" and (fx["form"][0] or fx["form"][2]):
-        # begin-free lengths with match < 0: pinned on the CPU, refused on the
-        # GPU until its kernel side is built
-        al = W.Aligner(cfg)
-        rc = al.align_batch_ends(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)[0]
-        al.close()
-        assert rc == -2  # WF2G_ERR_CONFIG
-        return
     got = _gpu(W, cfg, p)
     for i, (score, status, c, ev, eh) in enumerate(fx["rows"]):
         st, sc, cig, gv, gh = got[i]
@@ -81,8 +73,6 @@ def test_endsfree_matches_oracle(gpu_available, wfa, oracle_mod, case, spec_name
                                  score_only):
     W, O = wfa, oracle_mod
     spec = _spec(spec_name)
-    if spec["match"] != 0 and form != "extension" and (form[0] or form[2]):
-        pytest.skip("begin-free lengths with match < 0 are not served (rejection tested below)")
     wl, n, param, param2 = case
     p = W.generate(wl, n, first=1234, param=param, param2=param2)
     got = _gpu(W, W.Config(**spec, score_only=score_only, form=form), p)
@@ -132,12 +122,11 @@ def test_endsfree_dropin_cigar_fields(gpu_available, wfa, oracle_mod):
 
 def test_endsfree_rejections(gpu_available, wfa):
     """Forms the GPU path does not serve fail loudly: BiWFA with free ends (the
-    reference exits, wavefront/wavefront_align.c:67-82), begin-free lengths
-    with match < 0, and serving with free ends (its BiWFA fallback)."""
+    reference exits, wavefront/wavefront_align.c:67-82), and serving with free
+    ends (its BiWFA fallback)."""
     W = wfa
     p = W.generate(1, 4, first=3)
-    for cfg in [W.Config(form=(5, 5, 5, 5), memory_mode=W.MEM_ULTRALOW),
-                W.Config(match=-1, form=(5, 0, 0, 0))]:
+    for cfg in [W.Config(form=(5, 5, 5, 5), memory_mode=W.MEM_ULTRALOW)]:
         al = W.Aligner(cfg)
         rc = al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)[0]
         al.close()

@@ -358,9 +358,6 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
      * wavefront/wavefront_align.c:67-82) */
     if (cfg->ultralow) return -1;
     if (cfg->pbf < 0 || cfg->pef < 0 || cfg->tbf < 0 || cfg->tef < 0) return -1;
-    /* with match < 0 a begin-free run re-enters at every score that is a
-     * multiple of -match (wavefront/wavefront_compute.c:124-262): not computed */
-    if (!cfg->extension && p->match != 0 && (cfg->pbf > 0 || cfg->tbf > 0)) return -1;
     /* edit and indel never widen the score-0 wavefront's initialised window
      * (wavefront/wavefront_compute_edit.c:321-374), so their back-trace reads
      * begin-free diagonals as sourceless: not computed */

@@ -238,14 +238,17 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
                          int32_t* d_opslen, int32_t* d_end_info, int32_t* queue,
                          int32_t* retry, int32_t* retry_count, DevBuf& scratch, cudaStream_t st) {
   const bool cigar = !cfg.score_only;
-  void* fn = wf2g_fast_kernel_ptr(cigar, G, W);
-  if (!fn) return WF2G_ERR_CUDA_;
   FastParams fp;
   memset(&fp, 0, sizeof(fp));
   const int g = gcd_int(gcd_int(cfg.x, cfg.o1 + cfg.e1), cfg.e1);
   fp.x = cfg.x / g;
   fp.oe = (cfg.o1 + cfg.e1) / g;
   fp.e = cfg.e1 / g;
+  // a warp per pair takes two diagonals per lane when the scaled x is even
+  // and the scaled e odd (wfa_fast2.cu); else one cell per thread
+  const bool two = G == 32 && (fp.x & 1) == 0 && (fp.e & 1) == 1 && env_int("WF2G_FAST2", 1);
+  void* fn = two ? wf2g_fast2_kernel_ptr(cigar, (fp.oe & 1) == 0, W) : wf2g_fast_kernel_ptr(cigar, G, W);
+  if (!fn) return WF2G_ERR_CUDA_;
   fp.g = g;
   fp.match = cfg.match;
   // one warp per pair updates the rows in place (one slot fewer per ring)
@@ -289,10 +292,11 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
   if (smem > E->smem_optin) return 1;  // rows do not fit: the general passes take all
   fp.s_cap = W;
   fp.pair_cap = cigar && E->bits_cap > 0 ? E->bits_cap : 0;
-  // per step: 4-bit choice codes in 32-bit words, 8 iterations of a thread
-  // per word, and the row's limits (4 bytes)
-  const int iters = (W + G - 1) / G;
-  const int64_t rw = (int64_t)((iters + 7) / 8) * G;
+  // per step: 4-bit choice codes in 32-bit words (8 iterations of a thread
+  // per word; two diagonals per lane: 4 iterations of two cells), and the
+  // row's limits (4 bytes)
+  const int iters = two ? (W / 2 + 31) / 32 : (W + G - 1) / G;
+  const int64_t rw = two ? (int64_t)((iters + 3) / 4) * 32 : (int64_t)((iters + 7) / 8) * G;
   fp.items_off = cigar ? (int64_t)fp.s_cap * (rw * 4 + 4) : 0;
   fp.items_cap = cigar ? 4 * (int64_t)max_len + 64 : 0;
   fp.slice_bytes = cigar ? ((fp.items_off + fp.items_cap + 255) & ~int64_t(255)) : 0;

@@ -1,0 +1,463 @@
+// wfa_fast2.cu -- the warp-per-pair fast kernel with two diagonals per lane.
+//
+// Same semantics and the same retry contract as wfa_fast.cu (a pair it cannot
+// finish goes to the retry list, and the next pass takes it in full): exact
+// gap-affine, end-to-end, A/C/G/T, scores divided by g = gcd(x, o+e, e).
+// Served when the scaled x is even and the scaled e is odd (the default
+// (4,6,2) scales to (2,4,1); with match < 0 the transformed penalties
+// (2x-2m, 2o, 2e-m) of (4,6,2,-1) are (10,12,5)).
+//
+// Layout.  Each shared-memory row holds int16 offsets; the cells of the
+// step at scaled score s are written as 16x2 words of diagonal pairs
+// (a, a+1) with a = s (mod 2): the row of score s stores diagonal d at
+// element W/2 + d - (s & 1).  Then, with x even and e odd:
+//   * M[s-x] at (k, k+1) is one aligned word (same parity),
+//   * I[s-e] at (k-1, k) and D[s-e] at (k+1, k+2) are one aligned word each
+//     (opposite parity),
+//   * M[s-(o+e)] at (k-1, k) and (k+1, k+2) are one word each when o+e is
+//     odd, or two byte permutes of three words when it is even,
+// so a lane computes two cells with 16x2 integer instructions (max.s16x2,
+// add.s16x2, min.u16x2) from five or six 32-bit shared loads and writes
+// three 32-bit words.  Rows are updated in place (max(x,o+e) M rows, e I and
+// D rows): a lane's next words are loaded before the warp barrier that
+// precedes its stores, and a store never overwrites a cell that a later
+// lane or iteration still reads.
+//
+// Per cell, as the reference computes it (wavefront/wavefront_compute_affine.c:
+// 66-84, wavefront/wavefront_extend.c:86-121): I = max(M[s-o-e][k-1],
+// I[s-e][k-1]) + 1, D = max(M[s-o-e][k+1], D[s-e][k+1]), M = max(M[s-x][k]+1,
+// I, D); M is NULL unless 0 <= h <= tlen and 0 <= h-k <= plen (unsigned
+// compares on the clamped coordinates), else extended by the exact LCP.
+// Trimming (wavefront/wavefront_compute.c:579-613) scans the written rows
+// from both ends; I and D cells trimmed away become NULL.
+//
+// Choice codes: 4 bits per cell, 1 = the comparison failed: bit 0 "M from
+// mismatch" (M[s-x]+1 >= max(I, D)), bit 1 "deletion over insertion"
+// (D >= I), bit 2 "insertion extended" (I[s-e] >= M[s-o-e] at k-1), bit 3
+// "deletion extended".  A lane accumulates four iterations per 32-bit word:
+// the low half holds its low cells, the high half its high cells, the
+// first iteration in the top nibble of each half.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "wfa_fast_common.cuh"
+#include "wfa_kernels.cuh"
+
+namespace wf2g {
+
+__device__ __forceinline__ uint32_t vmax_s16x2(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm("max.s16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t vmin_s16x2(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm("min.s16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t vmin_u16x2(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm("min.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t vadd_s16x2(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm("add.s16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+// two int16 halves as one 16x2 word
+__device__ __forceinline__ uint32_t pack16x2(int lo, int hi) {
+  return ((uint32_t)lo & 0xFFFFu) | ((uint32_t)hi << 16);
+}
+
+// Kernel of the two-diagonals-per-lane fast pass.  CIGAR: full alignment or
+// score only.  MOS: o+e (scaled) is even, so M[s-o-e] shares the output
+// rows' parity.  W: elements per shared-memory row (diagonals
+// [4-W/2, W/2-4] are computed).
+template <bool CIGAR, bool MOS, int W>
+__global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
+  constexpr int HALF = W / 2;
+  constexpr int JM = (HALF + 31) / 32;     // most iterations of a step
+  constexpr int RW = ((JM + 3) / 4) * 32;  // 32-bit choice words per step
+  constexpr int WW = W / 2;                // words per row
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x;
+  const int nrows = p.R + 2 * p.RI;
+  int16_t* const rows = reinterpret_cast<int16_t*>(smem + p.rows_off);
+  uint32_t* const rows32 = reinterpret_cast<uint32_t*>(smem + p.rows_off);
+  uint2* const QP = reinterpret_cast<uint2*>(smem + p.q_off);
+  uint2* const QT = QP + p.nq;
+  int2* const meta = reinterpret_cast<int2*>(smem + p.meta_off);
+  // per-warp slice: [choice words: s_cap rows of RW][row limits: s_cap short2][walk items]
+  uint8_t* const slice = p.scratch + (int64_t)blockIdx.x * p.slice_bytes;
+  uint32_t* const codes = reinterpret_cast<uint32_t*>(slice);
+  short2* const tab = reinterpret_cast<short2*>(slice + (int64_t)p.s_cap * RW * 4);
+  uint8_t* const items = slice + p.items_off;
+  const int rowI = p.R, rowD = p.R + p.RI;
+
+  for (int i = lane; i < nrows * WW; i += 32) rows32[i] = 0x80008000u;
+  int used_lo = 0, used_hi = -1;  // words of every row the previous pair touched
+  const int n_items = p.num_items_dev ? *p.num_items_dev : p.n_items;
+
+  while (true) {
+    // ---------------------------------------------------------- next pair
+    int item = 0;
+    if (lane == 0) item = atomicAdd(p.queue, 1);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= n_items) break;
+    const int pair = p.items ? p.items[item] : item;
+    const int plen = p.p_len[pair];
+    const int tlen = p.t_len[pair];
+    auto punt = [&]() {
+      if (lane == 0) p.retry_items[atomicAdd(p.retry_count, 1)] = pair;
+    };
+
+    // ---------------------------------------------------------- reset
+    if (used_lo <= used_hi) {
+      const int span = used_hi - used_lo + 1;
+      for (int i = lane; i < nrows * span; i += 32) {
+        const int r = i / span, j = i - r * span;
+        rows32[r * WW + used_lo + j] = 0x80008000u;
+      }
+    }
+    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
+    bool ok = fast_stage<32>(p.seqs + p.p_off[pair], min(plen, p.max_len), QP, p.nq, lane);
+    ok &= fast_stage<32>(p.seqs + p.t_off[pair], min(tlen, p.max_len), QT, p.nq, lane);
+    __syncwarp();
+    const int k_end = tlen - plen;
+    if (!ok || plen > p.max_len || tlen > p.max_len || k_end < 4 - HALF || k_end > HALF - 4) {
+      punt();
+      used_lo = 0;
+      used_hi = -1;
+      __syncwarp();
+      continue;
+    }
+
+    // ---------------------------------------------------------- score 0
+    // M[0][0] = 0, extended at once (wavefront/wavefront_aligner.c:311-382)
+    const int L0 = fast_lcp(QP, QT, 0, 0, min(plen, tlen));
+    int s = 0;           // scaled score of the last computed wavefront
+    int cM = 0, cI = 0;  // its ring slots
+    int null_steps = 0;
+    int64_t bt_used = 0;     // choice codes of the pair: the general kernel's byte count
+    int w_lo = 0, w_hi = 0;  // diagonals touched
+    bool done = (plen == tlen) && (L0 >= tlen);
+    if (lane == 0) {
+      rows[HALF] = (int16_t)L0;  // row 0 (slot 0 of M, parity 0), diagonal 0
+      meta[0] = make_int2(0, 0);
+      if (CIGAR) tab[0] = make_short2(0, 0);
+    }
+    __syncwarp();
+    const uint32_t plen2 = pack16x2(plen, plen), tlen2 = pack16x2(tlen, tlen);
+
+    bool leave = false;
+    while (!done) {
+      if ((int64_t)p.g * s + 1 >= (int64_t)p.max_steps || s + 1 >= p.s_cap) {
+        // the reference computes score g*s+1 next and stops there at the
+        // step limit (wavefront/wavefront_unialign.c:102-107): the general
+        // kernel reports that
+        leave = true;
+        break;
+      }
+      ++s;
+      const int par = s & 1;
+      cM = (cM + 1 == p.R) ? 0 : cM + 1;
+      cI = (cI + 1 == p.RI) ? 0 : cI + 1;
+      const int sMx = cM - p.x < 0 ? cM - p.x + p.R : cM - p.x;
+      const int sMo = cM - p.oe < 0 ? cM - p.oe + p.R : cM - p.oe;
+      const int sIe = cI - p.e < 0 ? cI - p.e + p.RI : cI - p.e;
+      // input limits (wavefront/wavefront_compute.c:306-352; a score below 0
+      // is a null wavefront)
+      const int2 kEmpty = make_int2(1, 0);
+      const int2 eMx = s >= p.x ? meta[sMx] : kEmpty;
+      const int2 eMo = s >= p.oe ? meta[sMo] : kEmpty;
+      const int2 eI = s >= p.e ? meta[rowI + sIe] : kEmpty;
+      const int2 eD = s >= p.e ? meta[rowD + sIe] : kEmpty;
+      const bool vMx = eMx.x <= eMx.y, vMo = eMo.x <= eMo.y;
+      const bool vI = eI.x <= eI.y, vD = eD.x <= eD.y;
+      // element of diagonal 0 in the output slots (this step's parity), and
+      // in the same slots' previous contents (scores s-R and s-RI)
+      const int bM = cM * W + HALF - par;
+      const int bI = (rowI + cI) * W + HALF - par;
+      const int bD = (rowD + cI) * W + HALF - par;
+      const int obM = cM * W + HALF - ((s - p.R) & 1);
+      const int obI = (rowI + cI) * W + HALF - ((s - p.RI) & 1);
+      const int obD = (rowD + cI) * W + HALF - ((s - p.RI) & 1);
+      const int2 oldM = meta[cM], oldI = meta[rowI + cI], oldD = meta[rowD + cI];
+      if (!(vMx | vMo | vI | vD)) {
+        // a null step (wavefront/wavefront_compute_affine.c:236-243): the
+        // slots taken over become empty and all-NULL
+        for (int k = oldM.x + lane; k <= oldM.y; k += 32) rows[obM + k] = kNull16;
+        for (int k = oldI.x + lane; k <= oldI.y; k += 32) rows[obI + k] = kNull16;
+        for (int k = oldD.x + lane; k <= oldD.y; k += 32) rows[obD + k] = kNull16;
+        __syncwarp();
+        if (lane == 0) {
+          meta[cM] = meta[rowI + cI] = meta[rowD + cI] = kEmpty;
+          if (CIGAR) tab[s] = make_short2(1, 0);
+        }
+        __syncwarp();
+        // more null steps than the scope: the end is unreachable
+        // (wavefront/wavefront_extend.c:95-101), left to the general kernel
+        if (++null_steps > p.R + 1) {
+          leave = true;
+          break;
+        }
+        continue;
+      }
+      null_steps = 0;
+      // output range: union of the inputs' (wavefront/wavefront_compute.c:40-87)
+      int lo = INT_MAX, hi = INT_MIN;
+      if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
+      if (vMo) { lo = min(lo, eMo.x - 1); hi = max(hi, eMo.y + 1); }
+      if (vI) { lo = min(lo, eI.x + 1); hi = max(hi, eI.y + 1); }
+      if (vD) { lo = min(lo, eD.x - 1); hi = max(hi, eD.y - 1); }
+      bt_used += hi - lo + 1;
+      if (lo < 4 - HALF || hi > HALF - 4 ||  // wider than the rows
+          (CIGAR && p.pair_cap > 0 && bt_used > p.pair_cap)) {  // over the pair's budget
+        leave = true;
+        break;
+      }
+      w_lo = min(w_lo, lo);
+      w_hi = max(w_hi, hi);
+      if (CIGAR && lane == 0) tab[s] = make_short2((short)lo, (short)hi);
+
+      // ======================================== the cells
+      // pairs (a0 + 2q, a0 + 2q + 1), a0 = s (mod 2), q < nq; lane q % 32
+      const int a0 = lo - ((lo - par) & 1);
+      const int nq = ((hi - a0) >> 1) + 1;
+      const int niter = (nq + 31) >> 5;
+      const uint32_t* const wMx = rows32 + ((sMx * W + HALF + a0 - par) >> 1);
+      const uint32_t* const wMo =
+          rows32 + (MOS ? ((sMo * W + HALF + a0 - par) >> 1) : ((sMo * W + HALF + a0 - 2 + par) >> 1));
+      const uint32_t* const wI = rows32 + (((rowI + sIe) * W + HALF + a0 - 2 + par) >> 1);
+      const uint32_t* const wD = rows32 + (((rowD + sIe) * W + HALF + a0 + par) >> 1);
+      uint32_t* const oM = rows32 + ((bM + a0) >> 1);
+      uint32_t* const oI = rows32 + ((bI + a0) >> 1);
+      uint32_t* const oD = rows32 + ((bD + a0) >> 1);
+      uint32_t* const crow = CIGAR ? codes + (int64_t)s * RW + lane : nullptr;
+      uint32_t n_x = 0, n_mm = 0, n_mp = 0, n_i = 0, n_d = 0;
+      auto load = [&](int q) {
+        n_x = wMx[q];
+        if (MOS) {
+          const uint32_t w0 = wMo[q - 1], w1 = wMo[q], w2 = wMo[q + 1];
+          n_mm = __byte_perm(w0, w1, 0x5432);  // (k-1, k)
+          n_mp = __byte_perm(w1, w2, 0x5432);  // (k+1, k+2)
+        } else {
+          n_mm = wMo[q];
+          n_mp = wMo[q + 1];
+        }
+        n_i = wI[q];
+        n_d = wD[q];
+      };
+      if (lane < nq) load(lane);
+      int k0 = a0 + 2 * lane;
+      uint32_t acc = 0;  // choice codes of up to four iterations
+      for (int j = 0; j < niter; ++j, k0 += 64) {
+        const uint32_t mx = n_x, mm = n_mm, mp = n_mp, ie = n_i, de = n_d;
+        const int q = lane + 32 * j;
+        if (q + 32 < nq) load(q + 32);
+        // in place: this iteration's stores overwrite cells that the next
+        // iteration's loads (just issued) and this iteration's neighbours
+        // read; the barrier orders every lane's loads before the stores
+        __syncwarp();
+        if (q < nq) {
+          const uint32_t moi = vmax_s16x2(mm, ie);          // max(M[s-o-e][k-1], I[s-e][k-1])
+          const uint32_t i1 = vadd_s16x2(moi, 0x00010001u);
+          const uint32_t d1 = vmax_s16x2(mp, de);           // max(M[s-o-e][k+1], D[s-e][k+1])
+          const uint32_t mis = vadd_s16x2(mx, 0x00010001u);
+          const uint32_t gap = vmax_s16x2(d1, i1);
+          const uint32_t best = vmax_s16x2(mis, gap);
+          // h = best, v = best - k, clamped into the sequences; a clamp that
+          // changed either marks the cell out of bounds
+          const uint32_t vv = vadd_s16x2(best, pack16x2(-k0, -k0 - 1));
+          const uint32_t hc = vmin_u16x2(best, tlen2), vc = vmin_u16x2(vv, plen2);
+          const uint32_t oob = (hc ^ best) | (vc ^ vv);
+          const int ev0 = vc & 0xFFFF, ev1 = vc >> 16, eh0 = hc & 0xFFFF, eh1 = hc >> 16;
+          // first 16-base windows of both cells; further windows only for the
+          // rare long match
+          const uint2 pa0 = QP[ev0 >> 4], pa1 = QP[ev1 >> 4];
+          const uint2 ta0 = QT[eh0 >> 4], ta1 = QT[eh1 >> 4];
+          const uint32_t x0 = __funnelshift_l(pa0.x, pa0.y, (uint32_t)ev0 << 1) ^
+                              __funnelshift_l(ta0.x, ta0.y, (uint32_t)eh0 << 1);
+          const uint32_t x1 = __funnelshift_l(pa1.x, pa1.y, (uint32_t)ev1 << 1) ^
+                              __funnelshift_l(ta1.x, ta1.y, (uint32_t)eh1 << 1);
+          int L0c = __clz(x0) >> 1, L1c = __clz(x1) >> 1;
+          const bool long0 = (x0 == 0) && ((oob & 0xFFFFu) == 0);
+          const bool long1 = (x1 == 0) && ((oob >> 16) == 0);
+          if (long0 | long1) {
+            if (long0) {
+              const int lim = min(plen - ev0, tlen - eh0);
+              if (lim > 16) L0c = 16 + fast_lcp(QP, QT, ev0 + 16, eh0 + 16, lim - 16);
+            }
+            if (long1) {
+              const int lim = min(plen - ev1, tlen - eh1);
+              if (lim > 16) L1c = 16 + fast_lcp(QP, QT, ev1 + 16, eh1 + 16, lim - 16);
+            }
+          }
+          // extended offset, capped at min(plen + k, tlen) (the end of the
+          // shorter rest); NULL out of bounds
+          const uint32_t capv = vmin_s16x2(vadd_s16x2(pack16x2(k0, k0 + 1), plen2), tlen2);
+          const uint32_t mext = vmin_s16x2(vadd_s16x2(best, pack16x2(L0c, L1c)), capv);
+          const uint32_t nullm = vmin_u16x2(oob, 0x00010001u) * 0xFFFFu;
+          oM[q] = (mext & ~nullm) | (0x80008000u & nullm);
+          oI[q] = i1;
+          oD[q] = d1;
+          if (CIGAR) {
+            const uint32_t f0 = vmin_u16x2(best ^ mis, 0x00010001u);
+            const uint32_t f1 = vmin_u16x2(gap ^ d1, 0x00010001u);
+            const uint32_t f2 = vmin_u16x2(moi ^ ie, 0x00010001u);
+            const uint32_t f3 = vmin_u16x2(d1 ^ de, 0x00010001u);
+            acc = (acc << 4) | f0 | (f1 << 1) | (f2 << 2) | (f3 << 3);
+          }
+        } else if (CIGAR) {
+          acc <<= 4;
+        }
+        if (CIGAR && ((j & 3) == 3 || j == niter - 1)) {
+          crow[(j >> 2) * 32] = acc << (4 * (3 - (j & 3)));
+          acc = 0;
+        }
+      }
+      __syncwarp();
+      // Cells written outside [lo, hi] (the first pair's low cell, the last
+      // pair's high cell) and the slots' previous contents outside the
+      // written elements become NULL.
+      const int aL = a0 + 2 * nq - 1;
+      if (lane == 0) {
+        if (a0 < lo) rows[bM + a0] = rows[bI + a0] = rows[bD + a0] = kNull16;
+        if (aL > hi) rows[bM + aL] = rows[bI + aL] = rows[bD + aL] = kNull16;
+      }
+      {
+        const int nlo = a0, nhi = aL;  // written, as element offsets from each row's base
+        if (oldM.x <= oldM.y) {
+          for (int el = obM + oldM.x + lane; el <= min(obM + oldM.y, bM + nlo - 1); el += 32) rows[el] = kNull16;
+          for (int el = max(obM + oldM.x, bM + nhi + 1) + lane; el <= obM + oldM.y; el += 32) rows[el] = kNull16;
+        }
+        if (oldI.x <= oldI.y) {
+          for (int el = obI + oldI.x + lane; el <= min(obI + oldI.y, bI + nlo - 1); el += 32) rows[el] = kNull16;
+          for (int el = max(obI + oldI.x, bI + nhi + 1) + lane; el <= obI + oldI.y; el += 32) rows[el] = kNull16;
+        }
+        if (oldD.x <= oldD.y) {
+          for (int el = obD + oldD.x + lane; el <= min(obD + oldD.y, bD + nlo - 1); el += 32) rows[el] = kNull16;
+          for (int el = max(obD + oldD.x, bD + nhi + 1) + lane; el <= obD + oldD.y; el += 32) rows[el] = kNull16;
+        }
+      }
+      __syncwarp();
+      // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
+      // 579-613): M is not NULL; I has h <= tlen; D has h - k <= plen
+      auto inb = [&](int comp, int k) -> bool {
+        const int v = comp == 0 ? rows[bM + k] : comp == 1 ? rows[bI + k] : rows[bD + k];
+        return comp == 0 ? v != kNull16
+                         : comp == 1 ? (uint32_t)v <= (uint32_t)tlen : (uint32_t)(v - k) <= (uint32_t)plen;
+      };
+      auto first_in = [&](int comp) -> int {
+        for (int b = lo; b <= hi; b += 32) {
+          const int k = b + lane;
+          const uint32_t m = __ballot_sync(kFull, k <= hi && inb(comp, k));
+          if (m) return b + __ffs(m) - 1;
+        }
+        return INT_MAX;
+      };
+      auto last_in = [&](int comp) -> int {
+        for (int b = hi; b >= lo; b -= 32) {
+          const int k = b - lane;
+          const uint32_t m = __ballot_sync(kFull, k >= lo && inb(comp, k));
+          if (m) return b - (__ffs(m) - 1);
+        }
+        return INT_MIN;
+      };
+      const int fM = first_in(0);
+      const int lM = fM == INT_MAX ? INT_MIN : last_in(0);
+      const int fI = first_in(1);
+      const int lI = fI == INT_MAX ? INT_MIN : last_in(1);
+      const int fD = first_in(2);
+      const int lD = fD == INT_MAX ? INT_MIN : last_in(2);
+      // I and D cells trimmed away become NULL (M out of bounds is NULL already)
+      {
+        const int nIL = fI == INT_MAX ? hi - lo + 1 : fI - lo, nIR = fI == INT_MAX ? 0 : hi - lI;
+        const int nDL = fD == INT_MAX ? hi - lo + 1 : fD - lo, nDR = fD == INT_MAX ? 0 : hi - lD;
+        for (int q = lane; q < nIL; q += 32) rows[bI + lo + q] = kNull16;
+        for (int q = lane; q < nIR; q += 32) rows[bI + hi - q] = kNull16;
+        for (int q = lane; q < nDL; q += 32) rows[bD + lo + q] = kNull16;
+        for (int q = lane; q < nDR; q += 32) rows[bD + hi - q] = kNull16;
+      }
+      const int2 tM = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
+      if (lane == 0) {
+        meta[cM] = tM;
+        meta[rowI + cI] = fI == INT_MAX ? kEmpty : make_int2(fI, lI);
+        meta[rowD + cI] = fD == INT_MAX ? kEmpty : make_int2(fD, lD);
+      }
+      // termination on M[s] at k_end (wavefront/wavefront_termination.c:37-60)
+      done = tM.x <= k_end && k_end <= tM.y && rows[bM + k_end] >= tlen;
+      __syncwarp();
+    }
+    // words touched by this pair: elements [W/2 + w_lo - 4, W/2 + w_hi + 3]
+    used_lo = (HALF + w_lo - 4) >> 1;
+    used_hi = (HALF + w_hi + 3) >> 1;
+
+    if (leave) {
+      punt();
+      __syncwarp();
+      continue;
+    }
+    // the result: the classic score (wavefront/wavefront_compute.c:108-120)
+    // at WFA score g*s, in the reference's wrapping int arithmetic
+    const int S = p.g * s;
+    const int score =
+        p.match == 0 ? -S
+                     : (int)((uint32_t)(-p.match) * ((uint32_t)plen + (uint32_t)tlen) - (uint32_t)S) / 2;
+    if (!CIGAR) {
+      if (lane == 0) {
+        p.scores[pair] = score;
+        p.status[pair] = kStCompleted;
+        if (p.end_info) {
+          p.end_info[3 * (int64_t)pair] = plen;
+          p.end_info[3 * (int64_t)pair + 1] = tlen;
+          p.end_info[3 * (int64_t)pair + 2] = S;
+        }
+      }
+    } else {
+      // The rows' limits go to shared memory (the rows are no longer needed;
+      // the next pair clears all of them), then the walk and the replay.
+      short2* const stab = reinterpret_cast<short2*>(rows);
+      for (int i = lane; i <= s; i += 32) stab[i] = tab[i];
+      used_lo = 0;
+      used_hi = WW - 1;
+      __syncwarp();
+      auto code_at = [&](int ss, int kk, bool& bad) -> uint32_t {
+        const short2 lh = stab[ss];
+        if (kk < lh.x || kk > lh.y) {
+          bad = true;
+          return 0u;
+        }
+        const int a0s = lh.x - ((lh.x - (ss & 1)) & 1);
+        const int r = kk - a0s, q = r >> 1, jj = q >> 5;
+        const uint32_t w = codes[(int64_t)ss * RW + (jj >> 2) * 32 + (q & 31)];
+        const uint32_t z = (w >> (((r & 1) << 4) + ((3 - (jj & 3)) << 2))) & 15u;
+        // to the walk's code: source of M (0 mismatch, 1 deletion, 2
+        // insertion), bit 2 insertion extended, bit 3 deletion extended
+        return (!(z & 1u) ? 0u : (!(z & 2u) ? 1u : 2u)) | (~z & 12u);
+      };
+      if (!fast_backtrace(p, pair, plen, tlen, s, k_end, score, S, QP, QT, items, lane, code_at))
+        punt();
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace wf2g
+
+// Kernel of the two-diagonals-per-lane pass for (full CIGAR?, o+e even?, row width).
+extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width) {
+  using namespace wf2g;
+#define WF2G_FAST2_CASE(W)                                                                   \
+  if (width == W) {                                                                          \
+    if (mos) return cigar ? (void*)wfa_fast2_kernel<true, true, W> : (void*)wfa_fast2_kernel<false, true, W>; \
+    return cigar ? (void*)wfa_fast2_kernel<true, false, W> : (void*)wfa_fast2_kernel<false, false, W>;        \
+  }
+  WF2G_FAST2_CASE(1024)
+  WF2G_FAST2_CASE(2048)
+#undef WF2G_FAST2_CASE
+  return nullptr;
+}
