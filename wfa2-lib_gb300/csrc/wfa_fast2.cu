@@ -252,9 +252,13 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         n_d = wD[q];
       };
       if (lane < nq) load(lane);
-      int k0 = a0 + 2 * lane;
+      // per lane: its pair's diagonals (k, k+1) and their negations, as 16x2
+      uint32_t kv = pack16x2(a0 + 2 * lane, a0 + 2 * lane + 1);
+      uint32_t negk = pack16x2(-a0 - 2 * lane, -a0 - 2 * lane - 1);
+      const char* const qp = reinterpret_cast<const char*>(QP);
+      const char* const qt = reinterpret_cast<const char*>(QT);
       uint32_t acc = 0;  // choice codes of up to four iterations
-      for (int j = 0; j < niter; ++j, k0 += 64) {
+      for (int j = 0; j < niter; ++j) {
         const uint32_t mx = n_x, mm = n_mm, mp = n_mp, ie = n_i, de = n_d;
         const int q = lane + 32 * j;
         if (q + 32 < nq) load(q + 32);
@@ -271,35 +275,38 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
           const uint32_t best = vmax_s16x2(mis, gap);
           // h = best, v = best - k, clamped into the sequences; a clamp that
           // changed either marks the cell out of bounds
-          const uint32_t vv = vadd_s16x2(best, pack16x2(-k0, -k0 - 1));
+          const uint32_t vv = vadd_s16x2(best, negk);
           const uint32_t hc = vmin_u16x2(best, tlen2), vc = vmin_u16x2(vv, plen2);
           const uint32_t oob = (hc ^ best) | (vc ^ vv);
-          const int ev0 = vc & 0xFFFF, ev1 = vc >> 16, eh0 = hc & 0xFFFF, eh1 = hc >> 16;
-          // first 16-base windows of both cells; further windows only for the
-          // rare long match
-          const uint2 pa0 = QP[ev0 >> 4], pa1 = QP[ev1 >> 4];
-          const uint2 ta0 = QT[eh0 >> 4], ta1 = QT[eh1 >> 4];
-          const uint32_t x0 = __funnelshift_l(pa0.x, pa0.y, (uint32_t)ev0 << 1) ^
-                              __funnelshift_l(ta0.x, ta0.y, (uint32_t)eh0 << 1);
-          const uint32_t x1 = __funnelshift_l(pa1.x, pa1.y, (uint32_t)ev1 << 1) ^
-                              __funnelshift_l(ta1.x, ta1.y, (uint32_t)eh1 << 1);
+          // first 16-base windows of both cells: byte offsets of the word
+          // pairs ((v >> 4) * 8, both halves at once; v < 2^15) and funnel
+          // shifts (only their low 5 bits count)
+          const uint32_t offP = (vc >> 1) & 0xFFF87FF8u, offT = (hc >> 1) & 0xFFF87FF8u;
+          const uint2 pa0 = *reinterpret_cast<const uint2*>(qp + (offP & 0xFFFFu));
+          const uint2 pa1 = *reinterpret_cast<const uint2*>(qp + (offP >> 16));
+          const uint2 ta0 = *reinterpret_cast<const uint2*>(qt + (offT & 0xFFFFu));
+          const uint2 ta1 = *reinterpret_cast<const uint2*>(qt + (offT >> 16));
+          const uint32_t x0 = __funnelshift_l(pa0.x, pa0.y, vc << 1) ^
+                              __funnelshift_l(ta0.x, ta0.y, hc << 1);
+          const uint32_t x1 = __funnelshift_l(pa1.x, pa1.y, vc >> 15) ^
+                              __funnelshift_l(ta1.x, ta1.y, hc >> 15);
           int L0c = __clz(x0) >> 1, L1c = __clz(x1) >> 1;
-          const bool long0 = (x0 == 0) && ((oob & 0xFFFFu) == 0);
-          const bool long1 = (x1 == 0) && ((oob >> 16) == 0);
-          if (long0 | long1) {
-            if (long0) {
+          if ((x0 == 0) | (x1 == 0)) {
+            // a whole window matched: further windows, for cells in bounds
+            const int ev0 = vc & 0xFFFF, ev1 = vc >> 16, eh0 = hc & 0xFFFF, eh1 = hc >> 16;
+            if (x0 == 0 && (oob & 0xFFFFu) == 0) {
               const int lim = min(plen - ev0, tlen - eh0);
               if (lim > 16) L0c = 16 + fast_lcp(QP, QT, ev0 + 16, eh0 + 16, lim - 16);
             }
-            if (long1) {
+            if (x1 == 0 && (oob >> 16) == 0) {
               const int lim = min(plen - ev1, tlen - eh1);
               if (lim > 16) L1c = 16 + fast_lcp(QP, QT, ev1 + 16, eh1 + 16, lim - 16);
             }
           }
           // extended offset, capped at min(plen + k, tlen) (the end of the
           // shorter rest); NULL out of bounds
-          const uint32_t capv = vmin_s16x2(vadd_s16x2(pack16x2(k0, k0 + 1), plen2), tlen2);
-          const uint32_t mext = vmin_s16x2(vadd_s16x2(best, pack16x2(L0c, L1c)), capv);
+          const uint32_t capv = vmin_s16x2(vadd_s16x2(kv, plen2), tlen2);
+          const uint32_t mext = vmin_s16x2(vadd_s16x2(best, (uint32_t)L0c | ((uint32_t)L1c << 16)), capv);
           const uint32_t nullm = vmin_u16x2(oob, 0x00010001u) * 0xFFFFu;
           oM[q] = (mext & ~nullm) | (0x80008000u & nullm);
           oI[q] = i1;
@@ -318,78 +325,91 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
           crow[(j >> 2) * 32] = acc << (4 * (3 - (j & 3)));
           acc = 0;
         }
+        kv = vadd_s16x2(kv, 0x00400040u);
+        negk = vadd_s16x2(negk, 0xFFC0FFC0u);
       }
       __syncwarp();
       // Cells written outside [lo, hi] (the first pair's low cell, the last
-      // pair's high cell) and the slots' previous contents outside the
-      // written elements become NULL.
+      // pair's high cell) become NULL, and so do the slots' previous contents
+      // outside the written cells [a0, aL].  A previous content at score s'
+      // sits one element off when s' has the other parity: in this step's
+      // diagonals it spans [x + sh, y + sh], sh = (s & 1) - (s' & 1).
       const int aL = a0 + 2 * nq - 1;
       if (lane == 0) {
         if (a0 < lo) rows[bM + a0] = rows[bI + a0] = rows[bD + a0] = kNull16;
         if (aL > hi) rows[bM + aL] = rows[bI + aL] = rows[bD + aL] = kNull16;
       }
       {
-        const int nlo = a0, nhi = aL;  // written, as element offsets from each row's base
-        if (oldM.x <= oldM.y) {
-          for (int el = obM + oldM.x + lane; el <= min(obM + oldM.y, bM + nlo - 1); el += 32) rows[el] = kNull16;
-          for (int el = max(obM + oldM.x, bM + nhi + 1) + lane; el <= obM + oldM.y; el += 32) rows[el] = kNull16;
-        }
-        if (oldI.x <= oldI.y) {
-          for (int el = obI + oldI.x + lane; el <= min(obI + oldI.y, bI + nlo - 1); el += 32) rows[el] = kNull16;
-          for (int el = max(obI + oldI.x, bI + nhi + 1) + lane; el <= obI + oldI.y; el += 32) rows[el] = kNull16;
-        }
-        if (oldD.x <= oldD.y) {
-          for (int el = obD + oldD.x + lane; el <= min(obD + oldD.y, bD + nlo - 1); el += 32) rows[el] = kNull16;
-          for (int el = max(obD + oldD.x, bD + nhi + 1) + lane; el <= obD + oldD.y; el += 32) rows[el] = kNull16;
+        const int shM = par - ((s - p.R) & 1), shI = par - ((s - p.RI) & 1);
+        const bool cM_ = oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
+        const bool cI_ = oldI.x <= oldI.y && (oldI.x + shI < a0 || oldI.y + shI > aL);
+        const bool cD_ = oldD.x <= oldD.y && (oldD.x + shI < a0 || oldD.y + shI > aL);
+        if (cM_ | cI_ | cD_) {
+          auto clear_outside = [&](int base, int x, int y) {  // diagonals [x, y] at base, minus [a0, aL]
+            for (int k = x + lane; k <= min(y, a0 - 1); k += 32) rows[base + k] = kNull16;
+            for (int k = max(x, aL + 1) + lane; k <= y; k += 32) rows[base + k] = kNull16;
+          };
+          if (cM_) clear_outside(bM, oldM.x + shM, oldM.y + shM);
+          if (cI_) clear_outside(bI, oldI.x + shI, oldI.y + shI);
+          if (cD_) clear_outside(bD, oldD.x + shI, oldD.y + shI);
         }
       }
       __syncwarp();
       // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
-      // 579-613): M is not NULL; I has h <= tlen; D has h - k <= plen
+      // 579-613): M is not NULL; I has h <= tlen; D has h - k <= plen.  Lanes
+      // 0-5 test the six end cells; only a component with an end out of
+      // bounds is scanned.
       auto inb = [&](int comp, int k) -> bool {
-        const int v = comp == 0 ? rows[bM + k] : comp == 1 ? rows[bI + k] : rows[bD + k];
+        const int v = rows[(comp == 0 ? bM : comp == 1 ? bI : bD) + k];
         return comp == 0 ? v != kNull16
                          : comp == 1 ? (uint32_t)v <= (uint32_t)tlen : (uint32_t)(v - k) <= (uint32_t)plen;
       };
-      auto first_in = [&](int comp) -> int {
-        for (int b = lo; b <= hi; b += 32) {
-          const int k = b + lane;
-          const uint32_t m = __ballot_sync(kFull, k <= hi && inb(comp, k));
-          if (m) return b + __ffs(m) - 1;
+      const uint32_t ends = __ballot_sync(kFull, lane < 6 && inb(lane >> 1, (lane & 1) ? hi : lo));
+      int fM = lo, lM = hi, fI = lo, lI = hi, fD = lo, lD = hi;
+      if (ends != 0x3Fu) {
+        auto first_in = [&](int comp) -> int {
+          for (int b = lo; b <= hi; b += 32) {
+            const int k = b + lane;
+            const uint32_t m = __ballot_sync(kFull, k <= hi && inb(comp, k));
+            if (m) return b + __ffs(m) - 1;
+          }
+          return INT_MAX;
+        };
+        auto last_in = [&](int comp) -> int {
+          for (int b = hi; b >= lo; b -= 32) {
+            const int k = b - lane;
+            const uint32_t m = __ballot_sync(kFull, k >= lo && inb(comp, k));
+            if (m) return b - (__ffs(m) - 1);
+          }
+          return INT_MIN;
+        };
+        if ((ends & 3u) != 3u) {
+          fM = first_in(0);
+          lM = fM == INT_MAX ? INT_MIN : last_in(0);
         }
-        return INT_MAX;
-      };
-      auto last_in = [&](int comp) -> int {
-        for (int b = hi; b >= lo; b -= 32) {
-          const int k = b - lane;
-          const uint32_t m = __ballot_sync(kFull, k >= lo && inb(comp, k));
-          if (m) return b - (__ffs(m) - 1);
+        if (((ends >> 2) & 3u) != 3u) {
+          fI = first_in(1);
+          lI = fI == INT_MAX ? INT_MIN : last_in(1);
+          // I cells trimmed away become NULL (M out of bounds is NULL already)
+          const int nL = fI == INT_MAX ? hi - lo + 1 : fI - lo, nR = fI == INT_MAX ? 0 : hi - lI;
+          for (int q = lane; q < nL; q += 32) rows[bI + lo + q] = kNull16;
+          for (int q = lane; q < nR; q += 32) rows[bI + hi - q] = kNull16;
         }
-        return INT_MIN;
-      };
-      const int fM = first_in(0);
-      const int lM = fM == INT_MAX ? INT_MIN : last_in(0);
-      const int fI = first_in(1);
-      const int lI = fI == INT_MAX ? INT_MIN : last_in(1);
-      const int fD = first_in(2);
-      const int lD = fD == INT_MAX ? INT_MIN : last_in(2);
-      // I and D cells trimmed away become NULL (M out of bounds is NULL already)
-      {
-        const int nIL = fI == INT_MAX ? hi - lo + 1 : fI - lo, nIR = fI == INT_MAX ? 0 : hi - lI;
-        const int nDL = fD == INT_MAX ? hi - lo + 1 : fD - lo, nDR = fD == INT_MAX ? 0 : hi - lD;
-        for (int q = lane; q < nIL; q += 32) rows[bI + lo + q] = kNull16;
-        for (int q = lane; q < nIR; q += 32) rows[bI + hi - q] = kNull16;
-        for (int q = lane; q < nDL; q += 32) rows[bD + lo + q] = kNull16;
-        for (int q = lane; q < nDR; q += 32) rows[bD + hi - q] = kNull16;
+        if (((ends >> 4) & 3u) != 3u) {
+          fD = first_in(2);
+          lD = fD == INT_MAX ? INT_MIN : last_in(2);
+          const int nL = fD == INT_MAX ? hi - lo + 1 : fD - lo, nR = fD == INT_MAX ? 0 : hi - lD;
+          for (int q = lane; q < nL; q += 32) rows[bD + lo + q] = kNull16;
+          for (int q = lane; q < nR; q += 32) rows[bD + hi - q] = kNull16;
+        }
       }
-      const int2 tM = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
       if (lane == 0) {
-        meta[cM] = tM;
+        meta[cM] = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
         meta[rowI + cI] = fI == INT_MAX ? kEmpty : make_int2(fI, lI);
         meta[rowD + cI] = fD == INT_MAX ? kEmpty : make_int2(fD, lD);
       }
       // termination on M[s] at k_end (wavefront/wavefront_termination.c:37-60)
-      done = tM.x <= k_end && k_end <= tM.y && rows[bM + k_end] >= tlen;
+      done = fM <= k_end && k_end <= lM && rows[bM + k_end] >= tlen;
       __syncwarp();
     }
     // words touched by this pair: elements [W/2 + w_lo - 4, W/2 + w_hi + 3]
