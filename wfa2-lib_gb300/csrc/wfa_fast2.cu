@@ -28,8 +28,10 @@
 // I[s-e][k-1]) + 1, D = max(M[s-o-e][k+1], D[s-e][k+1]), M = max(M[s-x][k]+1,
 // I, D); M is NULL unless 0 <= h <= tlen and 0 <= h-k <= plen (unsigned
 // compares on the clamped coordinates), else extended by the exact LCP.
-// Trimming (wavefront/wavefront_compute.c:579-613) scans the written rows
-// from both ends; I and D cells trimmed away become NULL.
+// Trimming (wavefront/wavefront_compute.c:579-613) tests the end cells of
+// each component's natural range (M: [lo, hi]; I: its sources' range shifted
+// by +1; D: by -1) and scans only when one is out of bounds; I and D cells
+// trimmed away become NULL.
 //
 // Choice codes: 4 bits per cell, 1 = the comparison failed: bit 0 "M from
 // mismatch" (M[s-x]+1 >= max(I, D)), bit 1 "deletion over insertion"
@@ -222,6 +224,13 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       w_lo = min(w_lo, lo);
       w_hi = max(w_hi, hi);
       if (CIGAR && lane == 0) tab[s] = make_short2((short)lo, (short)hi);
+      // the natural ranges of I (sources at k-1) and D (sources at k+1): the
+      // cells of [lo, hi] outside them are computed from NULL or NULL-ish
+      // (negative) inputs only, so they come out negative, out of bounds
+      int iLo = INT_MAX, iHi = INT_MIN, dLo = INT_MAX, dHi = INT_MIN;
+      if (vMo) { iLo = eMo.x + 1; iHi = eMo.y + 1; dLo = eMo.x - 1; dHi = eMo.y - 1; }
+      if (vI) { iLo = min(iLo, eI.x + 1); iHi = max(iHi, eI.y + 1); }
+      if (vD) { dLo = min(dLo, eD.x - 1); dHi = max(dHi, eD.y - 1); }
 
       // ======================================== the cells
       // pairs (a0 + 2q, a0 + 2q + 1), a0 = s (mod 2), q < nq; lane q % 32
@@ -356,51 +365,61 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       }
       __syncwarp();
       // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
-      // 579-613): M is not NULL; I has h <= tlen; D has h - k <= plen.  Lanes
-      // 0-5 test the six end cells; only a component with an end out of
-      // bounds is scanned.
+      // 579-613): M is not NULL (over [lo, hi]); I has h <= tlen and D has
+      // h - k <= plen (over their natural ranges).  Lanes 0-5 test the six
+      // end cells; only a component with an end out of bounds is scanned.
       auto inb = [&](int comp, int k) -> bool {
         const int v = rows[(comp == 0 ? bM : comp == 1 ? bI : bD) + k];
         return comp == 0 ? v != kNull16
                          : comp == 1 ? (uint32_t)v <= (uint32_t)tlen : (uint32_t)(v - k) <= (uint32_t)plen;
       };
-      const uint32_t ends = __ballot_sync(kFull, lane < 6 && inb(lane >> 1, (lane & 1) ? hi : lo));
-      int fM = lo, lM = hi, fI = lo, lI = hi, fD = lo, lD = hi;
+      const bool iE = iLo > iHi, dE = dLo > dHi;  // no I (D) cell has a source
+      bool endok = true;
+      if (lane < 6) {
+        const int comp = lane >> 1, hiend = lane & 1;
+        const int k = comp == 0 ? (hiend ? hi : lo) : comp == 1 ? (hiend ? iHi : iLo) : (hiend ? dHi : dLo);
+        if (!(comp == 1 && iE) && !(comp == 2 && dE)) endok = inb(comp, k);
+      }
+      const uint32_t ends = __ballot_sync(kFull, lane < 6 && endok);
+      int fM = lo, lM = hi;
+      int fI = iE ? INT_MAX : iLo, lI = iE ? INT_MIN : iHi;
+      int fD = dE ? INT_MAX : dLo, lD = dE ? INT_MIN : dHi;
       if (ends != 0x3Fu) {
-        auto first_in = [&](int comp) -> int {
-          for (int b = lo; b <= hi; b += 32) {
-            const int k = b + lane;
-            const uint32_t m = __ballot_sync(kFull, k <= hi && inb(comp, k));
-            if (m) return b + __ffs(m) - 1;
+        auto first_in = [&](int comp, int a, int b) -> int {
+          for (int c = a; c <= b; c += 32) {
+            const int k = c + lane;
+            const uint32_t m = __ballot_sync(kFull, k <= b && inb(comp, k));
+            if (m) return c + __ffs(m) - 1;
           }
           return INT_MAX;
         };
-        auto last_in = [&](int comp) -> int {
-          for (int b = hi; b >= lo; b -= 32) {
-            const int k = b - lane;
-            const uint32_t m = __ballot_sync(kFull, k >= lo && inb(comp, k));
-            if (m) return b - (__ffs(m) - 1);
+        auto last_in = [&](int comp, int a, int b) -> int {
+          for (int c = b; c >= a; c -= 32) {
+            const int k = c - lane;
+            const uint32_t m = __ballot_sync(kFull, k >= a && inb(comp, k));
+            if (m) return c - (__ffs(m) - 1);
           }
           return INT_MIN;
         };
         if ((ends & 3u) != 3u) {
-          fM = first_in(0);
-          lM = fM == INT_MAX ? INT_MIN : last_in(0);
+          fM = first_in(0, lo, hi);
+          lM = fM == INT_MAX ? INT_MIN : last_in(0, lo, hi);
         }
+        // I and D cells of the natural ranges trimmed away become NULL (M out
+        // of bounds is NULL already)
         if (((ends >> 2) & 3u) != 3u) {
-          fI = first_in(1);
-          lI = fI == INT_MAX ? INT_MIN : last_in(1);
-          // I cells trimmed away become NULL (M out of bounds is NULL already)
-          const int nL = fI == INT_MAX ? hi - lo + 1 : fI - lo, nR = fI == INT_MAX ? 0 : hi - lI;
-          for (int q = lane; q < nL; q += 32) rows[bI + lo + q] = kNull16;
-          for (int q = lane; q < nR; q += 32) rows[bI + hi - q] = kNull16;
+          fI = first_in(1, iLo, iHi);
+          lI = fI == INT_MAX ? INT_MIN : last_in(1, iLo, iHi);
+          const int nL = fI == INT_MAX ? iHi - iLo + 1 : fI - iLo, nR = fI == INT_MAX ? 0 : iHi - lI;
+          for (int q = lane; q < nL; q += 32) rows[bI + iLo + q] = kNull16;
+          for (int q = lane; q < nR; q += 32) rows[bI + iHi - q] = kNull16;
         }
         if (((ends >> 4) & 3u) != 3u) {
-          fD = first_in(2);
-          lD = fD == INT_MAX ? INT_MIN : last_in(2);
-          const int nL = fD == INT_MAX ? hi - lo + 1 : fD - lo, nR = fD == INT_MAX ? 0 : hi - lD;
-          for (int q = lane; q < nL; q += 32) rows[bD + lo + q] = kNull16;
-          for (int q = lane; q < nR; q += 32) rows[bD + hi - q] = kNull16;
+          fD = first_in(2, dLo, dHi);
+          lD = fD == INT_MAX ? INT_MIN : last_in(2, dLo, dHi);
+          const int nL = fD == INT_MAX ? dHi - dLo + 1 : fD - dLo, nR = fD == INT_MAX ? 0 : dHi - lD;
+          for (int q = lane; q < nL; q += 32) rows[bD + dLo + q] = kNull16;
+          for (int q = lane; q < nR; q += 32) rows[bD + dHi - q] = kNull16;
         }
       }
       if (lane == 0) {
