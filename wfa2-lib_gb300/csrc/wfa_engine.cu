@@ -279,10 +279,17 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
   const int nw = G / 32;
   auto al16 = [](int64_t b) { return (b + 15) & ~int64_t(15); };
   int64_t off = 0;
-  fp.rows_off = 0;
-  off = al16((int64_t)nrows * W * 2);
-  fp.q_off = (int)off;
-  off = al16(off + (int64_t)2 * fp.nq * 8);
+  if (two) {
+    // the two sequences' word pairs interleaved at offset 0, then the rows
+    fp.q_off = 0;
+    fp.rows_off = (int)al16((int64_t)2 * fp.nq * 8);
+    off = al16(fp.rows_off + (int64_t)nrows * W * 2);
+  } else {
+    fp.rows_off = 0;
+    off = al16((int64_t)nrows * W * 2);
+    fp.q_off = (int)off;
+    off = al16(off + (int64_t)2 * fp.nq * 8);
+  }
   fp.meta_off = (int)off;
   off = al16(off + (int64_t)nw * nrows * 8);
   fp.red_off = (int)off;
@@ -292,11 +299,11 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
   if (smem > E->smem_optin) return 1;  // rows do not fit: the general passes take all
   fp.s_cap = W;
   fp.pair_cap = cigar && E->bits_cap > 0 ? E->bits_cap : 0;
-  // per step: 4-bit choice codes in 32-bit words (8 iterations of a thread
-  // per word; two diagonals per lane: 4 iterations of two cells), and the
-  // row's limits (4 bytes)
-  const int iters = two ? (W / 2 + 31) / 32 : (W + G - 1) / G;
-  const int64_t rw = two ? (int64_t)((iters + 3) / 4) * 32 : (int64_t)((iters + 7) / 8) * G;
+  // per step: 4-bit choice codes (one cell per thread: 8 iterations per
+  // 32-bit word; two diagonals per lane: a 16-bit entry per lane and
+  // iteration of 64 words), and the row's limits (4 bytes)
+  const int iters = two ? (W / 2 + 63) / 64 : (W + G - 1) / G;
+  const int64_t rw = two ? (int64_t)iters * 16 : (int64_t)((iters + 7) / 8) * G;
   fp.items_off = cigar ? (int64_t)fp.s_cap * (rw * 4 + 4) : 0;
   fp.items_cap = cigar ? 4 * (int64_t)max_len + 64 : 0;
   fp.slice_bytes = cigar ? ((fp.items_off + fp.items_cap + 255) & ~int64_t(255)) : 0;

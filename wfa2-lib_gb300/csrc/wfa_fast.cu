@@ -499,8 +499,8 @@ __global__ void __launch_bounds__(G) wfa_fast_kernel(const FastParams p) {
           const uint32_t w = codes[(int64_t)ss * RW + (jj >> 3) * G + tt];
           return (w >> ((jj & 7) << 2)) & 15u;
         };
-        if (!fast_backtrace(p, pair, plen, tlen, s, k_end, score, S, QP, QT, items, lane,
-                            code_at))
+        if (!fast_backtrace<1>(p, pair, plen, tlen, s, k_end, score, S, QP, QT, items, lane,
+                               code_at))
           punt();
       }
       if (G > 32 && lane == 0) {

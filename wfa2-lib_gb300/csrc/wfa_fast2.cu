@@ -36,9 +36,9 @@
 // Choice codes: 4 bits per cell, 1 = the comparison failed: bit 0 "M from
 // mismatch" (M[s-x]+1 >= max(I, D)), bit 1 "deletion over insertion"
 // (D >= I), bit 2 "insertion extended" (I[s-e] >= M[s-o-e] at k-1), bit 3
-// "deletion extended".  A lane accumulates four iterations per 32-bit word:
-// the low half holds its low cells, the high half its high cells, the
-// first iteration in the top nibble of each half.
+// "deletion extended".  A lane writes one 16-bit entry per iteration (its
+// two words' four cells).  M cells out of bounds are stored with the sign
+// bit set (far below 0), not as the exact NULL.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -81,16 +81,20 @@ __device__ __forceinline__ uint32_t pack16x2(int lo, int hi) {
 template <bool CIGAR, bool MOS, int W>
 __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
   constexpr int HALF = W / 2;
-  constexpr int JM = (HALF + 31) / 32;     // most iterations of a step
-  constexpr int RW = ((JM + 3) / 4) * 32;  // 32-bit choice words per step
-  constexpr int WW = W / 2;                // words per row
+  constexpr int JM = (HALF + 63) / 64;  // most iterations of a step (64 words each)
+  constexpr int RW = JM * 16;           // 32-bit choice words per step (16 bits per lane per iteration)
+  constexpr int WW = W / 2;             // words per row
+  // a range with no cell: min/max over ranges need no validity tests
+  constexpr int kBig = 1 << 20;
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x;
   const int nrows = p.R + 2 * p.RI;
   int16_t* const rows = reinterpret_cast<int16_t*>(smem + p.rows_off);
   uint32_t* const rows32 = reinterpret_cast<uint32_t*>(smem + p.rows_off);
-  uint2* const QP = reinterpret_cast<uint2*>(smem + p.q_off);
-  uint2* const QT = QP + p.nq;
+  // the two sequences' word pairs interleaved at the start of shared
+  // memory: entry i (16 bytes) = {P pair i, T pair i}
+  uint2* const QP = reinterpret_cast<uint2*>(smem);
+  uint2* const QT = QP + 1;
   int2* const meta = reinterpret_cast<int2*>(smem + p.meta_off);
   // per-warp slice: [choice words: s_cap rows of RW][row limits: s_cap short2][walk items]
   uint8_t* const slice = p.scratch + (int64_t)blockIdx.x * p.slice_bytes;
@@ -124,9 +128,9 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         rows32[r * WW + used_lo + j] = 0x80008000u;
       }
     }
-    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(1, 0);
-    bool ok = fast_stage<32>(p.seqs + p.p_off[pair], min(plen, p.max_len), QP, p.nq, lane);
-    ok &= fast_stage<32>(p.seqs + p.t_off[pair], min(tlen, p.max_len), QT, p.nq, lane);
+    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(kBig, -kBig);
+    bool ok = fast_stage<32, 2>(p.seqs + p.p_off[pair], min(plen, p.max_len), QP, p.nq, lane);
+    ok &= fast_stage<32, 2>(p.seqs + p.t_off[pair], min(tlen, p.max_len), QT, p.nq, lane);
     __syncwarp();
     const int k_end = tlen - plen;
     if (!ok || plen > p.max_len || tlen > p.max_len || k_end < 4 - HALF || k_end > HALF - 4) {
@@ -139,7 +143,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
 
     // ---------------------------------------------------------- score 0
     // M[0][0] = 0, extended at once (wavefront/wavefront_aligner.c:311-382)
-    const int L0 = fast_lcp(QP, QT, 0, 0, min(plen, tlen));
+    const int L0 = fast_lcp<2>(QP, QT, 0, 0, min(plen, tlen));
     int s = 0;           // scaled score of the last computed wavefront
     int cM = 0, cI = 0;  // its ring slots
     int null_steps = 0;
@@ -170,15 +174,14 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       const int sMx = cM - p.x < 0 ? cM - p.x + p.R : cM - p.x;
       const int sMo = cM - p.oe < 0 ? cM - p.oe + p.R : cM - p.oe;
       const int sIe = cI - p.e < 0 ? cI - p.e + p.RI : cI - p.e;
-      // input limits (wavefront/wavefront_compute.c:306-352; a score below 0
-      // is a null wavefront)
-      const int2 kEmpty = make_int2(1, 0);
-      const int2 eMx = s >= p.x ? meta[sMx] : kEmpty;
-      const int2 eMo = s >= p.oe ? meta[sMo] : kEmpty;
-      const int2 eI = s >= p.e ? meta[rowI + sIe] : kEmpty;
-      const int2 eD = s >= p.e ? meta[rowD + sIe] : kEmpty;
-      const bool vMx = eMx.x <= eMx.y, vMo = eMo.x <= eMo.y;
-      const bool vI = eI.x <= eI.y, vD = eD.x <= eD.y;
+      // input limits (wavefront/wavefront_compute.c:306-352).  A score below
+      // 0 is a null wavefront: its slot (s - d + R >= s for d <= R) has not
+      // been written for this pair yet and still holds the empty range.
+      const int2 kEmpty = make_int2(kBig, -kBig);
+      const int2 eMx = meta[sMx];
+      const int2 eMo = meta[sMo];
+      const int2 eI = meta[rowI + sIe];
+      const int2 eD = meta[rowD + sIe];
       // element of diagonal 0 in the output slots (this step's parity), and
       // in the same slots' previous contents (scores s-R and s-RI)
       const int bM = cM * W + HALF - par;
@@ -188,7 +191,10 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       const int obI = (rowI + cI) * W + HALF - ((s - p.RI) & 1);
       const int obD = (rowD + cI) * W + HALF - ((s - p.RI) & 1);
       const int2 oldM = meta[cM], oldI = meta[rowI + cI], oldD = meta[rowD + cI];
-      if (!(vMx | vMo | vI | vD)) {
+      // output range: union of the inputs' (wavefront/wavefront_compute.c:40-87)
+      const int lo = min(min(eMx.x, eMo.x - 1), min(eI.x + 1, eD.x - 1));
+      const int hi = max(max(eMx.y, eMo.y + 1), max(eI.y + 1, eD.y - 1));
+      if (lo > hi) {
         // a null step (wavefront/wavefront_compute_affine.c:236-243): the
         // slots taken over become empty and all-NULL
         for (int k = oldM.x + lane; k <= oldM.y; k += 32) rows[obM + k] = kNull16;
@@ -209,12 +215,6 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         continue;
       }
       null_steps = 0;
-      // output range: union of the inputs' (wavefront/wavefront_compute.c:40-87)
-      int lo = INT_MAX, hi = INT_MIN;
-      if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
-      if (vMo) { lo = min(lo, eMo.x - 1); hi = max(hi, eMo.y + 1); }
-      if (vI) { lo = min(lo, eI.x + 1); hi = max(hi, eI.y + 1); }
-      if (vD) { lo = min(lo, eD.x - 1); hi = max(hi, eD.y - 1); }
       bt_used += hi - lo + 1;
       if (lo < 4 - HALF || hi > HALF - 4 ||  // wider than the rows
           (CIGAR && p.pair_cap > 0 && bt_used > p.pair_cap)) {  // over the pair's budget
@@ -227,16 +227,13 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       // the natural ranges of I (sources at k-1) and D (sources at k+1): the
       // cells of [lo, hi] outside them are computed from NULL or NULL-ish
       // (negative) inputs only, so they come out negative, out of bounds
-      int iLo = INT_MAX, iHi = INT_MIN, dLo = INT_MAX, dHi = INT_MIN;
-      if (vMo) { iLo = eMo.x + 1; iHi = eMo.y + 1; dLo = eMo.x - 1; dHi = eMo.y - 1; }
-      if (vI) { iLo = min(iLo, eI.x + 1); iHi = max(iHi, eI.y + 1); }
-      if (vD) { dLo = min(dLo, eD.x - 1); dHi = max(dHi, eD.y - 1); }
+      const int iLo = min(eMo.x, eI.x) + 1, iHi = max(eMo.y, eI.y) + 1;
+      const int dLo = min(eMo.x, eD.x) - 1, dHi = max(eMo.y, eD.y) - 1;
 
       // ======================================== the cells
       // pairs (a0 + 2q, a0 + 2q + 1), a0 = s (mod 2), q < nq; lane q % 32
       const int a0 = lo - ((lo - par) & 1);
       const int nq = ((hi - a0) >> 1) + 1;
-      const int niter = (nq + 31) >> 5;
       const uint32_t* const wMx = rows32 + ((sMx * W + HALF + a0 - par) >> 1);
       const uint32_t* const wMo =
           rows32 + (MOS ? ((sMo * W + HALF + a0 - par) >> 1) : ((sMo * W + HALF + a0 - 2 + par) >> 1));
@@ -245,97 +242,109 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       uint32_t* const oM = rows32 + ((bM + a0) >> 1);
       uint32_t* const oI = rows32 + ((bI + a0) >> 1);
       uint32_t* const oD = rows32 + ((bD + a0) >> 1);
-      uint32_t* const crow = CIGAR ? codes + (int64_t)s * RW + lane : nullptr;
-      uint32_t n_x = 0, n_mm = 0, n_mp = 0, n_i = 0, n_d = 0;
-      auto load = [&](int q) {
-        n_x = wMx[q];
+      // choice codes: a 16-bit entry per lane and iteration
+      uint16_t* const crow = CIGAR ? reinterpret_cast<uint16_t*>(codes + (int64_t)s * RW) + lane : nullptr;
+      // The inputs of one word (two cells): M[s-x] at (k, k+1), M[s-o-e] at
+      // (k-1, k) and (k+1, k+2), I[s-e] at (k-1, k), D[s-e] at (k+1, k+2).
+      struct In { uint32_t x, mm, mp, i, d; };
+      auto load = [&](int q) -> In {
+        In r;
+        r.x = wMx[q];
         if (MOS) {
           const uint32_t w0 = wMo[q - 1], w1 = wMo[q], w2 = wMo[q + 1];
-          n_mm = __byte_perm(w0, w1, 0x5432);  // (k-1, k)
-          n_mp = __byte_perm(w1, w2, 0x5432);  // (k+1, k+2)
+          r.mm = __byte_perm(w0, w1, 0x5432);  // (k-1, k)
+          r.mp = __byte_perm(w1, w2, 0x5432);  // (k+1, k+2)
         } else {
-          n_mm = wMo[q];
-          n_mp = wMo[q + 1];
+          r.mm = wMo[q];
+          r.mp = wMo[q + 1];
         }
-        n_i = wI[q];
-        n_d = wD[q];
+        r.i = wI[q];
+        r.d = wD[q];
+        return r;
       };
-      if (lane < nq) load(lane);
-      // per lane: its pair's diagonals (k, k+1) and their negations, as 16x2
-      uint32_t kv = pack16x2(a0 + 2 * lane, a0 + 2 * lane + 1);
-      uint32_t negk = pack16x2(-a0 - 2 * lane, -a0 - 2 * lane - 1);
-      const char* const qp = reinterpret_cast<const char*>(QP);
-      const char* const qt = reinterpret_cast<const char*>(QT);
-      uint32_t acc = 0;  // choice codes of up to four iterations
+      const char* const qs = reinterpret_cast<const char*>(smem);
+      // One word: the cells (k, k+1), k = a0 + 2q, with kvp = (k + plen,
+      // k + 1 + plen) and negk = (-k, -k-1) as 16x2.  Stores the word's M, I and D and returns
+      // its choice codes (low half: cell k, high half: cell k+1).
+      auto cells = [&](int q, const In& in, uint32_t kvp, uint32_t negk) -> uint32_t {
+        const uint32_t moi = vmax_s16x2(in.mm, in.i);        // max(M[s-o-e][k-1], I[s-e][k-1])
+        const uint32_t i1 = vadd_s16x2(moi, 0x00010001u);
+        const uint32_t d1 = vmax_s16x2(in.mp, in.d);         // max(M[s-o-e][k+1], D[s-e][k+1])
+        const uint32_t mis = vadd_s16x2(in.x, 0x00010001u);
+        const uint32_t gap = vmax_s16x2(d1, i1);
+        const uint32_t best = vmax_s16x2(mis, gap);
+        // h = best, v = best - k, clamped into the sequences; a clamp that
+        // changed either marks the cell out of bounds
+        const uint32_t vv = vadd_s16x2(best, negk);
+        const uint32_t hc = vmin_u16x2(best, tlen2), vc = vmin_u16x2(vv, plen2);
+        const uint32_t oob = (hc ^ best) | (vc ^ vv);
+        // first 16-base windows of both cells: the 16-byte entries at
+        // (v >> 4) * 16 = v & ~15 (P) and h & ~15 (+8: T), and funnel
+        // shifts (only their low 5 bits count)
+        const uint2 pa0 = *reinterpret_cast<const uint2*>(qs + (vc & 0xFFF0u));
+        const uint2 pa1 = *reinterpret_cast<const uint2*>(qs + ((vc >> 16) & 0xFFF0u));
+        const uint2 ta0 = *reinterpret_cast<const uint2*>(qs + 8 + (hc & 0xFFF0u));
+        const uint2 ta1 = *reinterpret_cast<const uint2*>(qs + 8 + ((hc >> 16) & 0xFFF0u));
+        const uint32_t x0 = __funnelshift_l(pa0.x, pa0.y, vc << 1) ^
+                            __funnelshift_l(ta0.x, ta0.y, hc << 1);
+        const uint32_t x1 = __funnelshift_l(pa1.x, pa1.y, vc >> 15) ^
+                            __funnelshift_l(ta1.x, ta1.y, hc >> 15);
+        int L0c = __clz(x0) >> 1, L1c = __clz(x1) >> 1;
+        if ((x0 == 0) | (x1 == 0)) {
+          // a whole window matched: further windows, for cells in bounds
+          const int ev0 = vc & 0xFFFF, ev1 = vc >> 16, eh0 = hc & 0xFFFF, eh1 = hc >> 16;
+          if (x0 == 0 && (oob & 0xFFFFu) == 0) {
+            const int lim = min(plen - ev0, tlen - eh0);
+            if (lim > 16) L0c = 16 + fast_lcp<2>(QP, QT, ev0 + 16, eh0 + 16, lim - 16);
+          }
+          if (x1 == 0 && (oob >> 16) == 0) {
+            const int lim = min(plen - ev1, tlen - eh1);
+            if (lim > 16) L1c = 16 + fast_lcp<2>(QP, QT, ev1 + 16, eh1 + 16, lim - 16);
+          }
+        }
+        // extended offset, capped at min(plen + k, tlen) (the end of the
+        // shorter rest).  Out of bounds the sign bit is set: mext is then at
+        // most tlen or already below -2^14, so the cell stays far below 0
+        // (NULL-ish) for every later step.
+        const uint32_t capv = vmin_s16x2(kvp, tlen2);
+        const uint32_t mext = vmin_s16x2(vadd_s16x2(best, (uint32_t)L0c | ((uint32_t)L1c << 16)), capv);
+        oM[q] = mext | (vmin_u16x2(oob, 0x00010001u) << 15);
+        oI[q] = i1;
+        oD[q] = d1;
+        if (!CIGAR) return 0u;
+        const uint32_t f0 = vmin_u16x2(best ^ mis, 0x00010001u);
+        const uint32_t f1 = vmin_u16x2(gap ^ d1, 0x00010001u);
+        const uint32_t f2 = vmin_u16x2(moi ^ in.i, 0x00010001u);
+        const uint32_t f3 = vmin_u16x2(d1 ^ in.d, 0x00010001u);
+        return f0 | (f1 << 1) | (f2 << 2) | (f3 << 3);
+      };
+      // Lane t takes words t + 32m, m = 0 .. mlast; two per iteration (m =
+      // 2j and 2j+1), two independent chains.  Choice codes: per iteration a
+      // 16-bit entry per lane, nibbles [word 2j low cell, word 2j+1 low
+      // cell, word 2j high cell, word 2j+1 high cell].
+      const int mlast = (nq - 1) >> 5;
+      const int niter = (mlast >> 1) + 1;
+      In n0{}, n1{};
+      if (lane < nq) n0 = load(lane);
+      if (lane + 32 < nq) n1 = load(lane + 32);
+      uint32_t kvp0 = pack16x2(a0 + 2 * lane + plen, a0 + 2 * lane + 1 + plen);
+      uint32_t negk0 = pack16x2(-a0 - 2 * lane, -a0 - 2 * lane - 1);
       for (int j = 0; j < niter; ++j) {
-        const uint32_t mx = n_x, mm = n_mm, mp = n_mp, ie = n_i, de = n_d;
-        const int q = lane + 32 * j;
-        if (q + 32 < nq) load(q + 32);
+        const In c0 = n0, c1 = n1;
+        const int q0 = lane + 64 * j, q1 = q0 + 32;
+        if (q0 + 64 < nq) n0 = load(q0 + 64);
+        if (q1 + 64 < nq) n1 = load(q1 + 64);
         // in place: this iteration's stores overwrite cells that the next
         // iteration's loads (just issued) and this iteration's neighbours
         // read; the barrier orders every lane's loads before the stores
         __syncwarp();
-        if (q < nq) {
-          const uint32_t moi = vmax_s16x2(mm, ie);          // max(M[s-o-e][k-1], I[s-e][k-1])
-          const uint32_t i1 = vadd_s16x2(moi, 0x00010001u);
-          const uint32_t d1 = vmax_s16x2(mp, de);           // max(M[s-o-e][k+1], D[s-e][k+1])
-          const uint32_t mis = vadd_s16x2(mx, 0x00010001u);
-          const uint32_t gap = vmax_s16x2(d1, i1);
-          const uint32_t best = vmax_s16x2(mis, gap);
-          // h = best, v = best - k, clamped into the sequences; a clamp that
-          // changed either marks the cell out of bounds
-          const uint32_t vv = vadd_s16x2(best, negk);
-          const uint32_t hc = vmin_u16x2(best, tlen2), vc = vmin_u16x2(vv, plen2);
-          const uint32_t oob = (hc ^ best) | (vc ^ vv);
-          // first 16-base windows of both cells: byte offsets of the word
-          // pairs ((v >> 4) * 8, both halves at once; v < 2^15) and funnel
-          // shifts (only their low 5 bits count)
-          const uint32_t offP = (vc >> 1) & 0xFFF87FF8u, offT = (hc >> 1) & 0xFFF87FF8u;
-          const uint2 pa0 = *reinterpret_cast<const uint2*>(qp + (offP & 0xFFFFu));
-          const uint2 pa1 = *reinterpret_cast<const uint2*>(qp + (offP >> 16));
-          const uint2 ta0 = *reinterpret_cast<const uint2*>(qt + (offT & 0xFFFFu));
-          const uint2 ta1 = *reinterpret_cast<const uint2*>(qt + (offT >> 16));
-          const uint32_t x0 = __funnelshift_l(pa0.x, pa0.y, vc << 1) ^
-                              __funnelshift_l(ta0.x, ta0.y, hc << 1);
-          const uint32_t x1 = __funnelshift_l(pa1.x, pa1.y, vc >> 15) ^
-                              __funnelshift_l(ta1.x, ta1.y, hc >> 15);
-          int L0c = __clz(x0) >> 1, L1c = __clz(x1) >> 1;
-          if ((x0 == 0) | (x1 == 0)) {
-            // a whole window matched: further windows, for cells in bounds
-            const int ev0 = vc & 0xFFFF, ev1 = vc >> 16, eh0 = hc & 0xFFFF, eh1 = hc >> 16;
-            if (x0 == 0 && (oob & 0xFFFFu) == 0) {
-              const int lim = min(plen - ev0, tlen - eh0);
-              if (lim > 16) L0c = 16 + fast_lcp(QP, QT, ev0 + 16, eh0 + 16, lim - 16);
-            }
-            if (x1 == 0 && (oob >> 16) == 0) {
-              const int lim = min(plen - ev1, tlen - eh1);
-              if (lim > 16) L1c = 16 + fast_lcp(QP, QT, ev1 + 16, eh1 + 16, lim - 16);
-            }
-          }
-          // extended offset, capped at min(plen + k, tlen) (the end of the
-          // shorter rest); NULL out of bounds
-          const uint32_t capv = vmin_s16x2(vadd_s16x2(kv, plen2), tlen2);
-          const uint32_t mext = vmin_s16x2(vadd_s16x2(best, (uint32_t)L0c | ((uint32_t)L1c << 16)), capv);
-          const uint32_t nullm = vmin_u16x2(oob, 0x00010001u) * 0xFFFFu;
-          oM[q] = (mext & ~nullm) | (0x80008000u & nullm);
-          oI[q] = i1;
-          oD[q] = d1;
-          if (CIGAR) {
-            const uint32_t f0 = vmin_u16x2(best ^ mis, 0x00010001u);
-            const uint32_t f1 = vmin_u16x2(gap ^ d1, 0x00010001u);
-            const uint32_t f2 = vmin_u16x2(moi ^ ie, 0x00010001u);
-            const uint32_t f3 = vmin_u16x2(d1 ^ de, 0x00010001u);
-            acc = (acc << 4) | f0 | (f1 << 1) | (f2 << 2) | (f3 << 3);
-          }
-        } else if (CIGAR) {
-          acc <<= 4;
-        }
-        if (CIGAR && ((j & 3) == 3 || j == niter - 1)) {
-          crow[(j >> 2) * 32] = acc << (4 * (3 - (j & 3)));
-          acc = 0;
-        }
-        kv = vadd_s16x2(kv, 0x00400040u);
-        negk = vadd_s16x2(negk, 0xFFC0FFC0u);
+        uint32_t code = 0;
+        if (q0 < nq) code = cells(q0, c0, kvp0, negk0);
+        if (q1 < nq)
+          code |= cells(q1, c1, vadd_s16x2(kvp0, 0x00400040u), vadd_s16x2(negk0, 0xFFC0FFC0u)) << 4;
+        if (CIGAR) crow[j * 32] = (uint16_t)__byte_perm(code, 0u, 0x4420u);
+        kvp0 = vadd_s16x2(kvp0, 0x00800080u);
+        negk0 = vadd_s16x2(negk0, 0xFF80FF80u);
       }
       __syncwarp();
       // Cells written outside [lo, hi] (the first pair's low cell, the last
@@ -365,12 +374,12 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       }
       __syncwarp();
       // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
-      // 579-613): M is not NULL (over [lo, hi]); I has h <= tlen and D has
+      // 579-613): M is not negative (over [lo, hi]); I has h <= tlen and D has
       // h - k <= plen (over their natural ranges).  Lanes 0-5 test the six
       // end cells; only a component with an end out of bounds is scanned.
       auto inb = [&](int comp, int k) -> bool {
         const int v = rows[(comp == 0 ? bM : comp == 1 ? bI : bD) + k];
-        return comp == 0 ? v != kNull16
+        return comp == 0 ? v >= 0
                          : comp == 1 ? (uint32_t)v <= (uint32_t)tlen : (uint32_t)(v - k) <= (uint32_t)plen;
       };
       const bool iE = iLo > iHi, dE = dLo > dHi;  // no I (D) cell has a source
@@ -471,14 +480,15 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
           return 0u;
         }
         const int a0s = lh.x - ((lh.x - (ss & 1)) & 1);
-        const int r = kk - a0s, q = r >> 1, jj = q >> 5;
-        const uint32_t w = codes[(int64_t)ss * RW + (jj >> 2) * 32 + (q & 31)];
-        const uint32_t z = (w >> (((r & 1) << 4) + ((3 - (jj & 3)) << 2))) & 15u;
+        const int r = kk - a0s, q = r >> 1;
+        const uint32_t w =
+            reinterpret_cast<const uint16_t*>(codes + (int64_t)ss * RW)[(q >> 6) * 32 + (q & 31)];
+        const uint32_t z = (w >> (((r & 1) << 3) + (((q >> 5) & 1) << 2))) & 15u;
         // to the walk's code: source of M (0 mismatch, 1 deletion, 2
         // insertion), bit 2 insertion extended, bit 3 deletion extended
         return (!(z & 1u) ? 0u : (!(z & 2u) ? 1u : 2u)) | (~z & 12u);
       };
-      if (!fast_backtrace(p, pair, plen, tlen, s, k_end, score, S, QP, QT, items, lane, code_at))
+      if (!fast_backtrace<2>(p, pair, plen, tlen, s, k_end, score, S, QP, QT, items, lane, code_at))
         punt();
     }
     __syncwarp();

@@ -14,14 +14,16 @@ namespace wf2g {
 
 // Longest common prefix of P[v..] and T[h..], at most lim bases (lim >= 0,
 // v+lim <= plen, h+lim <= tlen): 16-base windows, XOR + count leading zeros
-// (wavefront/wavefront_extend_kernels.c:68-92).  Q[i] = {word i+1, word i}.
+// (wavefront/wavefront_extend_kernels.c:68-92).  Q[i*S] = {word i+1, word i}
+// (S = 2: the two sequences' word pairs interleaved).
+template <int S = 1>
 __device__ __forceinline__ int fast_lcp(const uint2* __restrict__ QP, const uint2* __restrict__ QT,
                                         int v, int h, int lim) {
   int L = 0;
   while (L < lim) {
     const int pv = v + L, ph = h + L;
-    const uint2 a = QP[pv >> 4];
-    const uint2 b = QT[ph >> 4];
+    const uint2 a = QP[(pv >> 4) * S];
+    const uint2 b = QT[(ph >> 4) * S];
     const uint32_t d = __funnelshift_l(a.x, a.y, (uint32_t)pv << 1) ^
                        __funnelshift_l(b.x, b.y, (uint32_t)ph << 1);
     if (d) {
@@ -40,9 +42,9 @@ __device__ __forceinline__ void fast_sync() {
 }
 
 // Stages one sequence as word pairs: base i at bits [31-2(i%16), 30-2(i%16)]
-// of word i/16, Q[i] = {word i+1, word i} for i < nq (words past the
+// of word i/16, Q[i*S] = {word i+1, word i} for i < nq (words past the
 // sequence are 0).  Returns false (group-uniform) if a byte is not A/C/G/T.
-template <int G>
+template <int G, int S = 1>
 __device__ bool fast_stage(const uint8_t* __restrict__ src, int len, uint2* Q, int nq, int t) {
   const int lane = t & 31;
   bool ok = true;
@@ -62,11 +64,11 @@ __device__ bool fast_stage(const uint8_t* __restrict__ src, int len, uint2* Q, i
     const int i0 = 2 * b, i1 = 2 * b + 1;
     // word j goes to Q[j].y and Q[j-1].x
     if (lane == 0) {
-      if (i0 < nq) Q[i0].y = w0;
-      if (i0 >= 1 && i0 - 1 < nq) Q[i0 - 1].x = w0;
+      if (i0 < nq) Q[i0 * S].y = w0;
+      if (i0 >= 1 && i0 - 1 < nq) Q[(i0 - 1) * S].x = w0;
     } else if (lane == 1) {
-      if (i1 < nq) Q[i1].y = w1;
-      if (i1 - 1 < nq) Q[i1 - 1].x = w1;
+      if (i1 < nq) Q[i1 * S].y = w1;
+      if (i1 - 1 < nq) Q[(i1 - 1) * S].x = w1;
     }
   }
   if (G == 32) return __all_sync(kFull, ok);
@@ -80,11 +82,11 @@ __device__ bool fast_stage(const uint8_t* __restrict__ src, int len, uint2* Q, i
 // 1 deletion, 2 insertion), bit 2 "insertion extended", bit 3 "deletion
 // extended"; it sets bad for a cell outside its row.  The walk records the
 // operations backwards in items (an 'E' at every M visit); the replay
-// re-extends each M visit with the same LCP.  Writes the pair's score,
-// status, CIGAR length and end position; returns false if the trace was
-// inconsistent or did not fit (the caller leaves the pair to the general
-// kernel).
-template <typename CodeAt>
+// re-extends each M visit with the same LCP (staged word pairs at stride
+// QS).  Writes the pair's score, status, CIGAR length and end position;
+// returns false if the trace was inconsistent or did not fit (the caller
+// leaves the pair to the general kernel).
+template <int QS, typename CodeAt>
 __device__ bool fast_backtrace(const FastParams& p, int pair, int plen, int tlen, int s,
                                int k_end, int score, int S, const uint2* QP, const uint2* QT,
                                uint8_t* items, int lane, CodeAt code_at) {
@@ -179,7 +181,7 @@ __device__ bool fast_backtrace(const FastParams& p, int pair, int plen, int tlen
     for (int q = 0; q < cnt; ++q) {
       const uint32_t it = __shfl_sync(kFull, mine, q);
       if (it == 'E') {
-        const int L = fast_lcp(QP, QT, v, h, min(plen - v, tlen - h));
+        const int L = fast_lcp<QS>(QP, QT, v, h, min(plen - v, tlen - h));
         if (out_n + L > cap) { bad = true; break; }
         for (int u = lane; u < L; u += 32) out[out_n + u] = 'M';
         out_n += L;
