@@ -247,7 +247,9 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
   // a warp per pair takes two diagonals per lane when the scaled x is even
   // and the scaled e odd (wfa_fast2.cu); else one cell per thread
   const bool two = G == 32 && (fp.x & 1) == 0 && (fp.e & 1) == 1 && env_int("WF2G_FAST2", 1);
-  void* fn = two ? wf2g_fast2_kernel_ptr(cigar, (fp.oe & 1) == 0, W) : wf2g_fast_kernel_ptr(cigar, G, W);
+  const bool d241 = fp.x == 2 && fp.oe == 4 && fp.e == 1;
+  void* fn = two ? wf2g_fast2_kernel_ptr(cigar, (fp.oe & 1) == 0, W, d241)
+                 : wf2g_fast_kernel_ptr(cigar, G, W);
   if (!fn) return WF2G_ERR_CUDA_;
   fp.g = g;
   fp.match = cfg.match;

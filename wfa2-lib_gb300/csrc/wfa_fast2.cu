@@ -77,9 +77,14 @@ __device__ __forceinline__ uint32_t pack16x2(int lo, int hi) {
 // Kernel of the two-diagonals-per-lane fast pass.  CIGAR: full alignment or
 // score only.  MOS: o+e (scaled) is even, so M[s-o-e] shares the output
 // rows' parity.  W: elements per shared-memory row (diagonals
-// [4-W/2, W/2-4] are computed).
-template <bool CIGAR, bool MOS, int W>
+// [4-W/2, W/2-4] are computed).  D241: the scaled penalties are the
+// default's (x, o+e, e) = (2, 4, 1), compiled in (rings of 4 M rows and 1 I
+// and D row).
+template <bool CIGAR, bool MOS, int W, bool D241>
 __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
+  static_assert(!D241 || MOS, "o+e = 4 is even");
+  const int X = D241 ? 2 : p.x, OE = D241 ? 4 : p.oe, E = D241 ? 1 : p.e;
+  const int R = D241 ? 4 : p.R, RI = D241 ? 1 : p.RI;
   constexpr int HALF = W / 2;
   constexpr int JM = (HALF + 63) / 64;  // most iterations of a step (64 words each)
   constexpr int RW = JM * 16;           // 32-bit choice words per step (16 bits per lane per iteration)
@@ -88,7 +93,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
   constexpr int kBig = 1 << 20;
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x;
-  const int nrows = p.R + 2 * p.RI;
+  const int nrows = R + 2 * RI;
   int16_t* const rows = reinterpret_cast<int16_t*>(smem + p.rows_off);
   uint32_t* const rows32 = reinterpret_cast<uint32_t*>(smem + p.rows_off);
   // the two sequences' word pairs interleaved at the start of shared
@@ -101,7 +106,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
   uint32_t* const codes = reinterpret_cast<uint32_t*>(slice);
   short2* const tab = reinterpret_cast<short2*>(slice + (int64_t)p.s_cap * RW * 4);
   uint8_t* const items = slice + p.items_off;
-  const int rowI = p.R, rowD = p.R + p.RI;
+  const int rowI = R, rowD = R + RI;
 
   for (int i = lane; i < nrows * WW; i += 32) rows32[i] = 0x80008000u;
   int used_lo = 0, used_hi = -1;  // words of every row the previous pair touched
@@ -169,11 +174,11 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       }
       ++s;
       const int par = s & 1;
-      cM = (cM + 1 == p.R) ? 0 : cM + 1;
-      cI = (cI + 1 == p.RI) ? 0 : cI + 1;
-      const int sMx = cM - p.x < 0 ? cM - p.x + p.R : cM - p.x;
-      const int sMo = cM - p.oe < 0 ? cM - p.oe + p.R : cM - p.oe;
-      const int sIe = cI - p.e < 0 ? cI - p.e + p.RI : cI - p.e;
+      cM = (cM + 1 == R) ? 0 : cM + 1;
+      cI = (cI + 1 == RI) ? 0 : cI + 1;
+      const int sMx = cM - X < 0 ? cM - X + R : cM - X;
+      const int sMo = cM - OE < 0 ? cM - OE + R : cM - OE;
+      const int sIe = cI - E < 0 ? cI - E + RI : cI - E;
       // input limits (wavefront/wavefront_compute.c:306-352).  A score below
       // 0 is a null wavefront: its slot (s - d + R >= s for d <= R) has not
       // been written for this pair yet and still holds the empty range.
@@ -187,10 +192,14 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       const int bM = cM * W + HALF - par;
       const int bI = (rowI + cI) * W + HALF - par;
       const int bD = (rowD + cI) * W + HALF - par;
-      const int obM = cM * W + HALF - ((s - p.R) & 1);
-      const int obI = (rowI + cI) * W + HALF - ((s - p.RI) & 1);
-      const int obD = (rowD + cI) * W + HALF - ((s - p.RI) & 1);
-      const int2 oldM = meta[cM], oldI = meta[rowI + cI], oldD = meta[rowD + cI];
+      const int obM = cM * W + HALF - ((s - R) & 1);
+      const int obI = (rowI + cI) * W + HALF - ((s - RI) & 1);
+      const int obD = (rowD + cI) * W + HALF - ((s - RI) & 1);
+      // the output slots' previous contents (the inputs themselves when the
+      // ring is exactly as long as their distance)
+      const int2 oldM = (R == OE) ? eMo : meta[cM];
+      const int2 oldI = (RI == E) ? eI : meta[rowI + cI];
+      const int2 oldD = (RI == E) ? eD : meta[rowD + cI];
       // output range: union of the inputs' (wavefront/wavefront_compute.c:40-87)
       const int lo = min(min(eMx.x, eMo.x - 1), min(eI.x + 1, eD.x - 1));
       const int hi = max(max(eMx.y, eMo.y + 1), max(eI.y + 1, eD.y - 1));
@@ -208,7 +217,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         __syncwarp();
         // more null steps than the scope: the end is unreachable
         // (wavefront/wavefront_extend.c:95-101), left to the general kernel
-        if (++null_steps > p.R + 1) {
+        if (++null_steps > R + 1) {
           leave = true;
           break;
         }
@@ -358,7 +367,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         if (aL > hi) rows[bM + aL] = rows[bI + aL] = rows[bD + aL] = kNull16;
       }
       {
-        const int shM = par - ((s - p.R) & 1), shI = par - ((s - p.RI) & 1);
+        const int shM = par - ((s - R) & 1), shI = par - ((s - RI) & 1);
         const bool cM_ = oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
         const bool cI_ = oldI.x <= oldI.y && (oldI.x + shI < a0 || oldI.y + shI > aL);
         const bool cD_ = oldD.x <= oldD.y && (oldD.x + shI < a0 || oldD.y + shI > aL);
@@ -497,13 +506,18 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
 
 }  // namespace wf2g
 
-// Kernel of the two-diagonals-per-lane pass for (full CIGAR?, o+e even?, row width).
-extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width) {
+// Kernel of the two-diagonals-per-lane pass for (full CIGAR?, o+e even?, row
+// width, default scaled penalties (2, 4, 1)?).
+extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241) {
   using namespace wf2g;
-#define WF2G_FAST2_CASE(W)                                                                   \
-  if (width == W) {                                                                          \
-    if (mos) return cigar ? (void*)wfa_fast2_kernel<true, true, W> : (void*)wfa_fast2_kernel<false, true, W>; \
-    return cigar ? (void*)wfa_fast2_kernel<true, false, W> : (void*)wfa_fast2_kernel<false, false, W>;        \
+#define WF2G_FAST2_CASE(W)                                                                        \
+  if (width == W) {                                                                               \
+    if (d241) return cigar ? (void*)wfa_fast2_kernel<true, true, W, true>                         \
+                           : (void*)wfa_fast2_kernel<false, true, W, true>;                       \
+    if (mos) return cigar ? (void*)wfa_fast2_kernel<true, true, W, false>                         \
+                          : (void*)wfa_fast2_kernel<false, true, W, false>;                       \
+    return cigar ? (void*)wfa_fast2_kernel<true, false, W, false>                                 \
+                 : (void*)wfa_fast2_kernel<false, false, W, false>;                               \
   }
   WF2G_FAST2_CASE(1024)
   WF2G_FAST2_CASE(2048)
