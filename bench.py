@@ -37,9 +37,9 @@ INT_OPS_PER_EXT_WORD = 8   # per additional 32-base extend word
 MEM_HIGH, MEM_ULTRALOW = 0, 3
 # DRAM bytes (read + write) per pair of the dominant kernel, from one ncu
 # capture of a 20,000-pair launch of the first fast pass on the headline
-# workload (dram__bytes_read.sum + dram__bytes_write.sum = 0.1223 + 0.7793 GB;
-# profiles/wfa_fast_kernel_workload1.md), scaled to a launch by its pairs
-TRAFFIC_BYTES_PER_PAIR = {(1, False): 901.58e6 / 20000}
+# workload (dram__bytes_read.sum + dram__bytes_write.sum = 0.1806 + 0.7180 GB;
+# profiles/wfa_fast2_kernel_workload1.md), scaled to a launch by its pairs
+TRAFFIC_BYTES_PER_PAIR = {(1, False): 898.60e6 / 20000}
 
 # The benchmark configurations: workload of the seeded generator, pairs per
 # GPU, distance metric, memory mode, pairs of the per-pair drop-in sample and
@@ -477,8 +477,12 @@ def main():
         h_opsoff = torch.empty(n + 1, dtype=torch.int64, pin_memory=True).numpy()
         h_opsoff[...] = ops_off
 
+        # the host API as a caller uses it: its own aligner, host buffers in,
+        # host buffers out
+        al_h = W.Aligner(cfg)
+
         def step_host():
-            rc = al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len,
+            rc = al_h.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len,
                                 ops_off=h_opsoff if cigar else None, scores=h_scores,
                                 status=h_status, ops=h_ops if cigar else None,
                                 ops_len=h_opslen if cigar else None)[0]
@@ -491,6 +495,7 @@ def main():
         for _ in range(args.steps):
             step_host()
         e2e_s = time.perf_counter() - t0
+        al_h.close()
         if dist:
             t = torch.tensor([e2e_s], device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)

@@ -36,7 +36,7 @@ def _served(metric, score_only, strategy, memory_mode=0):
     """The GPU's refusals (make_cfg in wfa2-lib_gb300/csrc/wfa_aligner.c)."""
     if memory_mode == 3 and strategy & ~0x04:  # BiWFA: wf-adaptive or none
         return False
-    return not (strategy & 0x20 and (not score_only or metric == 4))
+    return not (strategy & 0x20 and not score_only and metric == 4)  # z-drop, affine2p, CIGAR
 
 
 def _gpu(W, cfg, b):
@@ -140,9 +140,7 @@ def test_heuristic_rejections(gpu_available, wfa):
     p = W.generate(1, 4, first=3)
     for cfg in [W.Config(metric=W.EDIT, heuristic=dict(strategy=0x10, xdrop=20)),
                 W.Config(metric=W.INDEL, heuristic=dict(strategy=0x20, zdrop=20)),
-                W.Config(heuristic=dict(strategy=0x20, zdrop=20)),
-                W.Config(metric=W.GAP_AFFINE_2P, score_only=True,
-                         heuristic=dict(strategy=0x20, zdrop=20)),
+                W.Config(metric=W.GAP_AFFINE_2P, heuristic=dict(strategy=0x20, zdrop=20)),
                 W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x01, min_k=-9,
                                                                     max_k=9))]:
         al = W.Aligner(cfg)

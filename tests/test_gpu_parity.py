@@ -202,3 +202,27 @@ def test_unsupported_configurations_fail_loudly(gpu_available, wfa):
     st, score, ops = al.align(b"ACGT", b"ACGA")
     assert st == 0 and score == -4 and ops == "MMMX"
     al.close()
+
+
+def test_drop_in_long_affine2p_pairs(gpu_available, wfa, oracle_mod):
+    """wavefront_align() one pair at a time on 5-10 kbp gap-affine-2p pairs
+    (whose back-traces take tens of MB) gives the batch call's results, which
+    are the checker's: a single-pair call must not report WF_STATUS_OOM where
+    the batch completes."""
+    W, O = wfa, oracle_mod
+    p = W.generate(2, 40, first=0)
+    cfg = W.Config(metric=W.GAP_AFFINE_2P)
+    al = W.Aligner(cfg)
+    rc, scores, status, ops, ops_len, ops_off = al.align_batch(p.seqs, p.p_off, p.p_len,
+                                                               p.t_off, p.t_len)
+    assert rc == 0 and (status == 0).all()
+    for i in range(p.n):
+        st, score, cig = al.align(p.pattern(i), p.text(i))
+        assert (st, score) == (0, int(scores[i])), i
+        assert cig == ops[ops_off[i]:ops_off[i] + ops_len[i]].tobytes().decode(), i
+    al.close()
+    idx = [9, 17]  # two of the longest pairs of the sample
+    b = O.PairBatch.from_lists([p.pattern(i) for i in idx], [p.text(i) for i in idx])
+    r = O.align(b, O.Penalties(metric=4), nthreads=8)
+    for j, i in enumerate(idx):
+        assert int(r.score[j]) == int(scores[i]), i

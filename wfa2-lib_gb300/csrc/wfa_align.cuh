@@ -1410,7 +1410,10 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         const BtRow te = table[ss];
         if (zfirst) {
           zfirst = false;
-          if (te.width <= 0 || kk < te.lo || kk - te.lo >= te.width) {
+          // The first step always takes the reference's candidates from the
+          // sources: the best cell's diagonal may hold no cell at this score,
+          // or an out-of-bounds one whose choice byte compares NULL inputs.
+          {
             // candidates as the reference packs them: (offset << 4) | type,
             // larger wins (wavefront/wavefront_backtrace.c:36-59)
             auto cand = [&](int back, int r, int k, int add, int type) -> int64_t {

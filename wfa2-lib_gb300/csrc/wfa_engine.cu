@@ -476,10 +476,14 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
       std::max<int64_t>(int64_t(1) << 20, ((4 * (int64_t)max_len + 64) + 4095) & ~int64_t(4095));
   const int64_t pool_cap =
       E->pool_budget >= 0 ? E->pool_budget : (int64_t)env_int("WF2G_POOL_MB", 48 << 10) << 20;
-  // sized for the batch: a one-pair call takes a small pool, a large batch the budget
+  // sized for the batch: up to 64 MB per pair in flight, and at least what
+  // one pair may need up to 1 GB, so a small call (the drop-in's single
+  // pair) can hold a long pair's whole back-trace
   const int64_t per_pair = std::max(2 * block_bytes, std::min<int64_t>(need, int64_t(64) << 20));
   const int64_t pool_bytes = std::max(
-      2 * block_bytes, std::min(pool_cap, (int64_t)std::min(n, 8 * E->num_sms * 8) * per_pair));
+      2 * block_bytes,
+      std::min(pool_cap, std::max(std::min<int64_t>(need, int64_t(1) << 30),
+                                  (int64_t)std::min(n, 8 * E->num_sms * 8) * per_pair)));
   const int nblocks = (int)std::min<int64_t>(pool_bytes / block_bytes, INT32_MAX / 2);
   if (ensure(E->pool, (size_t)nblocks * block_bytes) ||
       ensure(E->poolctl, ((size_t)nblocks + 64) * sizeof(int32_t)))

@@ -37,8 +37,7 @@
 // mismatch" (M[s-x]+1 >= max(I, D)), bit 1 "deletion over insertion"
 // (D >= I), bit 2 "insertion extended" (I[s-e] >= M[s-o-e] at k-1), bit 3
 // "deletion extended".  A lane writes one 16-bit entry per iteration (its
-// two words' four cells).  M cells out of bounds are stored with the sign
-// bit set (far below 0), not as the exact NULL.
+// two words' four cells).
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -312,12 +311,12 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
           }
         }
         // extended offset, capped at min(plen + k, tlen) (the end of the
-        // shorter rest).  Out of bounds the sign bit is set: mext is then at
-        // most tlen or already below -2^14, so the cell stays far below 0
-        // (NULL-ish) for every later step.
+        // shorter rest); NULL out of bounds (exactly: the cap can be -1 on
+        // diagonal -plen-1, where a set sign bit alone would leave -1)
         const uint32_t capv = vmin_s16x2(kvp, tlen2);
         const uint32_t mext = vmin_s16x2(vadd_s16x2(best, (uint32_t)L0c | ((uint32_t)L1c << 16)), capv);
-        oM[q] = mext | (vmin_u16x2(oob, 0x00010001u) << 15);
+        const uint32_t nullm = vmin_u16x2(oob, 0x00010001u) * 0xFFFFu;
+        oM[q] = (mext & ~nullm) | (0x80008000u & nullm);
         oI[q] = i1;
         oD[q] = d1;
         if (!CIGAR) return 0u;
@@ -383,12 +382,12 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       }
       __syncwarp();
       // first/last in-bounds cell per component (wavefront/wavefront_compute.c:
-      // 579-613): M is not negative (over [lo, hi]); I has h <= tlen and D has
+      // 579-613): M is not NULL (over [lo, hi]); I has h <= tlen and D has
       // h - k <= plen (over their natural ranges).  Lanes 0-5 test the six
       // end cells; only a component with an end out of bounds is scanned.
       auto inb = [&](int comp, int k) -> bool {
         const int v = rows[(comp == 0 ? bM : comp == 1 ? bI : bD) + k];
-        return comp == 0 ? v >= 0
+        return comp == 0 ? v != kNull16
                          : comp == 1 ? (uint32_t)v <= (uint32_t)tlen : (uint32_t)(v - k) <= (uint32_t)plen;
       };
       const bool iE = iLo > iHi, dE = dLo > dHi;  // no I (D) cell has a source
