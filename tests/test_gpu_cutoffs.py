@@ -34,9 +34,7 @@ def _spec(name):
 
 def _served(metric, score_only, strategy, memory_mode=0):
     """The GPU's refusals (make_cfg in wfa2-lib_gb300/csrc/wfa_aligner.c)."""
-    if memory_mode == 3 and strategy & ~0x04:  # BiWFA: wf-adaptive or none
-        return False
-    return not (strategy & 0x20 and not score_only and metric == 4)  # z-drop, affine2p, CIGAR
+    return not (memory_mode == 3 and strategy & ~0x04)  # BiWFA: wf-adaptive or none
 
 
 def _gpu(W, cfg, b):
@@ -140,7 +138,6 @@ def test_heuristic_rejections(gpu_available, wfa):
     p = W.generate(1, 4, first=3)
     for cfg in [W.Config(metric=W.EDIT, heuristic=dict(strategy=0x10, xdrop=20)),
                 W.Config(metric=W.INDEL, heuristic=dict(strategy=0x20, zdrop=20)),
-                W.Config(metric=W.GAP_AFFINE_2P, heuristic=dict(strategy=0x20, zdrop=20)),
                 W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x01, min_k=-9,
                                                                     max_k=9))]:
         al = W.Aligner(cfg)
@@ -150,3 +147,29 @@ def test_heuristic_rejections(gpu_available, wfa):
         assert st == W.WF_STATUS_UNATTAINABLE
     with pytest.raises(RuntimeError):
         W.Server(W.Config(heuristic=dict(strategy=0x10, xdrop=20)))
+
+
+@pytest.mark.parametrize("case", CASES[:2])
+@pytest.mark.parametrize("spec_name", ["linear", "linear.m1", "affine", "affine2p"])
+def test_zdrop_full_alignment_matches_oracle(gpu_available, wfa, oracle_mod, case, spec_name):
+    """z-drop with a full alignment on gap-linear, gap-affine and
+    gap-affine-2p (match 0 and < 0): the walk from the best cell (its first step from the sources of the
+    current score, wavefront/wavefront_backtrace.c:62-219), the gaps to both
+    ends and the maximal-score trim, against the checker."""
+    W, O = wfa, oracle_mod
+    wl, n, param, param2 = case
+    spec = _spec(spec_name)
+    p = W.generate(wl, n, param=param, param2=param2)
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    hs = dict(strategy=0x20, zdrop=60, steps_between_cutoffs=1)
+    ref = _oracle_flags(O, spec, b, False, None, hs)
+    got = _gpu(W, W.Config(**spec, heuristic=hs), b)
+    compared = 0
+    for i in range(b.n):
+        if ref.flags[i] & (O.FLAG_STALE_SOURCE | O.FLAG_OVER_BOUND):
+            continue
+        want = (int(ref.status[i]), int(ref.score[i]), ref.cigar(i), int(ref.end[i][0]),
+                int(ref.end[i][1]))
+        assert got[i] == want, (spec_name, case, i)
+        compared += 1
+    assert compared >= b.n // 2, (spec_name, compared)

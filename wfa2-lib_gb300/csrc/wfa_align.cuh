@@ -1410,6 +1410,11 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
         const BtRow te = table[ss];
         if (zfirst) {
           zfirst = false;
+          // The reference's walk runs while v > 0 and h > 0
+          // (wavefront/wavefront_backtrace.c:358): from a best cell on
+          // the first row or column it takes no step, and its CIGAR is the
+          // end gaps alone.
+          if (end_v <= 0 || end_h <= 0) break;
           // The first step always takes the reference's candidates from the
           // sources: the best cell's diagonal may hold no cell at this score,
           // or an out-of-bounds one whose choice byte compares NULL inputs.

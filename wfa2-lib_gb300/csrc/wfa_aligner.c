@@ -322,12 +322,6 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   /* BiWFA is computed with the wf-adaptive cut-off or none */
   if (wf->memory_mode == wavefront_memory_ultralow && (strategy & ~wf_heuristic_wfadaptive))
     return -1;
-  /* not computed on the GPU yet: z-drop with gap-affine-2p and a full
-   * alignment (its first back-trace step differs from the reference's on
-   * some pairs) */
-  if ((strategy & wf_heuristic_zdrop) && wf->alignment_scope == compute_alignment &&
-      p->distance_metric == gap_affine_2p)
-    return -1;
   cfg->metric = (int)p->distance_metric;
   cfg->match = p->match;
   cfg->x = p->mismatch;

@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       }
       w_lo = min(w_lo, lo);
       w_hi = max(w_hi, hi);
-      if (CIGAR && lane == 0) tab[s] = make_short2((short)lo, (short)hi);
+      // (every lane stores the same value: no divergent branch per step)
+      if (CIGAR) tab[s] = make_short2((short)lo, (short)hi);
       // the natural ranges of I (sources at k-1) and D (sources at k+1): the
       // cells of [lo, hi] outside them are computed from NULL or NULL-ish
       // (negative) inputs only, so they come out negative, out of bounds
@@ -361,10 +362,8 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       // sits one element off when s' has the other parity: in this step's
       // diagonals it spans [x + sh, y + sh], sh = (s & 1) - (s' & 1).
       const int aL = a0 + 2 * nq - 1;
-      if (lane == 0) {
-        if (a0 < lo) rows[bM + a0] = rows[bI + a0] = rows[bD + a0] = kNull16;
-        if (aL > hi) rows[bM + aL] = rows[bI + aL] = rows[bD + aL] = kNull16;
-      }
+      if (a0 < lo) rows[bM + a0] = rows[bI + a0] = rows[bD + a0] = kNull16;
+      if (aL > hi) rows[bM + aL] = rows[bI + aL] = rows[bD + aL] = kNull16;
       {
         const int shM = par - ((s - R) & 1), shI = par - ((s - RI) & 1);
         const bool cM_ = oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
@@ -391,13 +390,11 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
                          : comp == 1 ? (uint32_t)v <= (uint32_t)tlen : (uint32_t)(v - k) <= (uint32_t)plen;
       };
       const bool iE = iLo > iHi, dE = dLo > dHi;  // no I (D) cell has a source
-      bool endok = true;
-      if (lane < 6) {
-        const int comp = lane >> 1, hiend = lane & 1;
-        const int k = comp == 0 ? (hiend ? hi : lo) : comp == 1 ? (hiend ? iHi : iLo) : (hiend ? dHi : dLo);
-        if (!(comp == 1 && iE) && !(comp == 2 && dE)) endok = inb(comp, k);
-      }
-      const uint32_t ends = __ballot_sync(kFull, lane < 6 && endok);
+      // (lanes 6-31 repeat lane 4's and 5's test, so no lane branches)
+      const int comp = min(lane >> 1, 2), hiend = lane & 1;
+      const int kend = comp == 0 ? (hiend ? hi : lo) : comp == 1 ? (hiend ? iHi : iLo) : (hiend ? dHi : dLo);
+      const bool endok = (comp == 1 && iE) || (comp == 2 && dE) || inb(comp, kend);
+      const uint32_t ends = __ballot_sync(kFull, endok) & 0x3Fu;
       int fM = lo, lM = hi;
       int fI = iE ? INT_MAX : iLo, lI = iE ? INT_MIN : iHi;
       int fD = dE ? INT_MAX : dLo, lD = dE ? INT_MIN : dHi;
@@ -439,11 +436,9 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
           for (int q = lane; q < nR; q += 32) rows[bD + dHi - q] = kNull16;
         }
       }
-      if (lane == 0) {
-        meta[cM] = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
-        meta[rowI + cI] = fI == INT_MAX ? kEmpty : make_int2(fI, lI);
-        meta[rowD + cI] = fD == INT_MAX ? kEmpty : make_int2(fD, lD);
-      }
+      meta[cM] = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
+      meta[rowI + cI] = fI == INT_MAX ? kEmpty : make_int2(fI, lI);
+      meta[rowD + cI] = fD == INT_MAX ? kEmpty : make_int2(fD, lD);
       // termination on M[s] at k_end (wavefront/wavefront_termination.c:37-60)
       done = fM <= k_end && k_end <= lM && rows[bM + k_end] >= tlen;
       __syncwarp();
