@@ -576,6 +576,12 @@ static int host_small(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seqs,
   if (ensure_hstage(E, in_bytes + out_bytes) || ensure(E->dstage, in_bytes) ||
       ensure(E->dout, out_bytes))
     return WF2G_ERR_OOM_;
+  // diagnostics: WF2G_TIMING=2 prints the phases of every small call
+  const bool timing = env_int("WF2G_TIMING", 0) >= 2;
+  const double t0 = timing ? wall_s() : 0.0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  if (timing)
+    for (auto& x : ev) cudaEventCreate(&x);
   uint8_t* const h = (uint8_t*)E->hstage;
   memcpy(h, p_off, n8);
   memcpy(h + i_toff, t_off, n8);
@@ -587,6 +593,8 @@ static int host_small(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seqs,
   uint8_t* const q = (uint8_t*)E->dout.p;
   if (cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return WF2G_ERR_CUDA_;
+  const double t1 = timing ? wall_s() : 0.0;
+  if (timing) cudaEventRecord(ev[0], st);
   const int rc = plan_and_run(
       E, cfg, n, (const char*)(d + i_seqs), (const int64_t*)d, (const int32_t*)(d + i_plen),
       (const int64_t*)(d + i_toff), (const int32_t*)(d + i_tlen), mlen, (int32_t*)q,
@@ -594,9 +602,20 @@ static int host_small(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seqs,
       cigar ? (const int64_t*)(d + i_opsoff) : nullptr, cigar ? (int32_t*)(q + o_opslen) : nullptr,
       nullptr, nullptr, 0, end_info ? (int32_t*)(q + o_end) : nullptr, st, true);
   if (rc) return rc;
+  if (timing) cudaEventRecord(ev[1], st);
+  const double t2 = timing ? wall_s() : 0.0;
   uint8_t* const ho = h + in_bytes;
   cudaError_t e = cudaMemcpyAsync(ho, q, out_bytes - 16, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (timing) {
+    float kms = 0;
+    cudaEventElapsedTime(&kms, ev[0], ev[1]);
+    fprintf(stderr,
+            "[wfa2gpu] small call (%d pairs): staging+copy in %.1f us, plan %.1f us, "
+            "copy out+wait %.1f us; kernels %.1f us\n",
+            n, 1e6 * (t1 - t0), 1e6 * (t2 - t1), 1e6 * (wall_s() - t2), 1e3 * kms);
+    for (auto& x : ev) cudaEventDestroy(x);
+  }
   if (e != cudaSuccess) {
     fprintf(stderr, "[wfa2gpu] CUDA error: %s\n", cudaGetErrorString(e));
     return WF2G_ERR_CUDA_;
@@ -631,9 +650,9 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
   if (cigar && (ensure(E->ops, (size_t)ops_end + 16) || ensure(E->opsoff, n8) || ensure(E->opslen, n4)))
     return WF2G_ERR_OOM_;
   if (end_info && ensure(E->endinfo, 3 * n4)) return WF2G_ERR_OOM_;
-  // chunks of at least 16k pairs, at most 8; one chunk when the CIGAR regions
+  // chunks of at least 16k pairs, at most 16; one chunk when the CIGAR regions
   // are not in pair order (the chunks' copies back could overlap)
-  const int want_chunks = std::max(1, std::min(env_int("WF2G_CHUNKS", 8), 64));
+  const int want_chunks = std::max(1, std::min(env_int("WF2G_CHUNKS", 16), 64));
   const int64_t chunk = std::max<int64_t>(16384, ((int64_t)n + want_chunks - 1) / want_chunks);
   int nchunks = (int)(((int64_t)n + chunk - 1) / chunk);
   if (cigar && !ops_ordered) nchunks = 1;
