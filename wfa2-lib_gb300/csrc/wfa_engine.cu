@@ -339,8 +339,9 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
   // counters: [0..3] work queues of passes 1-4, [4..6] retry counts of passes 1-3
   // (retry lists: pass q writes list q-1, at retry + (q-1) * n), [8]/[9] work
   // queue and retry count of the first fast pass (its list at retry + 3 * n),
-  // [10]/[11] those of the second (its list at retry + 4 * n)
-  if (ensure(E->counters, 16 * sizeof(int32_t)) || ensure(E->retry, (size_t)5 * n * sizeof(int32_t)))
+  // [10]/[11] those of the second (its list at retry + 4 * n), [12]/[13]
+  // those of the third (its list at retry + 5 * n)
+  if (ensure(E->counters, 16 * sizeof(int32_t)) || ensure(E->retry, (size_t)6 * n * sizeof(int32_t)))
     return WF2G_ERR_OOM_;
   int32_t* counters = (int32_t*)E->counters.p;
   int32_t* retry = (int32_t*)E->retry.p;
@@ -363,16 +364,32 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
     if (rc < 0) return rc;
     fast = (rc == 0);
     if (fast && env_int("WF2G_FAST_WIDE", 1)) {
+      // the pairs pass 1 left: rows of 1536 diagonals with a warp per pair
+      // (10 pairs per SM; they cover every pair of the headline workload),
+      // then 2048 for what remains (four warps per pair on small batches)
       const int gw = n <= small_n ? 128 : env_int("WF2G_FAST_WIDE_G", 32);
       const int g2 = gw <= 32 ? 32 : gw <= 64 ? 64 : 128;
-      rc = run_fast_pass(E, cfg, g2, 2048, n, retry + (size_t)3 * n, counters + 9, d_seqs, d_poff,
-                         d_plen, d_toff, d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff,
-                         d_opslen, d_end_info, counters + 10, retry + (size_t)4 * n,
-                         counters + 11, E->scratch0b, st);
+      const int w2 = g2 == 32 ? env_int("WF2G_FAST_W2", 1536) : 2048;
+      rc = run_fast_pass(E, cfg, g2, w2 == 1536 ? 1536 : 2048, n, retry + (size_t)3 * n,
+                         counters + 9, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len, d_scores,
+                         d_status, d_ops, d_opsoff, d_opslen, d_end_info, counters + 10,
+                         retry + (size_t)4 * n, counters + 11, E->scratch0b, st);
       if (rc < 0) return rc;
       if (rc == 0) {
         fast_left = retry + (size_t)4 * n;
         fast_left_n = counters + 11;
+        if (w2 == 1536) {
+          // pass 1 has finished on this stream: its scratch is free
+          rc = run_fast_pass(E, cfg, 32, 2048, n, retry + (size_t)4 * n, counters + 11, d_seqs,
+                             d_poff, d_plen, d_toff, d_tlen, max_len, d_scores, d_status, d_ops,
+                             d_opsoff, d_opslen, d_end_info, counters + 12, retry + (size_t)5 * n,
+                             counters + 13, E->scratch0, st);
+          if (rc < 0) return rc;
+          if (rc == 0) {
+            fast_left = retry + (size_t)5 * n;
+            fast_left_n = counters + 13;
+          }
+        }
       }
     }
     // (diagnostics: WF2G_VERBOSE=1 reads the count too, which waits for the

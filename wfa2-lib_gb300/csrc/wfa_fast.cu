@@ -525,6 +525,7 @@ extern "C" void* wf2g_fast_kernel_ptr(int cigar, int group, int width) {
   if (group == G && width == W) \
     return cigar ? (void*)wfa_fast_kernel<true, G, W> : (void*)wfa_fast_kernel<false, G, W>;
   WF2G_FAST_CASE(32, 1024)
+  WF2G_FAST_CASE(32, 1536)
   WF2G_FAST_CASE(32, 2048)
   WF2G_FAST_CASE(64, 1024)
   WF2G_FAST_CASE(64, 2048)

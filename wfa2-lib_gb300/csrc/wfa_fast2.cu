@@ -514,6 +514,7 @@ extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241) 
                  : (void*)wfa_fast2_kernel<false, false, W, false>;                               \
   }
   WF2G_FAST2_CASE(1024)
+  WF2G_FAST2_CASE(1536)
   WF2G_FAST2_CASE(2048)
 #undef WF2G_FAST2_CASE
   return nullptr;
