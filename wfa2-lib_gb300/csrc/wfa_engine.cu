@@ -107,6 +107,12 @@ extern "C" void wf2g_engine_free(void* engine) {
   if (E->hstage) cudaFreeHost(E->hstage);
   bi_state_free(E->bi);
   if (E->stream) cudaStreamDestroy(E->stream);
+  if (E->copy_in) cudaStreamDestroy(E->copy_in);
+  if (E->copy_out) cudaStreamDestroy(E->copy_out);
+  for (int c = 0; c < 64; ++c) {
+    if (E->ev_in[c]) cudaEventDestroy(E->ev_in[c]);
+    if (E->ev_done[c]) cudaEventDestroy(E->ev_done[c]);
+  }
   if (E->twin) wf2g_engine_free(E->twin);
   delete E;
 }
@@ -686,16 +692,39 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
   const int64_t twin0 = E->twin ? E->twin->launches : 0;
   const int64_t per = ((int64_t)n + nchunks - 1) / nchunks;
   uint8_t* const dseq = (uint8_t*)E->seqs.p;
-  // diagnostics: WF2G_TIMING=1 times the first chunk's copies and kernels
+  // Copies in run back to back on their own stream, ahead of the kernels;
+  // chunk c's kernels (on this engine's stream or the second engine's, in
+  // turn) wait for its copies in, and its copies out (on a third stream)
+  // wait for its kernels.  So neither direction of copies waits for the
+  // other chunks' kernels, only for its own chunk.
+  if (!E->copy_in && cudaStreamCreateWithFlags(&E->copy_in, cudaStreamNonBlocking) != cudaSuccess)
+    return WF2G_ERR_CUDA_;
+  if (!E->copy_out && cudaStreamCreateWithFlags(&E->copy_out, cudaStreamNonBlocking) != cudaSuccess)
+    return WF2G_ERR_CUDA_;
+  for (int c = 0; c < nchunks; ++c) {
+    if (!E->ev_in[c] && cudaEventCreateWithFlags(&E->ev_in[c], cudaEventDisableTiming) != cudaSuccess)
+      return WF2G_ERR_CUDA_;
+    if (!E->ev_done[c] && cudaEventCreateWithFlags(&E->ev_done[c], cudaEventDisableTiming) != cudaSuccess)
+      return WF2G_ERR_CUDA_;
+  }
+  // diagnostics: WF2G_TIMING=1 times the first chunk's copies in, kernels
+  // and copies out (each on its own stream)
   const bool timing = env_int("WF2G_TIMING", 0) != 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {};
   if (timing)
     for (auto& x : ev) cudaEventCreate(&x);
-  for (int c = 0; c < nchunks; ++c) {
+  // the stream the caller's batch is ordered on waits for nothing of ours
+  // yet: the copies in start after what the caller queued there
+  cudaEvent_t ev_start = E->ev_done[0];
+  if (cudaEventRecord(ev_start, st) != cudaSuccess ||
+      cudaStreamWaitEvent(E->copy_in, ev_start, 0) != cudaSuccess)
+    return WF2G_ERR_CUDA_;
+  int chunk_ml[64];
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < nchunks && e == cudaSuccess; ++c) {
     const int a = (int)(c * per), b = (int)std::min<int64_t>(n, (c + 1) * per);
+    chunk_ml[c] = 0;
     if (a >= b) break;
-    Engine* const Ec = (c & 1) ? E->twin : E;
-    const cudaStream_t sc = (c & 1) ? E->twin->stream : st;
     const int m = b - a;
     int64_t smin = INT64_MAX, smax = 0;
     int ml = 0;
@@ -704,50 +733,69 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
       smax = std::max(smax, std::max(p_off[i] + p_len[i], t_off[i] + t_len[i]));
       ml = std::max(ml, std::max(p_len[i], t_len[i]));
     }
+    chunk_ml[c] = ml;
     if (smin > smax) smin = smax;
     const size_t m4 = (size_t)m * 4, m8 = (size_t)m * 8;
-    cudaError_t e = cudaSuccess;
-    if (timing && c == 0) cudaEventRecord(ev[0], sc);
+    const cudaStream_t ci = E->copy_in;
+    if (timing && c == 0) cudaEventRecord(ev[0], ci);
     if (smax > smin)
-      e = cudaMemcpyAsync(dseq + smin, seqs + smin, (size_t)(smax - smin), cudaMemcpyHostToDevice, sc);
-    if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->poff.p + a, p_off + a, m8, cudaMemcpyHostToDevice, sc);
-    if (e == cudaSuccess) e = cudaMemcpyAsync((int32_t*)E->plen.p + a, p_len + a, m4, cudaMemcpyHostToDevice, sc);
-    if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->toff.p + a, t_off + a, m8, cudaMemcpyHostToDevice, sc);
-    if (e == cudaSuccess) e = cudaMemcpyAsync((int32_t*)E->tlen.p + a, t_len + a, m4, cudaMemcpyHostToDevice, sc);
+      e = cudaMemcpyAsync(dseq + smin, seqs + smin, (size_t)(smax - smin), cudaMemcpyHostToDevice, ci);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->poff.p + a, p_off + a, m8, cudaMemcpyHostToDevice, ci);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int32_t*)E->plen.p + a, p_len + a, m4, cudaMemcpyHostToDevice, ci);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int64_t*)E->toff.p + a, t_off + a, m8, cudaMemcpyHostToDevice, ci);
+    if (e == cudaSuccess) e = cudaMemcpyAsync((int32_t*)E->tlen.p + a, t_len + a, m4, cudaMemcpyHostToDevice, ci);
     if (cigar && e == cudaSuccess)
-      e = cudaMemcpyAsync((int64_t*)E->opsoff.p + a, ops_off + a, m8, cudaMemcpyHostToDevice, sc);
-    if (e != cudaSuccess) return WF2G_ERR_CUDA_;
-    if (timing && c == 0) cudaEventRecord(ev[1], sc);
+      e = cudaMemcpyAsync((int64_t*)E->opsoff.p + a, ops_off + a, m8, cudaMemcpyHostToDevice, ci);
+    if (timing && c == 0) cudaEventRecord(ev[1], ci);
+    if (e == cudaSuccess) e = cudaEventRecord(E->ev_in[c], ci);
+  }
+  if (e != cudaSuccess) return WF2G_ERR_CUDA_;
+  for (int c = 0; c < nchunks; ++c) {
+    const int a = (int)(c * per), b = (int)std::min<int64_t>(n, (c + 1) * per);
+    if (a >= b) break;
+    Engine* const Ec = (c & 1) ? E->twin : E;
+    const cudaStream_t sc = (c & 1) ? E->twin->stream : st;
+    const int m = b - a;
+    const size_t m4 = (size_t)m * 4;
+    if (cudaStreamWaitEvent(sc, E->ev_in[c], 0) != cudaSuccess) return WF2G_ERR_CUDA_;
+    if (timing && c == 0) cudaEventRecord(ev[2], sc);
     const int rc = plan_and_run(
         Ec, cfg, m, (const char*)dseq, (const int64_t*)E->poff.p + a, (const int32_t*)E->plen.p + a,
-        (const int64_t*)E->toff.p + a, (const int32_t*)E->tlen.p + a, ml,
+        (const int64_t*)E->toff.p + a, (const int32_t*)E->tlen.p + a, chunk_ml[c],
         (int32_t*)E->scores.p + a, (int32_t*)E->status.p + a, cigar ? (char*)E->ops.p : nullptr,
         cigar ? (const int64_t*)E->opsoff.p + a : nullptr,
         cigar ? (int32_t*)E->opslen.p + a : nullptr, nullptr, nullptr, 0,
         end_info ? (int32_t*)E->endinfo.p + 3 * (size_t)a : nullptr, sc);
     if (rc) return rc;
-    if (timing && c == 0) cudaEventRecord(ev[2], sc);
-    e = cudaMemcpyAsync(scores + a, (int32_t*)E->scores.p + a, m4, cudaMemcpyDeviceToHost, sc);
+    if (timing && c == 0) cudaEventRecord(ev[3], sc);
+    const cudaStream_t co = E->copy_out;
+    e = cudaEventRecord(E->ev_done[c], sc);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(co, E->ev_done[c], 0);
+    if (timing && c == 0) cudaEventRecord(ev[4], co);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(status + a, (int32_t*)E->status.p + a, m4, cudaMemcpyDeviceToHost, sc);
+      e = cudaMemcpyAsync(scores + a, (int32_t*)E->scores.p + a, m4, cudaMemcpyDeviceToHost, co);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(status + a, (int32_t*)E->status.p + a, m4, cudaMemcpyDeviceToHost, co);
     if (end_info && e == cudaSuccess)
       e = cudaMemcpyAsync(end_info + 3 * (size_t)a, (int32_t*)E->endinfo.p + 3 * (size_t)a, 3 * m4,
-                          cudaMemcpyDeviceToHost, sc);
+                          cudaMemcpyDeviceToHost, co);
     if (cigar && e == cudaSuccess) {
-      e = cudaMemcpyAsync(ops_len + a, (int32_t*)E->opslen.p + a, m4, cudaMemcpyDeviceToHost, sc);
+      e = cudaMemcpyAsync(ops_len + a, (int32_t*)E->opslen.p + a, m4, cudaMemcpyDeviceToHost, co);
       // the chunk's CIGAR regions (the whole buffer when there is one chunk)
       const int64_t omin = nchunks == 1 ? 0 : ops_off[a];
       const int64_t omax =
           nchunks == 1 ? ops_end : ops_off[b - 1] + (int64_t)p_len[b - 1] + t_len[b - 1];
       if (e == cudaSuccess && omax > omin)
         e = cudaMemcpyAsync(ops + omin, (char*)E->ops.p + omin, (size_t)(omax - omin),
-                            cudaMemcpyDeviceToHost, sc);
+                            cudaMemcpyDeviceToHost, co);
     }
-    if (timing && c == 0) cudaEventRecord(ev[3], sc);
+    if (timing && c == 0) cudaEventRecord(ev[5], co);
     if (e != cudaSuccess) return WF2G_ERR_CUDA_;
   }
   const double t_enq = (env_int("WF2G_VERBOSE", 0) || env_int("WF2G_TIMING", 0)) ? wall_s() : 0.0;
-  cudaError_t e = cudaStreamSynchronize(st);
+  // the copies out of the last chunk follow every chunk's kernels
+  e = cudaStreamSynchronize(E->copy_out);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e == cudaSuccess && nchunks > 1) e = cudaStreamSynchronize(E->twin->stream);
   if (env_int("WF2G_VERBOSE", 0) || env_int("WF2G_TIMING", 0))
     fprintf(stderr, "[wfa2gpu] host batch: %d chunks, enqueue %.1f ms, wait %.1f ms\n", nchunks,
@@ -756,8 +804,8 @@ static int host_chunked(Engine* E, const wf2g_cfg_t& cfg, int n, const char* seq
   if (timing) {
     float a = 0, b = 0, c = 0;
     cudaEventElapsedTime(&a, ev[0], ev[1]);
-    cudaEventElapsedTime(&b, ev[1], ev[2]);
-    cudaEventElapsedTime(&c, ev[2], ev[3]);
+    cudaEventElapsedTime(&b, ev[2], ev[3]);
+    cudaEventElapsedTime(&c, ev[4], ev[5]);
     cudaPointerAttributes pa, pb;
     const int ta = cudaPointerGetAttributes(&pa, seqs) == cudaSuccess ? (int)pa.type : -1;
     const int tb = (cigar && cudaPointerGetAttributes(&pb, ops) == cudaSuccess) ? (int)pb.type : -1;

@@ -78,6 +78,10 @@ struct Engine {
   int num_sms = 0;
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
+  // host batches: a stream for the copies in, one for the copies out, and
+  // an event per chunk for each (created on first use)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_in[64] = {}, ev_done[64] = {};
   int64_t launches = 0;
   // batch buffers (host-input path)
   DevBuf seqs, poff, plen, toff, tlen, scores, status, ops, opsoff, opslen, endinfo;
