@@ -226,3 +226,21 @@ def test_drop_in_long_affine2p_pairs(gpu_available, wfa, oracle_mod):
     r = O.align(b, O.Penalties(metric=4), nthreads=8)
     for j, i in enumerate(idx):
         assert int(r.score[j]) == int(scores[i]), i
+
+
+def test_host_batch_in_chunks(gpu_available, wfa, oracle_mod):
+    """A host batch large enough for several chunks (copies in and out on
+    their own streams, kernels on two engines in turn) gives the checker's
+    scores, statuses and CIGARs for every pair."""
+    W, O = wfa, oracle_mod
+    p = W.generate(0, 40000, first=900)
+    al = W.Aligner(W.Config())
+    rc, scores, status, ops, ops_len, ops_off = al.align_batch(p.seqs, p.p_off, p.p_len,
+                                                               p.t_off, p.t_len)
+    al.close()
+    assert rc == 0
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    r = O.align(b, O.Penalties(), nthreads=8)
+    res = O.compare(b, O.Penalties(), scores, status, ops, ops_off, ops_len, r)
+    assert all(res[k] == 0 for k in ("score_mismatch", "status_mismatch", "cigar_mismatch",
+                                      "cigar_invalid", "rescore_mismatch")), res

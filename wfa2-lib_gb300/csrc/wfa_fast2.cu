@@ -162,9 +162,14 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
     __syncwarp();
     const uint32_t plen2 = pack16x2(plen, plen), tlen2 = pack16x2(tlen, tlen);
 
+    // the last scaled score to compute: step s -> s+1 needs g*s + 1 <
+    // max_steps (the reference computes score g*s+1 next and stops there at
+    // the step limit) and s + 1 < s_cap
+    const int64_t s_steps = p.max_steps >= 2 ? ((int64_t)p.max_steps - 2) / p.g + 1 : -1;
+    const int s_lim = (int)(s_steps < p.s_cap - 1 ? s_steps : (int64_t)(p.s_cap - 1));
     bool leave = false;
     while (!done) {
-      if ((int64_t)p.g * s + 1 >= (int64_t)p.max_steps || s + 1 >= p.s_cap) {
+      if (s + 1 > s_lim) {
         // the reference computes score g*s+1 next and stops there at the
         // step limit (wavefront/wavefront_unialign.c:102-107): the general
         // kernel reports that
@@ -243,14 +248,17 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       // pairs (a0 + 2q, a0 + 2q + 1), a0 = s (mod 2), q < nq; lane q % 32
       const int a0 = lo - ((lo - par) & 1);
       const int nq = ((hi - a0) >> 1) + 1;
-      const uint32_t* const wMx = rows32 + ((sMx * W + HALF + a0 - par) >> 1);
-      const uint32_t* const wMo =
-          rows32 + (MOS ? ((sMo * W + HALF + a0 - par) >> 1) : ((sMo * W + HALF + a0 - 2 + par) >> 1));
-      const uint32_t* const wI = rows32 + (((rowI + sIe) * W + HALF + a0 - 2 + par) >> 1);
-      const uint32_t* const wD = rows32 + (((rowD + sIe) * W + HALF + a0 + par) >> 1);
-      uint32_t* const oM = rows32 + ((bM + a0) >> 1);
-      uint32_t* const oI = rows32 + ((bI + a0) >> 1);
-      uint32_t* const oD = rows32 + ((bD + a0) >> 1);
+      // word of pair 0 in a row of this step's parity (element W/2 + a0 - par
+      // is even); the other parity's (k-1, k) word is hb + par - 1 and its
+      // (k+1, k+2) word hb + par
+      const int hb = (HALF + a0 - par) >> 1;
+      const uint32_t* const wMx = rows32 + sMx * WW + hb;
+      const uint32_t* const wMo = rows32 + sMo * WW + (MOS ? hb : hb + par - 1);
+      const uint32_t* const wI = rows32 + (rowI + sIe) * WW + hb + par - 1;
+      const uint32_t* const wD = rows32 + (rowD + sIe) * WW + hb + par;
+      uint32_t* const oM = rows32 + cM * WW + hb;
+      uint32_t* const oI = rows32 + (rowI + cI) * WW + hb;
+      uint32_t* const oD = rows32 + (rowD + cI) * WW + hb;
       // choice codes: a 16-bit entry per lane and iteration
       uint16_t* const crow = CIGAR ? reinterpret_cast<uint16_t*>(codes + (int64_t)s * RW) + lane : nullptr;
       // The inputs of one word (two cells): M[s-x] at (k, k+1), M[s-o-e] at
@@ -366,7 +374,9 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       if (aL > hi) rows[bM + aL] = rows[bI + aL] = rows[bD + aL] = kNull16;
       {
         const int shM = par - ((s - R) & 1), shI = par - ((s - RI) & 1);
-        const bool cM_ = oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
+        // (with a ring exactly o+e long the old M row is M[s-o-e], whose
+        // range the written span covers)
+        const bool cM_ = R != OE && oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
         const bool cI_ = oldI.x <= oldI.y && (oldI.x + shI < a0 || oldI.y + shI > aL);
         const bool cD_ = oldD.x <= oldD.y && (oldD.x + shI < a0 || oldD.y + shI > aL);
         if (cM_ | cI_ | cD_) {
