@@ -154,6 +154,131 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _timed_device(torch, stream, step, steps):
+    """CUDA-event time of `steps` calls of step() on `stream` after one untimed call."""
+    step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0
+
+
+def secondary_lines(W, O, torch, args, stream, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len,
+                    d_scores, d_status, d_ops, d_opsoff, d_opslen, p, n):
+    """Bounded measurements of the other configurations inside the headline
+    run, so that each has a recorded number: the headline batch under the
+    library's default heuristic (wf-adaptive 10,50,1), a sample of config 2
+    (affine2p, 1-10 kbp) and of config 3 (BiWFA, 100 kbp), each with a
+    parity check."""
+    out = {}
+    dev = d_seqs.device
+    # -- config 1 with wf-adaptive (10,50,1), full CIGAR, the same device batch
+    wa = W.Aligner(W.Config(wfadaptive=(10, 50, 1)))
+
+    def step_wa():
+        rc = wa.align_batch_device(n, d_seqs.data_ptr(), d_poff.data_ptr(), d_plen.data_ptr(),
+                                   d_toff.data_ptr(), d_tlen.data_ptr(), max_len,
+                                   d_scores.data_ptr(), d_status.data_ptr(), d_ops.data_ptr(),
+                                   d_opsoff.data_ptr(), d_opslen.data_ptr(), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"wf-adaptive batch failed: {rc}")
+    wa_s = _timed_device(torch, stream, step_wa, args.steps)
+    wa.close()
+    k = min(n, 20000)
+    g_sc, g_st = d_scores[:k].cpu().numpy(), d_status[:k].cpu().numpy()
+    g_len = d_opslen[:k].cpu().numpy()
+    offs = d_opsoff[:k + 1].cpu().numpy()
+    g_ops = d_ops[:int(offs[-1])].cpu().numpy()
+    b = O.PairBatch(p.seqs, p.p_off[:k], p.p_len[:k], p.t_off[:k], p.t_len[:k])
+    r = O.align(b, O.Penalties(), wfadaptive=(10, 50, 1), nthreads=os.cpu_count() or 1)
+    flagged = (r.flags & O.FLAG_STALE_SOURCE) != 0
+    bad = 0
+    for i in np.flatnonzero(~flagged):
+        cig = g_ops[offs[i]:offs[i] + g_len[i]].tobytes().decode()
+        bad += (int(g_sc[i]) != int(r.score[i])) or (int(g_st[i]) != int(r.status[i])) or \
+            (cig != r.cigar(i))
+    assert bad == 0, f"wf-adaptive parity: {bad} mismatches"
+    out["config1_wfadaptive"] = {
+        "value": n * args.steps / wa_s, "unit": "pairs/s", "ms_per_step": 1000 * wa_s / args.steps,
+        "parity": f"first {k} pairs: scores, statuses and CIGARs equal the checker's "
+                  f"({int(flagged.sum())} flagged stale-source pairs skipped)"}
+
+    # -- config 2 sample: affine2p (4,6,2,24,1), 1-10 kbp, full CIGAR
+    q = W.generate(2, 2000, first=0)
+    ql = q.p_len.astype(np.int64) + q.t_len
+    qo = np.zeros(q.n + 1, np.int64)
+    np.cumsum(ql, out=qo[1:])
+    t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+         for x in (q.seqs, q.p_off, q.p_len, q.t_off, q.t_len, qo)]
+    qs, qst = (torch.empty(q.n, dtype=torch.int32, device=dev) for _ in range(2))
+    qops = torch.empty(int(qo[-1]) + 16, dtype=torch.uint8, device=dev)
+    qol = torch.empty(q.n, dtype=torch.int32, device=dev)
+    a2 = W.Aligner(W.Config(metric=4))
+    qmax = int(max(q.p_len.max(), q.t_len.max()))
+
+    def step_a2():
+        rc = a2.align_batch_device(q.n, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(),
+                                   t[3].data_ptr(), t[4].data_ptr(), qmax, qs.data_ptr(),
+                                   qst.data_ptr(), qops.data_ptr(), t[5].data_ptr(),
+                                   qol.data_ptr(), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"affine2p batch failed: {rc}")
+    a2_s = _timed_device(torch, stream, step_a2, 1)
+    a2.close()
+    kk = 8
+    b2 = O.PairBatch(q.seqs, q.p_off[:kk], q.p_len[:kk], q.t_off[:kk], q.t_len[:kk])
+    r2 = O.align(b2, O.Penalties(metric=4), nthreads=os.cpu_count() or 1)
+    g2 = qs[:kk].cpu().numpy()
+    assert np.array_equal(g2, r2.score) and (qst[:kk].cpu().numpy() == 0).all(), "affine2p parity"
+    out["config2_affine2p_sample"] = {
+        "value": q.n / a2_s, "unit": "pairs/s",
+        "sample": f"{q.n} pairs of the config-2 workload, device-resident, one step",
+        "parity": f"first {kk} scores equal the checker's"}
+
+    # -- config 3 sample: BiWFA (ultralow memory), 100 kbp, full CIGAR; its
+    # scores against the unidirectional score-only run of the same pairs
+    z = W.generate(3, 48, first=0)
+    zl = z.p_len.astype(np.int64) + z.t_len
+    zo = np.zeros(z.n + 1, np.int64)
+    np.cumsum(zl, out=zo[1:])
+    u = [torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+         for x in (z.seqs, z.p_off, z.p_len, z.t_off, z.t_len, zo)]
+    zs, zst = (torch.empty(z.n, dtype=torch.int32, device=dev) for _ in range(2))
+    zops = torch.empty(int(zo[-1]) + 16, dtype=torch.uint8, device=dev)
+    zol = torch.empty(z.n, dtype=torch.int32, device=dev)
+    zmax = int(max(z.p_len.max(), z.t_len.max()))
+    bi = W.Aligner(W.Config(memory_mode=MEM_ULTRALOW))
+
+    def step_bi():
+        rc = bi.align_batch_device(z.n, u[0].data_ptr(), u[1].data_ptr(), u[2].data_ptr(),
+                                   u[3].data_ptr(), u[4].data_ptr(), zmax, zs.data_ptr(),
+                                   zst.data_ptr(), zops.data_ptr(), u[5].data_ptr(),
+                                   zol.data_ptr(), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"BiWFA batch failed: {rc}")
+    bi_s = _timed_device(torch, stream, step_bi, 1)
+    bi.close()
+    bi_scores = zs.cpu().numpy().copy()
+    uni = W.Aligner(W.Config(score_only=True))
+    rc = uni.align_batch_device(z.n, u[0].data_ptr(), u[1].data_ptr(), u[2].data_ptr(),
+                                u[3].data_ptr(), u[4].data_ptr(), zmax, zs.data_ptr(),
+                                zst.data_ptr(), 0, 0, 0, stream.cuda_stream)
+    torch.cuda.synchronize()
+    uni.close()
+    assert rc == 0 and np.array_equal(bi_scores, zs.cpu().numpy()), "BiWFA score parity"
+    out["config3_biwfa_sample"] = {
+        "value": z.n / bi_s, "unit": "pairs/s",
+        "sample": f"{z.n} pairs of the config-3 workload (100 kbp), device-resident, one step "
+                  "(a batch this small is bound by the longest pair's latency)",
+        "parity": "BiWFA scores equal the unidirectional score-only scores"}
+    return out
+
+
 def gen_pinned(W, torch, workload, n, first, param=0, param2=0):
     """Seeded pairs in pinned host memory."""
     def alloc(nbytes):
@@ -629,6 +754,9 @@ def main():
         secondary["config1_score_only"] = {
             "value": n * args.steps / so_s, "unit": "pairs/s", "ms_per_step": 1000 * so_s / args.steps,
             "parity": f"all {n} scores equal the checker's"}
+        secondary.update(secondary_lines(W, O, torch, args, stream, d_seqs, d_poff, d_plen, d_toff,
+                                         d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff,
+                                         d_opslen, p, n))
 
     # CPU baseline and work units (WFA cells, extend chars): the checker's run
     # over the whole batch where it ran, else a bounded sample of the workload
