@@ -225,10 +225,21 @@ static int gcd_int(int a, int b) {
 }
 
 // Whether the fast pass serves this configuration.
+// wf-adaptive alone, on penalties that scale to the default's (2, 4, 1):
+// the two-diagonal kernel's cut-off variant (a warp per pair)
+static bool fast_wfadaptive(const wf2g_cfg_t& cfg) {
+  if (cfg.heur != kHsWfadaptive || env_int("WF2G_FAST_WFA", 1) == 0 || env_int("WF2G_FAST2", 1) == 0)
+    return false;
+  if (cfg.x <= 0 || cfg.o1 <= 0 || cfg.e1 <= 0) return false;
+  const int g = gcd_int(gcd_int(cfg.x, cfg.o1 + cfg.e1), cfg.e1);
+  return cfg.x / g == 2 && (cfg.o1 + cfg.e1) / g == 4 && cfg.e1 / g == 1;
+}
+
 static bool fast_eligible(const wf2g_cfg_t& cfg, int max_len, const int8_t* d_cb,
                           const int8_t* d_ce, int score_cap) {
-  return env_int("WF2G_FAST", 1) != 0 && cfg.metric == 3 && cfg.heur == 0 && !cfg.endsfree &&
-         !cfg.extension && !cfg.ultralow && d_cb == nullptr && d_ce == nullptr && score_cap == 0 &&
+  return env_int("WF2G_FAST", 1) != 0 && cfg.metric == 3 &&
+         (cfg.heur == 0 || fast_wfadaptive(cfg)) && !cfg.endsfree && !cfg.extension &&
+         !cfg.ultralow && d_cb == nullptr && d_ce == nullptr && score_cap == 0 &&
          max_len <= kFastMaxLen && cfg.x > 0 && cfg.o1 > 0 && cfg.e1 > 0;
 }
 
@@ -254,8 +265,13 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
   // and the scaled e odd (wfa_fast2.cu); else one cell per thread
   const bool two = G == 32 && (fp.x & 1) == 0 && (fp.e & 1) == 1 && env_int("WF2G_FAST2", 1);
   const bool d241 = fp.x == 2 && fp.oe == 4 && fp.e == 1;
-  void* fn = two ? wf2g_fast2_kernel_ptr(cigar, (fp.oe & 1) == 0, W, d241)
+  const bool wfa = cfg.heur != 0;  // fast_eligible admits wf-adaptive alone, with d241
+  if (wfa && !(two && d241)) return WF2G_ERR_CUDA_;
+  void* fn = two ? wf2g_fast2_kernel_ptr(cigar, (fp.oe & 1) == 0, W, d241, wfa)
                  : wf2g_fast_kernel_ptr(cigar, G, W);
+  fp.h_min_len = cfg.h_min_len;
+  fp.h_max_dist = cfg.h_max_dist;
+  fp.h_steps = cfg.h_steps;
   if (!fn) return WF2G_ERR_CUDA_;
   fp.g = g;
   fp.match = cfg.match;
@@ -299,7 +315,8 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
     off = al16(off + (int64_t)2 * fp.nq * 8);
   }
   fp.meta_off = (int)off;
-  off = al16(off + (int64_t)nw * nrows * 8);
+  // row limits, and (two diagonals per lane) the rows' windows
+  off = al16(off + (int64_t)(nw + 1) * nrows * 8);
   fp.red_off = (int)off;
   // two step-parameter buffers, the per-warp partial reductions, a broadcast slot
   off = al16(off + 256 + (int64_t)nw * 8 * 4 + 16);
@@ -361,7 +378,8 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
     // place; the second, over what the first left: rows of 2048.  A batch
     // too small to fill the GPU (the drop-in's single pair) takes four warps
     // per pair instead, which shortens each pair's steps.
-    const int small_n = env_int("WF2G_FAST_SMALL_N", 2 * E->num_sms);
+    // (the wf-adaptive variant exists for a warp per pair only)
+    const int small_n = cfg.heur != 0 ? 0 : env_int("WF2G_FAST_SMALL_N", 2 * E->num_sms);
     const int g1 = n <= small_n ? 128 : 32;
     int rc = run_fast_pass(E, cfg, g1, 1024, n, nullptr, nullptr, d_seqs, d_poff, d_plen, d_toff,
                            d_tlen, max_len, d_scores, d_status, d_ops, d_opsoff, d_opslen,
@@ -373,7 +391,7 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
       // the pairs pass 1 left: rows of 1536 diagonals with a warp per pair
       // (10 pairs per SM; they cover every pair of the headline workload),
       // then 2048 for what remains (four warps per pair on small batches)
-      const int gw = n <= small_n ? 128 : env_int("WF2G_FAST_WIDE_G", 32);
+      const int gw = n <= small_n ? 128 : cfg.heur != 0 ? 32 : env_int("WF2G_FAST_WIDE_G", 32);
       const int g2 = gw <= 32 ? 32 : gw <= 64 ? 64 : 128;
       const int w2 = g2 == 32 ? env_int("WF2G_FAST_W2", 1536) : 2048;
       rc = run_fast_pass(E, cfg, g2, w2 == 1536 ? 1536 : 2048, n, retry + (size_t)3 * n,

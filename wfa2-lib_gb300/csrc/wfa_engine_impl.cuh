@@ -30,7 +30,7 @@ extern "C" void* wf2g_bi_gather_ptr(void);
 extern "C" size_t wf2g_bi_smem_bytes(int a2p, int scope);
 extern "C" void* wf2g_pool_init_ptr(void);
 extern "C" void* wf2g_fast_kernel_ptr(int cigar, int group, int width);
-extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241);
+extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241, int wfa);
 
 namespace eng {
 

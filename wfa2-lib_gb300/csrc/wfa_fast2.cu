@@ -78,8 +78,9 @@ __device__ __forceinline__ uint32_t pack16x2(int lo, int hi) {
 // rows' parity.  W: elements per shared-memory row (diagonals
 // [4-W/2, W/2-4] are computed).  D241: the scaled penalties are the
 // default's (x, o+e, e) = (2, 4, 1), compiled in (rings of 4 M rows and 1 I
-// and D row).
-template <bool CIGAR, bool MOS, int W, bool D241>
+// and D row).  WFA: the wf-adaptive cut-off (wavefront/wavefront_heuristic.c:
+// 229-289), the library's default heuristic.
+template <bool CIGAR, bool MOS, int W, bool D241, bool WFA>
 __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
   static_assert(!D241 || MOS, "o+e = 4 is even");
   const int X = D241 ? 2 : p.x, OE = D241 ? 4 : p.oe, E = D241 ? 1 : p.e;
@@ -100,6 +101,13 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
   uint2* const QP = reinterpret_cast<uint2*>(smem);
   uint2* const QT = QP + 1;
   int2* const meta = reinterpret_cast<int2*>(smem + p.meta_off);
+  // per ring slot, the cells its row may hold: its limits before a cut-off.
+  // A cut only shrinks the limits; the cut cells stay readable as the
+  // neighbours of the next steps' cells, as in the reference, where later
+  // compute steps pad with NULL only beyond a wavefront's initialised window
+  // (wavefront/wavefront_compute.c:498-527).  Without a cut-off it equals
+  // the limits.
+  int2* const win = meta + nrows;
   // per-warp slice: [choice words: s_cap rows of RW][row limits: s_cap short2][walk items]
   uint8_t* const slice = p.scratch + (int64_t)blockIdx.x * p.slice_bytes;
   uint32_t* const codes = reinterpret_cast<uint32_t*>(slice);
@@ -132,7 +140,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         rows32[r * WW + used_lo + j] = 0x80008000u;
       }
     }
-    for (int r = lane; r < nrows; r += 32) meta[r] = make_int2(kBig, -kBig);
+    for (int r = lane; r < nrows; r += 32) meta[r] = win[r] = make_int2(kBig, -kBig);
     bool ok = fast_stage<32, 2>(p.seqs + p.p_off[pair], min(plen, p.max_len), QP, p.nq, lane);
     ok &= fast_stage<32, 2>(p.seqs + p.t_off[pair], min(tlen, p.max_len), QT, p.nq, lane);
     __syncwarp();
@@ -154,9 +162,15 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
     int64_t bt_used = 0;     // choice codes of the pair: the general kernel's byte count
     int w_lo = 0, w_hi = 0;  // diagonals touched
     bool done = (plen == tlen) && (L0 >= tlen);
+    int steps_wait = WFA ? p.h_steps : 0;  // steps to the next cut-off
+    if (WFA && !done) {
+      // the cut-off of M[0]: one cell, never cut; it counts toward the wait
+      --steps_wait;
+      if (steps_wait <= 0 && 1 >= p.h_min_len) steps_wait = p.h_steps;
+    }
     if (lane == 0) {
       rows[HALF] = (int16_t)L0;  // row 0 (slot 0 of M, parity 0), diagonal 0
-      meta[0] = make_int2(0, 0);
+      meta[0] = win[0] = make_int2(0, 0);
       if (CIGAR) tab[0] = make_short2(0, 0);
     }
     __syncwarp();
@@ -201,9 +215,9 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       const int obD = (rowD + cI) * W + HALF - ((s - RI) & 1);
       // the output slots' previous contents (the inputs themselves when the
       // ring is exactly as long as their distance)
-      const int2 oldM = (R == OE) ? eMo : meta[cM];
-      const int2 oldI = (RI == E) ? eI : meta[rowI + cI];
-      const int2 oldD = (RI == E) ? eD : meta[rowD + cI];
+      const int2 oldM = WFA ? win[cM] : (R == OE) ? eMo : meta[cM];
+      const int2 oldI = WFA ? win[rowI + cI] : (RI == E) ? eI : meta[rowI + cI];
+      const int2 oldD = WFA ? win[rowD + cI] : (RI == E) ? eD : meta[rowD + cI];
       // output range: union of the inputs' (wavefront/wavefront_compute.c:40-87)
       const int lo = min(min(eMx.x, eMo.x - 1), min(eI.x + 1, eD.x - 1));
       const int hi = max(max(eMx.y, eMo.y + 1), max(eI.y + 1, eD.y - 1));
@@ -216,6 +230,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         __syncwarp();
         if (lane == 0) {
           meta[cM] = meta[rowI + cI] = meta[rowD + cI] = kEmpty;
+          win[cM] = win[rowI + cI] = win[rowD + cI] = kEmpty;
           if (CIGAR) tab[s] = make_short2(1, 0);
         }
         __syncwarp();
@@ -241,8 +256,20 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       // the natural ranges of I (sources at k-1) and D (sources at k+1): the
       // cells of [lo, hi] outside them are computed from NULL or NULL-ish
       // (negative) inputs only, so they come out negative, out of bounds
-      const int iLo = min(eMo.x, eI.x) + 1, iHi = max(eMo.y, eI.y) + 1;
-      const int dLo = min(eMo.x, eD.x) - 1, dHi = max(eMo.y, eD.y) - 1;
+      // (under a cut-off the sources' windows, clamped to [lo, hi])
+      int iLo, iHi, dLo, dHi;
+      if (WFA) {
+        const int2 wMo = win[sMo], wI = win[rowI + sIe], wD = win[rowD + sIe];
+        iLo = max(lo, min(wMo.x, wI.x) + 1);
+        iHi = min(hi, max(wMo.y, wI.y) + 1);
+        dLo = max(lo, min(wMo.x, wD.x) - 1);
+        dHi = min(hi, max(wMo.y, wD.y) - 1);
+      } else {
+        iLo = min(eMo.x, eI.x) + 1;
+        iHi = max(eMo.y, eI.y) + 1;
+        dLo = min(eMo.x, eD.x) - 1;
+        dHi = max(eMo.y, eD.y) - 1;
+      }
 
       // ======================================== the cells
       // pairs (a0 + 2q, a0 + 2q + 1), a0 = s (mod 2), q < nq; lane q % 32
@@ -376,7 +403,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         const int shM = par - ((s - R) & 1), shI = par - ((s - RI) & 1);
         // (with a ring exactly o+e long the old M row is M[s-o-e], whose
         // range the written span covers)
-        const bool cM_ = R != OE && oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
+        const bool cM_ = (WFA || R != OE) && oldM.x <= oldM.y && (oldM.x + shM < a0 || oldM.y + shM > aL);
         const bool cI_ = oldI.x <= oldI.y && (oldI.x + shI < a0 || oldI.y + shI > aL);
         const bool cD_ = oldD.x <= oldD.y && (oldD.x + shI < a0 || oldD.y + shI > aL);
         if (cM_ | cI_ | cD_) {
@@ -446,11 +473,79 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
           for (int q = lane; q < nR; q += 32) rows[bD + dHi - q] = kNull16;
         }
       }
-      meta[cM] = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
-      meta[rowI + cI] = fI == INT_MAX ? kEmpty : make_int2(fI, lI);
-      meta[rowD + cI] = fD == INT_MAX ? kEmpty : make_int2(fD, lD);
+      int2 tM = fM == INT_MAX ? kEmpty : make_int2(fM, lM);
+      int2 tI = fI == INT_MAX ? kEmpty : make_int2(fI, lI);
+      int2 tD = fD == INT_MAX ? kEmpty : make_int2(fD, lD);
       // termination on M[s] at k_end (wavefront/wavefront_termination.c:37-60)
-      done = fM <= k_end && k_end <= lM && rows[bM + k_end] >= tlen;
+      done = tM.x <= k_end && k_end <= tM.y && rows[bM + k_end] >= tlen;
+      if (WFA) {
+        win[cM] = tM;
+        win[rowI + cI] = tI;
+        win[rowD + cI] = tD;
+      }
+      const int2 winM = tM, winI = tI, winD = tD;  // the windows, before a cut
+      if (WFA && !done && tM.x <= tM.y) {
+        // wf-adaptive cut-off of the extended M[s] (wavefront/wavefront_
+        // heuristic.c:229-289, dispatch :506-563): cells further from the end
+        // than the closest by more than max_distance_threshold are cut from
+        // both ends, keeping the end diagonal's side; I and D take the
+        // intersection of limits
+        --steps_wait;
+        if (steps_wait <= 0 && tM.y - tM.x + 1 >= p.h_min_len) {
+          auto dist = [&](int k) -> int {
+            const int off = rows[bM + k];
+            return off < 0 ? (1 << 30) : max(plen - (off - k), tlen - off);
+          };
+          int dmin = max(plen, tlen);
+          for (int k = tM.x + lane; k <= tM.y; k += 32) dmin = min(dmin, dist(k));
+          dmin = __reduce_min_sync(kFull, dmin);
+          const int top = min(k_end, tM.y);
+          int nlo = max(tM.x, top);
+          for (int c = tM.x; c < top; c += 32) {
+            const int k = c + lane;
+            const uint32_t m = __ballot_sync(kFull, k < top && dist(k) - dmin <= p.h_max_dist);
+            if (m) {
+              nlo = c + __ffs(m) - 1;
+              break;
+            }
+          }
+          const int bot = max(k_end, nlo);
+          int nhi = min(tM.y, bot);
+          for (int c = tM.y; c > bot; c -= 32) {
+            const int k = c - lane;
+            const uint32_t m = __ballot_sync(kFull, k > bot && dist(k) - dmin <= p.h_max_dist);
+            if (m) {
+              nhi = c - (__ffs(m) - 1);
+              break;
+            }
+          }
+          steps_wait = p.h_steps;
+          if (nlo != tM.x || nhi != tM.y) {
+            tM = make_int2(nlo, nhi);
+            tI = make_int2(max(tI.x, nlo), min(tI.y, nhi));
+            tD = make_int2(max(tD.x, nlo), min(tD.y, nhi));
+            // a row the cut empties reads as NULL everywhere (its window too)
+            if (tM.x > tM.y) {
+              for (int k = winM.x + lane; k <= winM.y; k += 32) rows[bM + k] = kNull16;
+              tM = kEmpty;
+              win[cM] = kEmpty;
+            }
+            if (tI.x > tI.y) {
+              for (int k = winI.x + lane; k <= winI.y; k += 32) rows[bI + k] = kNull16;
+              tI = kEmpty;
+              win[rowI + cI] = kEmpty;
+            }
+            if (tD.x > tD.y) {
+              for (int k = winD.x + lane; k <= winD.y; k += 32) rows[bD + k] = kNull16;
+              tD = kEmpty;
+              win[rowD + cI] = kEmpty;
+            }
+          }
+        }
+      }
+      meta[cM] = tM;
+      meta[rowI + cI] = tI;
+      meta[rowD + cI] = tD;
       __syncwarp();
     }
     // words touched by this pair: elements [W/2 + w_lo - 4, W/2 + w_hi + 3]
@@ -511,17 +606,23 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
 }  // namespace wf2g
 
 // Kernel of the two-diagonals-per-lane pass for (full CIGAR?, o+e even?, row
-// width, default scaled penalties (2, 4, 1)?).
-extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241) {
+// width, default scaled penalties (2, 4, 1)?, wf-adaptive cut-off?).  The
+// cut-off is compiled for the default penalties only.
+extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241, int wfa) {
   using namespace wf2g;
 #define WF2G_FAST2_CASE(W)                                                                        \
   if (width == W) {                                                                               \
-    if (d241) return cigar ? (void*)wfa_fast2_kernel<true, true, W, true>                         \
-                           : (void*)wfa_fast2_kernel<false, true, W, true>;                       \
-    if (mos) return cigar ? (void*)wfa_fast2_kernel<true, true, W, false>                         \
-                          : (void*)wfa_fast2_kernel<false, true, W, false>;                       \
-    return cigar ? (void*)wfa_fast2_kernel<true, false, W, false>                                 \
-                 : (void*)wfa_fast2_kernel<false, false, W, false>;                               \
+    if (wfa) {                                                                                    \
+      if (!d241) return nullptr;                                                                  \
+      return cigar ? (void*)wfa_fast2_kernel<true, true, W, true, true>                           \
+                   : (void*)wfa_fast2_kernel<false, true, W, true, true>;                         \
+    }                                                                                             \
+    if (d241) return cigar ? (void*)wfa_fast2_kernel<true, true, W, true, false>                  \
+                           : (void*)wfa_fast2_kernel<false, true, W, true, false>;                \
+    if (mos) return cigar ? (void*)wfa_fast2_kernel<true, true, W, false, false>                  \
+                          : (void*)wfa_fast2_kernel<false, true, W, false, false>;                \
+    return cigar ? (void*)wfa_fast2_kernel<true, false, W, false, false>                          \
+                 : (void*)wfa_fast2_kernel<false, false, W, false, false>;                        \
   }
   WF2G_FAST2_CASE(1024)
   WF2G_FAST2_CASE(1536)

@@ -148,6 +148,9 @@ struct FastParams {
   int match;      // the user's match (<= 0), for the classic score
   int R, RI;      // ring depths: max(x, oe) + 1 M rows, e + 1 I and D rows
   int max_steps;  // unscaled step limit (INT32_MAX: none)
+  // wf-adaptive cut-off (two-diagonal kernel): min_wavefront_length,
+  // max_distance_threshold, steps_between_cutoffs
+  int h_min_len, h_max_dist, h_steps;
   const uint8_t* seqs;
   const int64_t* p_off;
   const int32_t* p_len;
