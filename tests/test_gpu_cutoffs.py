@@ -173,3 +173,34 @@ def test_zdrop_full_alignment_matches_oracle(gpu_available, wfa, oracle_mod, cas
         assert got[i] == want, (spec_name, case, i)
         compared += 1
     assert compared >= b.n // 2, (spec_name, compared)
+
+
+@pytest.mark.parametrize("params", [(10, 50, 1), (20, 30, 2), (1, 0, 3), (5, 10, 1)])
+@pytest.mark.parametrize("score_only", [False, True])
+def test_wfadaptive_fast_pass_matches_oracle(gpu_available, wfa, oracle_mod, params, score_only):
+    """wf-adaptive alone on the default penalties runs in the two-diagonal
+    fast kernel (cut-off after the termination test, limits shrunk, the cut
+    cells kept readable in the rows' windows): every pair the checker does
+    not flag as reading a cut-emptied source equals the checker, on a batch
+    of 0.5-1.5 kbp pairs and on random-tail pairs where the cuts fire."""
+    W, O = wfa, oracle_mod
+    for wl, n in [(1, 600), (6, 120)]:
+        p = W.generate(wl, n, first=77)
+        b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+        al = W.Aligner(W.Config(score_only=score_only, wfadaptive=params))
+        rc, scores, status, ops, ops_len, ops_off = al.align_batch(p.seqs, p.p_off, p.p_len,
+                                                                   p.t_off, p.t_len)
+        al.close()
+        assert rc == 0
+        r = O.align(b, O.Penalties(), score_only=score_only, wfadaptive=params)
+        compared = 0
+        for i in range(n):
+            if r.flags[i] & O.FLAG_STALE_SOURCE:
+                continue
+            got = (int(status[i]), int(scores[i]))
+            assert got == (int(r.status[i]), int(r.score[i])), (params, wl, i)
+            if not score_only:
+                assert ops[ops_off[i]:ops_off[i] + ops_len[i]].tobytes().decode() == r.cigar(i), \
+                    (params, wl, i)
+            compared += 1
+        assert compared >= n // 2
