@@ -325,6 +325,11 @@ void wavefront_aligner_set_heuristic_banded_adaptive(wavefront_aligner_t* const 
 /* wavefront/wfa.h:185-194 (wavefront/wavefront_aligner.c:606-645) */
 void wavefront_aligner_set_max_alignment_steps(wavefront_aligner_t* const wf_aligner,
     const int max_alignment_steps);
+/* wavefront/wavefront_aligner.h:54-66: CIGAR trimming and display */
+bool wavefront_aligner_maxtrim_cigar(wavefront_aligner_t* const wf_aligner);
+void wavefront_aligner_print_mode(FILE* const stream, wavefront_aligner_t* const wf_aligner);
+void wavefront_aligner_print_scope(FILE* const stream, wavefront_aligner_t* const wf_aligner);
+void wavefront_aligner_print_conf(FILE* const stream, wavefront_aligner_t* const wf_aligner);
 void wavefront_aligner_set_max_memory(wavefront_aligner_t* const wf_aligner,
     const uint64_t max_memory_resident, const uint64_t max_memory_abort);
 void wavefront_aligner_set_max_num_threads(wavefront_aligner_t* const wf_aligner,
@@ -364,6 +369,10 @@ int cigar_score_edit(const cigar_t* const cigar);
 int cigar_score_gap_linear(const cigar_t* const cigar, const linear_penalties_t* const penalties);
 int cigar_score_gap_affine(const cigar_t* const cigar, const affine_penalties_t* const penalties);
 int cigar_score_gap_affine2p(const cigar_t* const cigar, const affine2p_penalties_t* const penalties);
+/* alignment/cigar_utils.h:61-69 (maximal-score trimming, cigar_utils.c:112-318) */
+bool cigar_maxtrim_gap_linear(cigar_t* const cigar, const linear_penalties_t* const penalties);
+bool cigar_maxtrim_gap_affine(cigar_t* const cigar, const affine_penalties_t* const penalties);
+bool cigar_maxtrim_gap_affine2p(cigar_t* const cigar, const affine2p_penalties_t* const penalties);
 bool cigar_check_alignment(FILE* const stream,
     const char* const pattern, const int pattern_length,
     const char* const text, const int text_length,

@@ -170,3 +170,82 @@ def test_heuristic_setters_add_strategies(wfa):
                                              | wfa.WF_HEURISTIC_WFADAPTIVE)
     assert h.contents.heuristic.steps_between_cutoffs == 1
     wfa.lib().wavefront_aligner_delete(h)
+
+
+def _maxtrim_py(ops, match, x, o, e, linear=False):
+    """Maximal-score prefix as alignment/cigar_utils.c:112-220 computes it."""
+    earn = match if match != 0 else -1
+    score = best = v = h = bv = bh = 0
+    best_i, last = 0, ""
+    for i, op in enumerate(ops):
+        if op == "M":
+            score -= earn; v += 1; h += 1
+        elif op == "X":
+            score -= x; v += 1; h += 1
+        else:
+            score -= o if linear else e + (0 if last == op else o)
+            if op == "I":
+                h += 1
+            else:
+                v += 1
+        last = op
+        if score > best:
+            best, best_i, bv, bh = score, i, v, h
+    # (the reference reports a trim when the best prefix is not the whole
+    # CIGAR; a best score of 0 leaves the offset at the first operation)
+    was_trimmed = best_i != len(ops) - 1
+    return ((ops[:best_i + 1], best, bv, bh) if best > 0 else ("", None, -1, -1)), was_trimmed
+
+
+def test_maxtrim_and_display_on_host(wfa, tmp_path):
+    """cigar_maxtrim_* and wavefront_aligner_maxtrim_cigar trim to the
+    maximal-score prefix (alignment/cigar_utils.c:112-318); the display calls
+    print the reference's labels (wavefront/wavefront_aligner.c:680-735)."""
+    L = wfa.lib()
+    L.cigar_new.restype = C.POINTER(wfa.Cigar)
+    L.cigar_new.argtypes = [C.c_int]
+    L.cigar_free.argtypes = [C.POINTER(wfa.Cigar)]
+    L.cigar_maxtrim_gap_affine.restype = C.c_bool
+    L.cigar_maxtrim_gap_affine2p.restype = C.c_bool
+    for ops in ["MMMXMMIIIMMDDMMMMXX", "MMMMMMMMXXXXXXXIIIIIIIIII", "XXIIDD", "MMXMDDDDDDDDMM"]:
+        for match in (0, -2):
+            cg = L.cigar_new(64)
+            C.memmove(cg.contents.operations, ops.encode(), len(ops))
+            cg.contents.begin_offset, cg.contents.end_offset = 0, len(ops)
+            ap = wfa.AffinePenalties(match, 4, 6, 2)
+            trimmed = L.cigar_maxtrim_gap_affine(cg, C.byref(ap))
+            (want_ops, want_score, ev, eh), want_trimmed = _maxtrim_py(ops, match, 4, 6, 2)
+            c = cg.contents
+            got = bytes(c.operations[c.begin_offset:c.end_offset]).decode()
+            assert got == want_ops, (ops, match)
+            assert trimmed == want_trimmed, (ops, match)
+            if want_score is not None:
+                assert (c.score, c.end_v, c.end_h) == (want_score, ev, eh)
+            # affine2p with the second model never cheaper is the affine rule
+            # on runs
+            cg2 = L.cigar_new(64)
+            C.memmove(cg2.contents.operations, ops.encode(), len(ops))
+            cg2.contents.begin_offset, cg2.contents.end_offset = 0, len(ops)
+            a2 = wfa.Affine2pPenalties(match, 4, 6, 2, 1000, 1000)
+            L.cigar_maxtrim_gap_affine2p(cg2, C.byref(a2))
+            c2 = cg2.contents
+            got2 = bytes(c2.operations[c2.begin_offset:c2.end_offset]).decode()
+            assert len(got2) <= len(ops) and ops.startswith(got2)
+            L.cigar_free(cg)
+            L.cigar_free(cg2)
+    # display
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    attr = wfa.default_attributes()
+    h = L.wavefront_aligner_new(C.byref(attr))
+    out = tmp_path / "conf.txt"
+    fp = libc.fopen(str(out).encode(), b"w")
+    for name in ("mode", "scope", "conf"):
+        fn = getattr(L, f"wavefront_aligner_print_{name}")
+        fn.argtypes = [C.c_void_p, C.c_void_p]
+        fn(fp, h)
+    libc.fclose(fp)
+    assert out.read_text() == "WFA(alignment,end2end)(MHigh,inf)"
+    L.wavefront_aligner_delete(h)

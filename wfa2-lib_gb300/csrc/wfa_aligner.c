@@ -629,3 +629,50 @@ int64_t wavefront_server_gpu_launches(wavefront_server_t* const server) {
 void wavefront_server_delete(wavefront_server_t* const server) {
   if (server) wf2g_server_free(server);
 }
+
+/* ------------------------------------------------------------ utilities and display */
+/* wavefront/wavefront_aligner.c:664-676: trims the aligner's CIGAR to its
+ * maximal-score prefix under the user's penalties; edit and indel are not
+ * trimmed */
+bool wavefront_aligner_maxtrim_cigar(wavefront_aligner_t* const wf_aligner) {
+  switch (wf_aligner->penalties.distance_metric) {
+    case gap_linear:
+      return cigar_maxtrim_gap_linear(wf_aligner->cigar, &wf_aligner->penalties.linear_penalties);
+    case gap_affine:
+      return cigar_maxtrim_gap_affine(wf_aligner->cigar, &wf_aligner->penalties.affine_penalties);
+    case gap_affine_2p:
+      return cigar_maxtrim_gap_affine2p(wf_aligner->cigar,
+                                        &wf_aligner->penalties.affine2p_penalties);
+    default:
+      return false;
+  }
+}
+/* wavefront/wavefront_aligner.c:680-735: the same labels as the reference
+ * prints them */
+void wavefront_aligner_print_mode(FILE* const stream, wavefront_aligner_t* const wf_aligner) {
+  if (wf_aligner->align_mode_tag != NULL) fprintf(stream, "%s::", wf_aligner->align_mode_tag);
+  static const char* const names[] = {"WFA", "BiWFA", "BiWFA::Forward", "BiWFA::Reverse",
+                                      "BiWFA::SubWFA"};
+  const int m = (int)wf_aligner->align_mode;
+  fputs(m >= 1 && m <= 4 ? names[m] : names[0], stream);
+}
+void wavefront_aligner_print_scope(FILE* const stream, wavefront_aligner_t* const wf_aligner) {
+  const char* const scope = wf_aligner->alignment_scope == compute_score ? "score" : "alignment";
+  const alignment_form_t* const f = &wf_aligner->alignment_form;
+  if (f->span == alignment_end2end) {
+    fprintf(stream, "(%s,end2end)", scope);
+  } else {
+    fprintf(stream, "(%s,endsfree,%d,%d,%d,%d)", scope, f->pattern_begin_free,
+            f->pattern_end_free, f->text_begin_free, f->text_end_free);
+  }
+}
+void wavefront_aligner_print_conf(FILE* const stream, wavefront_aligner_t* const wf_aligner) {
+  static const char* const modes[] = {"MHigh", "MMed", "MLow", "BiWFA"};
+  const int m = (int)wf_aligner->memory_mode;
+  fprintf(stream, "(%s", m >= 0 && m <= 3 ? modes[m] : "");
+  if (wf_aligner->system.max_alignment_steps == INT_MAX) {
+    fprintf(stream, ",inf)");
+  } else {
+    fprintf(stream, ",%d)", wf_aligner->system.max_alignment_steps);
+  }
+}

@@ -167,6 +167,112 @@ int cigar_score_gap_affine2p(const cigar_t* const c, const affine2p_penalties_t*
   return s;
 }
 
+/* Maximal-score trimming (alignment/cigar_utils.c:112-318): the CIGAR is cut
+ * to its highest-scoring prefix under the penalties, where a match earns
+ * -match (1 when match is 0).  A best prefix of score 0 clears the CIGAR;
+ * otherwise its score and end position are set.  Returns whether the best
+ * prefix ends before the last operation.  The affine2p rule scores whole
+ * runs (each gap run the cheaper of its two models) and may end only at a
+ * run's end. */
+typedef struct {
+  int score, v, h;
+} trim_walk_t;
+static bool maxtrim_apply(cigar_t* const c, int best, int best_i, int bv, int bh) {
+  const bool trimmed = best_i != c->end_offset - 1;
+  if (best == 0) {
+    cigar_clear(c);
+  } else {
+    c->end_offset = best_i + 1;
+    if (c->end_offset < c->max_operations) c->operations[c->end_offset] = '\0';
+    c->score = best;
+    c->end_v = bv;
+    c->end_h = bh;
+  }
+  return trimmed;
+}
+static void trim_step(trim_walk_t* w, char op, int cost) {
+  w->score -= cost;
+  if (op == 'M' || op == 'X') {
+    ++w->v;
+    ++w->h;
+  } else if (op == 'I') {
+    ++w->h;
+  } else {
+    ++w->v;
+  }
+}
+bool cigar_maxtrim_gap_linear(cigar_t* const c, const linear_penalties_t* const p) {
+  const int earn = p->match != 0 ? p->match : -1;
+  trim_walk_t w = {0, 0, 0};
+  int best = 0, best_i = c->begin_offset, bv = 0, bh = 0;
+  for (int i = c->begin_offset; i < c->end_offset; ++i) {
+    const char op = c->operations[i];
+    trim_step(&w, op, op == 'M' ? earn : op == 'X' ? p->mismatch : p->indel);
+    if (w.score > best) {
+      best = w.score;
+      best_i = i;
+      bv = w.v;
+      bh = w.h;
+    }
+  }
+  return maxtrim_apply(c, best, best_i, bv, bh);
+}
+bool cigar_maxtrim_gap_affine(cigar_t* const c, const affine_penalties_t* const p) {
+  const int earn = p->match != 0 ? p->match : -1;
+  trim_walk_t w = {0, 0, 0};
+  int best = 0, best_i = c->begin_offset, bv = 0, bh = 0;
+  char last = '\0';
+  for (int i = c->begin_offset; i < c->end_offset; ++i) {
+    const char op = c->operations[i];
+    const int cost = op == 'M'   ? earn
+                     : op == 'X' ? p->mismatch
+                                 : p->gap_extension + (last == op ? 0 : p->gap_opening);
+    trim_step(&w, op, cost);
+    last = op;
+    if (w.score > best) {
+      best = w.score;
+      best_i = i;
+      bv = w.v;
+      bh = w.h;
+    }
+  }
+  return maxtrim_apply(c, best, best_i, bv, bh);
+}
+static int trim_run_2p(char op, int len, const affine2p_penalties_t* p, int* v, int* h) {
+  if (op == 'M' || op == 'X') {
+    *v += len;
+    *h += len;
+    return (op == 'M' ? (p->match != 0 ? p->match : -1) : p->mismatch) * len;
+  }
+  if (op == 'I') *h += len;
+  else *v += len;
+  const int a = p->gap_opening1 + p->gap_extension1 * len;
+  const int b = p->gap_opening2 + p->gap_extension2 * len;
+  return a < b ? a : b;
+}
+bool cigar_maxtrim_gap_affine2p(cigar_t* const c, const affine2p_penalties_t* const p) {
+  if (c->begin_offset >= c->end_offset) return false;
+  int score = 0, v = 0, h = 0, run = 0;
+  int best = 0, best_i = c->begin_offset, bv = 0, bh = 0;
+  char last = '\0';
+  for (int i = c->begin_offset; i <= c->end_offset; ++i) {
+    const char op = i < c->end_offset ? c->operations[i] : '\0';
+    if (op != last && last != '\0') {  /* a run ends at i - 1 */
+      score -= trim_run_2p(last, run, p, &v, &h);
+      run = 0;
+      if (score > best) {
+        best = score;
+        best_i = i - 1;
+        bv = v;
+        bh = h;
+      }
+    }
+    last = op;
+    ++run;
+  }
+  return maxtrim_apply(c, best, best_i, bv, bh);
+}
+
 bool cigar_check_alignment(FILE* const stream, const char* const pattern,
                            const int pattern_length, const char* const text,
                            const int text_length, const cigar_t* const c, const bool verbose) {
