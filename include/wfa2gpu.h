@@ -325,7 +325,8 @@ void wavefront_aligner_set_heuristic_banded_adaptive(wavefront_aligner_t* const 
 /* wavefront/wfa.h:185-194 (wavefront/wavefront_aligner.c:606-645) */
 void wavefront_aligner_set_max_alignment_steps(wavefront_aligner_t* const wf_aligner,
     const int max_alignment_steps);
-/* wavefront/wavefront_aligner.h:54-66: CIGAR trimming and display */
+/* wavefront/wavefront_aligner.h:51-66: size, CIGAR trimming and display */
+uint64_t wavefront_aligner_get_size(wavefront_aligner_t* const wf_aligner);
 bool wavefront_aligner_maxtrim_cigar(wavefront_aligner_t* const wf_aligner);
 void wavefront_aligner_print_mode(FILE* const stream, wavefront_aligner_t* const wf_aligner);
 void wavefront_aligner_print_scope(FILE* const stream, wavefront_aligner_t* const wf_aligner);

@@ -631,6 +631,11 @@ void wavefront_server_delete(wavefront_server_t* const server) {
 }
 
 /* ------------------------------------------------------------ utilities and display */
+/* wavefront/wavefront_aligner.c:647-662: the memory the aligner holds; here
+ * the GPU engine's device and pinned host buffers */
+uint64_t wavefront_aligner_get_size(wavefront_aligner_t* const wf_aligner) {
+  return wf_aligner ? (uint64_t)wf2g_engine_bytes(wf_aligner->engine) : 0;
+}
 /* wavefront/wavefront_aligner.c:664-676: trims the aligner's CIGAR to its
  * maximal-score prefix under the user's penalties; edit and indel are not
  * trimmed */

@@ -125,6 +125,19 @@ extern "C" int64_t wf2g_engine_launches(const void* engine) {
   return engine ? ((const Engine*)engine)->launches : 0;
 }
 
+extern "C" int64_t wf2g_engine_bytes(const void* engine) {
+  if (!engine) return 0;
+  const Engine* E = (const Engine*)engine;
+  const DevBuf* bufs[] = {&E->seqs,   &E->poff,     &E->plen,     &E->toff,      &E->tlen,
+                          &E->scores, &E->status,   &E->ops,      &E->opsoff,    &E->opslen,
+                          &E->counters, &E->retry,  &E->scratch0, &E->scratch0b, &E->scratch1,
+                          &E->scratch2, &E->dstage, &E->dout,     &E->pool,      &E->poolctl,
+                          &E->endinfo};
+  int64_t total = (int64_t)E->hstage_cap;
+  for (const DevBuf* b : bufs) total += (int64_t)b->cap;
+  return total + wf2g_engine_bytes(E->twin);
+}
+
 // One persistent launch over a work list.
 struct Pass {
   int enc;          // 2 or 8 bits per staged base

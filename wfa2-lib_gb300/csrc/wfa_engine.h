@@ -52,6 +52,10 @@ int wf2g_engine_align(void* engine, const wf2g_cfg_t* cfg, int num_pairs, int on
 
 int64_t wf2g_engine_launches(const void* engine);
 
+/* Device and pinned host bytes the engine holds (its buffers grow on demand
+ * and are kept for the next call). */
+int64_t wf2g_engine_bytes(const void* engine);
+
 /* Allocation-free batch alignment on the current device (wfa_noalloc.cu):
  * device pointers only, scratch from a fixed array in the library image. */
 int wf2g_noalloc_align(const wf2g_cfg_t* cfg, int num_pairs, const char* d_seqs,
