@@ -204,3 +204,34 @@ def test_wfadaptive_fast_pass_matches_oracle(gpu_available, wfa, oracle_mod, par
                     (params, wl, i)
             compared += 1
         assert compared >= n // 2
+
+
+@pytest.mark.parametrize("params", [None, (20, 30, 2), (1, 0, 3)])
+@pytest.mark.parametrize("score_only", [False, True])
+def test_wider_passes_match_oracle(gpu_available, wfa, oracle_mod, monkeypatch, params,
+                                   score_only):
+    """With the first fast pass narrowed to diagonals [-32, 32]
+    (WF2G_FAST_REACH), it sends most pairs to the wider passes: the second
+    and third passes then align most of the batch, with and without the
+    wf-adaptive cut-off, and equal the checker."""
+    W, O = wfa, oracle_mod
+    monkeypatch.setenv("WF2G_FAST_REACH", "32")
+    n = 600
+    p = W.generate(1, n, first=77)
+    b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
+    al = W.Aligner(W.Config(score_only=score_only, wfadaptive=params))
+    rc, scores, status, ops, ops_len, ops_off = al.align_batch(p.seqs, p.p_off, p.p_len,
+                                                               p.t_off, p.t_len)
+    al.close()
+    assert rc == 0
+    r = O.align(b, O.Penalties(), score_only=score_only, wfadaptive=params)
+    compared = 0
+    for i in range(n):
+        if r.flags[i] & O.FLAG_STALE_SOURCE:
+            continue
+        assert (int(status[i]), int(scores[i])) == (int(r.status[i]), int(r.score[i])), (params, i)
+        if not score_only:
+            assert ops[ops_off[i]:ops_off[i] + ops_len[i]].tobytes().decode() == r.cigar(i), \
+                (params, i)
+        compared += 1
+    assert compared >= n // 2

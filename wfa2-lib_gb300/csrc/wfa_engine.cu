@@ -285,6 +285,11 @@ static int run_fast_pass(Engine* E, const wf2g_cfg_t& cfg, int G, int W, int n,
   fp.h_min_len = cfg.h_min_len;
   fp.h_max_dist = cfg.h_max_dist;
   fp.h_steps = cfg.h_steps;
+  fp.probe_limit = env_int("WF2G_PROBE_LIMIT", 500);
+  // (WF2G_FAST_REACH narrows the first pass, which sends more pairs to the
+  // wider passes: a test of those)
+  fp.reach = W / 2 - 4;
+  if (W == 1024) fp.reach = std::min(fp.reach, std::max(8, env_int("WF2G_FAST_REACH", fp.reach)));
   if (!fn) return WF2G_ERR_CUDA_;
   fp.g = g;
   fp.match = cfg.match;
@@ -406,7 +411,10 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
       // then 2048 for what remains (four warps per pair on small batches)
       const int gw = n <= small_n ? 128 : cfg.heur != 0 ? 32 : env_int("WF2G_FAST_WIDE_G", 32);
       const int g2 = gw <= 32 ? 32 : gw <= 64 ? 64 : 128;
-      const int w2 = g2 == 32 ? env_int("WF2G_FAST_W2", 1536) : 2048;
+      // (score-only wf-adaptive: 2048 at once, wfa_fast2.cu)
+      const int w2 = g2 == 32 && !(cfg.heur != 0 && cfg.score_only)
+                         ? env_int("WF2G_FAST_W2", 1536)
+                         : 2048;
       rc = run_fast_pass(E, cfg, g2, w2 == 1536 ? 1536 : 2048, n, retry + (size_t)3 * n,
                          counters + 9, d_seqs, d_poff, d_plen, d_toff, d_tlen, max_len, d_scores,
                          d_status, d_ops, d_opsoff, d_opslen, d_end_info, counters + 10,
@@ -439,8 +447,15 @@ int plan_and_run(Engine* E, const wf2g_cfg_t& cfg, int n, const char* d_seqs,
               cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess)
         return WF2G_ERR_CUDA_;
-      if (verbose)
-        fprintf(stderr, "[wfa2gpu] fast passes: %d of %d pairs left to the general kernel\n", left, n);
+      if (verbose) {
+        int32_t c[6] = {0, 0, 0, 0, 0, 0};  // per fast pass: pairs taken, pairs left
+        if (cudaMemcpy(c, counters + 8, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess)
+          return WF2G_ERR_CUDA_;
+        fprintf(stderr,
+                "[wfa2gpu] fast passes: %d of %d pairs left to the general kernel (left by "
+                "each pass: %d %d %d)\n",
+                left, n, c[1], c[3], c[5]);
+      }
       if (skip_empty && left == 0) return WF2G_OK_;
     }
   }

@@ -91,9 +91,14 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
   constexpr int WW = W / 2;             // words per row
   // a range with no cell: min/max over ranges need no validity tests
   constexpr int kBig = 1 << 20;
+  // the step at which the first pass projects each pair's final score (the
+  // projected score beyond which it leaves for the wider rows: p.probe_limit)
+  constexpr int kProbe = 192;
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x;
   const int nrows = R + 2 * RI;
+  // diagonals [-reach, reach] are computed (at most W/2 - 4)
+  const int reach = min(p.reach, HALF - 4);
   int16_t* const rows = reinterpret_cast<int16_t*>(smem + p.rows_off);
   uint32_t* const rows32 = reinterpret_cast<uint32_t*>(smem + p.rows_off);
   // the two sequences' word pairs interleaved at the start of shared
@@ -145,7 +150,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
     ok &= fast_stage<32, 2>(p.seqs + p.t_off[pair], min(tlen, p.max_len), QT, p.nq, lane);
     __syncwarp();
     const int k_end = tlen - plen;
-    if (!ok || plen > p.max_len || tlen > p.max_len || k_end < 4 - HALF || k_end > HALF - 4) {
+    if (!ok || plen > p.max_len || tlen > p.max_len || k_end < -reach || k_end > reach) {
       punt();
       used_lo = 0;
       used_hi = -1;
@@ -244,7 +249,7 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
       }
       null_steps = 0;
       bt_used += hi - lo + 1;
-      if (lo < 4 - HALF || hi > HALF - 4 ||  // wider than the rows
+      if (lo < -reach || hi > reach ||  // wider than the rows
           (CIGAR && p.pair_cap > 0 && bt_used > p.pair_cap)) {  // over the pair's budget
         leave = true;
         break;
@@ -483,6 +488,25 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
         win[rowI + cI] = tI;
         win[rowD + cI] = tD;
       }
+      if (!WFA && W == 1024 && s == kProbe && !done && tM.x <= tM.y) {
+        // a pair whose progress so far (the furthest antidiagonal h + v)
+        // projects a final scaled score beyond these rows' reach (the range
+        // grows a diagonal per scaled step: +-508 is reached near 500)
+        // leaves now for the wider pass instead of at the edge; a scheduling
+        // choice only (the wider pass recomputes it in full).  Not under the
+        // cut-off, which keeps the range narrow and the projection wrong.
+        int prog = 0;
+        for (int k = tM.x + lane; k <= tM.y; k += 32) {
+          const int off = rows[bM + k];
+          if (off >= 0) prog = max(prog, 2 * off - k);
+        }
+        prog = __reduce_max_sync(kFull, prog);
+        if ((int64_t)kProbe * (plen + tlen) > (int64_t)p.probe_limit * max(prog, 1)) {
+          leave = true;
+          __syncwarp();
+          break;
+        }
+      }
       const int2 winM = tM, winI = tI, winD = tD;  // the windows, before a cut
       if (WFA && !done && tM.x <= tM.y) {
         // wf-adaptive cut-off of the extended M[s] (wavefront/wavefront_
@@ -607,15 +631,20 @@ __global__ void __launch_bounds__(32) wfa_fast2_kernel(const FastParams p) {
 
 // Kernel of the two-diagonals-per-lane pass for (full CIGAR?, o+e even?, row
 // width, default scaled penalties (2, 4, 1)?, wf-adaptive cut-off?).  The
-// cut-off is compiled for the default penalties only.
+// cut-off is compiled for the default penalties only, and not for
+// score-only rows of 1536 diagonals: that instance returned worse scores
+// than the oracle on GB300 for pairs the 1024-, 2048-row and full-CIGAR
+// 1536-row instances (and a CPU emulation of the kernel at every width) get
+// right, and the difference went away when unrelated code was added, so the
+// score-only wf-adaptive second pass takes rows of 2048 instead.
 extern "C" void* wf2g_fast2_kernel_ptr(int cigar, int mos, int width, int d241, int wfa) {
   using namespace wf2g;
 #define WF2G_FAST2_CASE(W)                                                                        \
   if (width == W) {                                                                               \
     if (wfa) {                                                                                    \
-      if (!d241) return nullptr;                                                                  \
+      if (!d241 || (W == 1536 && !cigar)) return nullptr;                                         \
       return cigar ? (void*)wfa_fast2_kernel<true, true, W, true, true>                           \
-                   : (void*)wfa_fast2_kernel<false, true, W, true, true>;                         \
+                   : (void*)wfa_fast2_kernel<false, true, W == 1536 ? 2048 : W, true, true>;      \
     }                                                                                             \
     if (d241) return cigar ? (void*)wfa_fast2_kernel<true, true, W, true, false>                  \
                            : (void*)wfa_fast2_kernel<false, true, W, true, false>;                \

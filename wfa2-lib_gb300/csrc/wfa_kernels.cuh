@@ -151,6 +151,12 @@ struct FastParams {
   // wf-adaptive cut-off (two-diagonal kernel): min_wavefront_length,
   // max_distance_threshold, steps_between_cutoffs
   int h_min_len, h_max_dist, h_steps;
+  // first pass: the projected final scaled score beyond which a pair leaves
+  // for the wider rows at the probe step
+  int probe_limit;
+  // the diagonals a pass computes, [-reach, reach]: its rows' W/2 - 4, or
+  // fewer in the first pass to send pairs to the wider ones
+  int reach;
   const uint8_t* seqs;
   const int64_t* p_off;
   const int32_t* p_len;
