@@ -126,8 +126,13 @@ common:
   if (p->endsfree && (p->pbf < 0 || p->pef < 0 || p->tbf < 0 || p->tef < 0)) return -1;
   /* edit and indel never widen the score-0 wavefront's initialised window
    * [0,0] (wavefront/wavefront_compute_edit.c:321-374), so their back-trace
-   * reads begin-free diagonals as sourceless: not restated */
-  if (p->endsfree && !p->extension && p->metric <= 1 && (p->pbf > 0 || p->tbf > 0)) return -1;
+   * reads begin-free diagonals as sourceless (wavefront/wavefront_backtrace.c:
+   * 62-75) and can end in matches over mismatches: a full alignment is not
+   * restated.  The score-only search reads the begin-free cells by their
+   * limits and is. */
+  if (p->endsfree && !p->extension && p->metric <= 1 && (p->pbf > 0 || p->tbf > 0) &&
+      !p->score_only)
+    return -1;
   return 0;
 }
 

@@ -143,6 +143,11 @@ ENDSFREE = {
     "w1_linear_m1_ef_begin": (1, 150, "linear.m1", False, 0, 0, (30, 10, 30, 10), None),
     "w1_affine_p4_ef_begin_wfapt": (1, 150, "affine.p4", False, 0, 0, (15, 15, 15, 15),
                                     (10, 50, 1)),
+    # edit and indel with begin-free lengths, score only (a full alignment's
+    # back-trace reads the begin-free diagonals as sourceless)
+    "w1_edit_ef_begin_score": (1, 200, "edit", True, 0, 0, (20, 20, 20, 20), None),
+    "w0_edit_ef_bounds_score": (0, 300, "edit", True, 0, 0, (99, 99, 99, 99), None),
+    "w5_indel_ef_begin_score": (5, 60, "indel", True, 500, 100, (40, 0, 40, 0), None),
 }
 
 

@@ -122,11 +122,15 @@ def test_endsfree_dropin_cigar_fields(gpu_available, wfa, oracle_mod):
 
 def test_endsfree_rejections(gpu_available, wfa):
     """Forms the GPU path does not serve fail loudly: BiWFA with free ends (the
-    reference exits, wavefront/wavefront_align.c:67-82), and serving with free
-    ends (its BiWFA fallback)."""
+    reference exits, wavefront/wavefront_align.c:67-82), edit/indel with
+    begin-free lengths and a full alignment (the reference's back-trace reads
+    the begin-free diagonals as sourceless; their score-only form is served),
+    and serving with free ends (its BiWFA fallback)."""
     W = wfa
     p = W.generate(1, 4, first=3)
-    for cfg in [W.Config(form=(5, 5, 5, 5), memory_mode=W.MEM_ULTRALOW)]:
+    for cfg in [W.Config(form=(5, 5, 5, 5), memory_mode=W.MEM_ULTRALOW),
+                W.Config(metric=W.EDIT, form=(5, 0, 0, 0)),
+                W.Config(metric=W.INDEL, form=(0, 0, 5, 0))]:
         al = W.Aligner(cfg)
         rc = al.align_batch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)[0]
         al.close()

@@ -91,6 +91,26 @@ def test_linear_metrics_endsfree(gpu_available, wfa, oracle_mod, name, form):
         assert got[i] == want, (name, form, i)
 
 
+@pytest.mark.parametrize("name", ["indel", "edit"])
+@pytest.mark.parametrize("form", [(20, 20, 20, 20), (0, 0, 60, 5), (45, 0, 0, 0)])
+@pytest.mark.parametrize("case", [(1, 150, 0, 0), (5, 40, 400, 300), (6, 8, 3000, 200)])
+def test_edit_indel_begin_free_score_only(gpu_available, wfa, oracle_mod, name, form, case):
+    """Edit and indel with begin-free lengths, score only: M[0] spans
+    [-pattern_begin_free, text_begin_free] and the edit driver reads it by its
+    limits (wavefront/wavefront_aligner.c:250-305,
+    wavefront/wavefront_compute_edit.c:321-374); score, status and end
+    position equal the checker's."""
+    W, O = wfa, oracle_mod
+    wl, n, param, param2 = case
+    pen = PENS[name]
+    p = W.generate(wl, n, first=57, param=param, param2=param2)
+    got = _gpu(W, W.Config(**pen, form=form, score_only=True), p, ends=True)
+    r = _oracle(O, pen, p, form=form, score_only=True)
+    for i in range(p.n):
+        want = (int(r.status[i]), int(r.score[i]), "", (int(r.end[i][0]), int(r.end[i][1])))
+        assert got[i] == want, (name, form, case, i)
+
+
 def test_linear_metrics_dropin(gpu_available, wfa, oracle_mod):
     """wavefront_align() per pair with edit and gap-linear attributes."""
     W, O = wfa, oracle_mod
@@ -123,8 +143,8 @@ def test_linear_metrics_biwfa(gpu_available, wfa, oracle_mod, name, case, score_
 
 
 def test_linear_metrics_rejections(gpu_available, wfa):
-    """Edit/indel begin-free lengths are not served; serving takes the
-    gap-affine metrics only."""
+    """Edit/indel begin-free lengths with a full alignment are not served
+    (score only is); serving takes the gap-affine metrics only."""
     W = wfa
     p = W.generate(1, 4, first=3)
     for cfg in [W.Config(metric=0, form=(5, 5, 5, 5))]:

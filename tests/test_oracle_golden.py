@@ -140,9 +140,11 @@ def test_oracle_heuristic_rejections(oracle_mod, wfa):
 def test_oracle_endsfree_rejections(oracle_mod, wfa):
     """Forms the restatement does not serve fail loudly: BiWFA with any
     ends-free form (the reference exits, wavefront/wavefront_align.c:67-82) and
-    edit/indel with begin-free lengths.  Begin-free lengths with match < 0
-    (re-entry at multiples of -match, wavefront/wavefront_compute.c:124-262)
-    are served and pinned to the ends-free fixtures."""
+    edit/indel with begin-free lengths and a full alignment (the reference's
+    back-trace reads the begin-free diagonals as sourceless).  Their
+    score-only form, and begin-free lengths with match < 0 (re-entry at
+    multiples of -match, wavefront/wavefront_compute.c:124-262), are served
+    and pinned to the ends-free fixtures."""
     O, W = oracle_mod, wfa
     p = W.generate(1, 4, first=3)
     b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
@@ -150,6 +152,10 @@ def test_oracle_endsfree_rejections(oracle_mod, wfa):
         O.align(b, O.Penalties(), memory_mode=O.MEM_ULTRALOW, form=(5, 5, 5, 5))
     with pytest.raises(ValueError):
         O.align(b, O.Penalties(O.EDIT), form=(5, 0, 0, 0))
+    with pytest.raises(ValueError):
+        O.align(b, O.Penalties(O.INDEL), form=(0, 0, 5, 0))
+    O.align(b, O.Penalties(O.EDIT), form=(5, 0, 0, 0), score_only=True)
+    O.align(b, O.Penalties(O.INDEL), form=(0, 0, 5, 0), score_only=True)
     O.align(b, O.Penalties(match=-1), form=(5, 0, 0, 0))
     O.align(b, O.Penalties(match=-1), form=(0, 5, 0, 5))
     O.align(b, O.Penalties(match=-1), form="extension")

@@ -355,8 +355,12 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
     if (cfg->pbf < 0 || cfg->pef < 0 || cfg->tbf < 0 || cfg->tef < 0) return -1;
     /* edit and indel never widen the score-0 wavefront's initialised window
      * (wavefront/wavefront_compute_edit.c:321-374), so their back-trace reads
-     * begin-free diagonals as sourceless: not computed */
-    if (!cfg->extension && p->distance_metric <= edit && (cfg->pbf > 0 || cfg->tbf > 0)) return -1;
+     * begin-free diagonals as sourceless and can end in matches over
+     * mismatches: a full alignment is not computed.  The score-only search
+     * is (it reads those cells by their limits). */
+    if (!cfg->extension && !cfg->score_only && p->distance_metric <= edit &&
+        (cfg->pbf > 0 || cfg->tbf > 0))
+      return -1;
   }
   /* the user's penalties, for maximal-score trimming (wavefront/wavefront_aligner.c:664-676) */
   if (lin) {
