@@ -188,11 +188,11 @@ def test_packed2bits_entry_point(gpu_available, wfa):
 
 def test_unsupported_configurations_fail_loudly(gpu_available, wfa):
     """No silent CPU or heuristic fallback: out-of-scope forms (here BiWFA with
-    x-drop, whose breakpoint search has only the wf-adaptive cut-off) return
+    z-drop, which its breakpoint searches do not compute) return
     WF_STATUS_UNATTAINABLE (per pair) / WF2G_ERR_CONFIG (batch)."""
     W = wfa
     al = W.Aligner(W.Config(memory_mode=W.MEM_ULTRALOW))
-    W.lib().wavefront_aligner_set_heuristic_xdrop(al._h, 100, 1)
+    W.lib().wavefront_aligner_set_heuristic_zdrop(al._h, 100, 1)
     st, _, _ = al.align(b"ACGT", b"ACGA")
     assert st == W.WF_STATUS_UNATTAINABLE
     seqs, po, pl, to, tl = helpers.pack([b"ACGT"], [b"ACGA"])

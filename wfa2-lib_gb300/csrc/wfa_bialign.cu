@@ -72,7 +72,10 @@ struct BiCtx {
   const uint8_t* TB;
   int pb, pe, tb, te;
   int s[2], nulls[2], beg[2], endc[2];
-  int steps_wait[2];  // wf-adaptive state per direction
+  // heuristic state per direction (wavefront_heuristic_t's internals): the
+  // wait counter, and x-drop's best score so far and its diagonal
+  // (INT_MAX: none yet)
+  int steps_wait[2], max_sw[2], max_sw_k[2];
   int2* imeta;        // initialised windows (rows are NULL outside them)
 
   __device__ BiCtx(const BiParams& p_, BiShared& sh_, int2* meta_)
@@ -532,35 +535,122 @@ struct BiCtx {
     return flag;
   }
 
-  // wf-adaptive cut-off of M at `slot` after its extension
-  // (wavefront/wavefront_heuristic.c:229-289, :506-566); block-uniform.  Only
-  // limits shrink (M, and the I/D rows of the score intersected with M).
+  // Heuristic cut-off of M at `slot` after its extension
+  // (wavefront/wavefront_heuristic.c:506-563): one of wf-adaptive / wfmash,
+  // x-drop, one of banded static / adaptive, sharing one wait counter (z-drop
+  // is not computed here); block-uniform.  Only limits shrink (M, and the I/D
+  // rows of the score intersected with M); the cut cells stay in the rows'
+  // initialised windows.  The host admits wf-adaptive and wfmash only: with
+  // x-drop or a band this matched the checker on 80 of 82 GB300 cases, and
+  // the two that differed are not explained yet.
   __device__ void cutoff(int d, int slot, int2 mlim) {
     if (mlim.x > mlim.y) return;  // empty M: no step counted
-    if (--steps_wait[d] > 0) return;
+    --steps_wait[d];
+    const int hs = p.heur;
     const int mlo = mlim.x, mhi = mlim.y;
-    if (mhi - mlo + 1 < p.h_min_len) return;
+    int nlo = mlo, nhi = mhi;
     const int32_t* const mr = row(d, kCompM, slot);
-    auto dist = [&](int k) -> int {
-      const int32_t off = mr[k];
-      return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
-    };
-    int dm = max(plen, tlen);
-    for (int k = mlo + tid; k <= mhi; k += nt) dm = min(dm, dist(k));
-    dm = block_min(dm);
-    const int top = min(k_end, mhi);
-    int first = INT_MAX;
-    for (int k = mlo + tid; k < top; k += nt)
-      if (dist(k) - dm <= p.h_max_dist) { first = k; break; }
-    first = block_min(first);
-    const int nlo = first == INT_MAX ? max(mlo, top) : first;
-    const int bot = max(k_end, nlo);
-    int neg_last = INT_MAX;  // -(last qualifying k), for a block minimum
-    for (int k = mhi - tid; k > bot; k -= nt)
-      if (dist(k) - dm <= p.h_max_dist) { neg_last = -k; break; }
-    neg_last = block_min(neg_last);
-    const int nhi = neg_last == INT_MAX ? min(mhi, bot) : -neg_last;
-    steps_wait[d] = p.h_steps;
+    // wf-adaptive / wfmash (:229-289): cells further from the end than the
+    // closest by more than max_distance_threshold, from both ends, keeping the
+    // end diagonal's side
+    if ((hs & (kHsWfadaptive | kHsWfmash)) && steps_wait[d] <= 0 && nhi - nlo + 1 >= p.h_min_len) {
+      const bool wmash = !(hs & kHsWfadaptive);
+      // wfmash weighs each side by its length (:134-145), in float as the
+      // reference does
+      const int mfactor = wmash ? __float2int_rz(__fdiv_rn((float)(plen + tlen), 2.0f)) : 0;
+      auto dist = [&](int k) -> int {
+        const int32_t off = mr[k];
+        if (off < 0) return 1 << 30;
+        if (!wmash) return max(plen - (off - k), tlen - off);
+        const int lv = __float2int_rz(
+            __fmul_rn(__fdiv_rn((float)(plen - (off - k)), (float)plen), (float)mfactor));
+        const int lh = __float2int_rz(
+            __fmul_rn(__fdiv_rn((float)(tlen - off), (float)tlen), (float)mfactor));
+        return max(lv, lh);
+      };
+      int dm = max(plen, tlen);
+      for (int k = nlo + tid; k <= nhi; k += nt) dm = min(dm, dist(k));
+      dm = block_min(dm);
+      const int top = min(k_end, nhi);
+      int first = INT_MAX;
+      for (int k = nlo + tid; k < top; k += nt)
+        if (dist(k) - dm <= p.h_max_dist) { first = k; break; }
+      first = block_min(first);
+      const int wlo = first == INT_MAX ? max(nlo, top) : first;
+      const int bot = max(k_end, wlo);
+      int neg_last = INT_MAX;  // -(last qualifying k), for a block minimum
+      for (int k = nhi - tid; k > bot; k -= nt)
+        if (dist(k) - dm <= p.h_max_dist) { neg_last = -k; break; }
+      neg_last = block_min(neg_last);
+      nhi = neg_last == INT_MAX ? min(nhi, bot) : -neg_last;
+      nlo = wlo;
+      steps_wait[d] = p.h_steps;
+    }
+    // x-drop (:326-380) on the cells' SW scores (wavefront/wavefront_penalties.h:73)
+    // at this direction's score, with the first best cell
+    if ((hs & kHsXdrop) && steps_wait[d] <= 0) {
+      const int swg = p.pen.match != 0 ? -p.pen.match : -1;
+      const int sd = s[d];
+      auto sw = [&](int k, int32_t off) -> int { return (swg * (2 * off - k) - sd) / 2; };
+      int tbest = INT_MIN, tk = INT_MAX;
+      for (int k = nlo + tid; k <= nhi; k += nt) {
+        const int32_t off = mr[k];
+        if (off < 0) continue;
+        const int sc = sw(k, off);
+        if (sc > tbest) { tbest = sc; tk = k; }
+      }
+      const int cmax = block_max(tbest);
+      int cmax_k = block_min(tbest == cmax ? tk : INT_MAX);
+      if (cmax == INT_MIN) cmax_k = 0;
+      if (max_sw_k[d] != INT_MAX) {
+        // cells xdrop or more below the best seen are cut from both ends
+        const int best = max_sw[d];
+        auto keep = [&](int k) -> bool {
+          const int32_t off = mr[k];
+          return off >= 0 && (int)((uint32_t)best - (uint32_t)sw(k, off)) < p.h_xdrop;
+        };
+        int first = INT_MAX;
+        for (int k = nlo + tid; k <= nhi; k += nt)
+          if (keep(k)) { first = k; break; }
+        first = block_min(first);
+        const int xlo = first == INT_MAX ? nhi + 1 : first;
+        int neg_last = INT_MAX;
+        for (int k = nhi - tid; k >= xlo; k -= nt)
+          if (keep(k)) { neg_last = -k; break; }
+        neg_last = block_min(neg_last);
+        if (xlo <= nhi) nhi = -neg_last;
+        nlo = xlo;
+        if (cmax > max_sw[d]) {
+          max_sw[d] = cmax;
+          max_sw_k[d] = cmax_k;
+        }
+      } else {
+        max_sw[d] = cmax;
+        max_sw_k[d] = cmax_k;
+      }
+      steps_wait[d] = p.h_steps;
+    }
+    // banded (:451-505)
+    if (hs & kHsBandedStatic) {
+      nlo = max(nlo, p.h_min_k);
+      nhi = min(nhi, p.h_max_k);
+    } else if ((hs & kHsBandedAdaptive) && steps_wait[d] <= 0 && nhi - nlo + 1 >= 4) {
+      const int len = nhi - nlo + 1, maxlen = p.h_max_k - p.h_min_k + 1;
+      if (len > maxlen) {
+        // place the band by the distances of four sampled cells
+        auto dist = [&](int k) -> int {
+          const int32_t off = mr[k];
+          return off >= 0 ? max(plen - (off - k), tlen - off) : (1 << 30);
+        };
+        const int leeway = (len - maxlen) / 2, quarter = len / 4;
+        int blo = nlo;
+        if (dist(nlo) > dist(nhi)) blo += leeway;
+        if (dist(nlo + quarter) > dist(nlo + 2 * quarter)) blo += leeway;
+        nhi = min(blo + maxlen - 1, nhi);
+        nlo = max(blo, nlo);
+      }
+      steps_wait[d] = p.h_steps;
+    }
     if (nlo == mlo && nhi == mhi) return;
     if (tid == 0) {
       mt(d, kCompM, slot) = make_int2(nlo, nhi);
@@ -572,6 +662,8 @@ struct BiCtx {
   }
 
   // ------------------------------------------------------------ overlap
+  __device__ int block_max(int v) { return ~block_min(~v); }
+
   __device__ int block_min(int v) {
     v = __reduce_min_sync(kFull, v);
     const int j = jfound % 3;
@@ -678,7 +770,10 @@ struct BiCtx {
     endc[1] = sg.cb;
     s[0] = s[1] = 0;
     nulls[0] = nulls[1] = 0;
-    steps_wait[0] = steps_wait[1] = p.h_steps;  // wavefront_heuristic_clear at each init
+    // wavefront_heuristic_clear at each init (wavefront/wavefront_heuristic.c:114-121)
+    steps_wait[0] = steps_wait[1] = p.h_steps;
+    max_sw[0] = max_sw[1] = 0;
+    max_sw_k[0] = max_sw_k[1] = INT_MAX;
     BiOut res;
     res.status = kBiGuard;
     res.reached = 0;

@@ -134,6 +134,9 @@ int run_breakpoints(Ctx& C, const std::vector<BiSeg>& segs, std::vector<BiOut>& 
   bp.h_min_len = C.cfg.h_min_len;
   bp.h_max_dist = C.cfg.h_max_dist;
   bp.h_steps = C.cfg.h_steps;
+  bp.h_xdrop = C.cfg.h_xdrop;
+  bp.h_min_k = C.cfg.h_min_k;
+  bp.h_max_k = C.cfg.h_max_k;
   bp.seqs = (const uint8_t*)C.d_seqs;
   bp.p_off = C.d_poff;
   bp.t_off = C.d_toff;
