@@ -34,7 +34,7 @@ def _spec(name):
 
 def _served(metric, score_only, strategy, memory_mode=0):
     """The GPU's refusals (make_cfg in wfa2-lib_gb300/csrc/wfa_aligner.c)."""
-    return not (memory_mode == 3 and strategy & ~0x44)  # BiWFA: wf-adaptive, wfmash
+    return not (memory_mode == 3 and strategy & 0x20)  # BiWFA: no z-drop
 
 
 def _gpu(W, cfg, b):
@@ -143,15 +143,13 @@ def test_heuristics_match_oracle(gpu_available, wfa, oracle_mod, case, hname, sp
 
 def test_heuristic_rejections(gpu_available, wfa):
     """Drops with edit/indel (the reference exits, wavefront/wavefront_align.c:
-    83-89), BiWFA with a heuristic other than wf-adaptive or wfmash, and
-    serving with a heuristic other than wf-adaptive are refused loudly."""
+    83-89), BiWFA with z-drop, and serving with a heuristic other than
+    wf-adaptive are refused loudly."""
     W = wfa
     p = W.generate(1, 4, first=3)
     for cfg in [W.Config(metric=W.EDIT, heuristic=dict(strategy=0x10, xdrop=20)),
                 W.Config(metric=W.INDEL, heuristic=dict(strategy=0x20, zdrop=20)),
-                W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x20, zdrop=50)),
-                W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x01, min_k=-9,
-                                                                    max_k=9))]:
+                W.Config(memory_mode=W.MEM_ULTRALOW, heuristic=dict(strategy=0x20, zdrop=50))]:
         al = W.Aligner(cfg)
         st, _, _ = al.align(bytes(p.seqs[p.p_off[0]:p.p_off[0] + p.p_len[0]]),
                             bytes(p.seqs[p.t_off[0]:p.t_off[0] + p.t_len[0]]))
@@ -169,10 +167,11 @@ def test_biwfa_heuristics_match_oracle(gpu_available, wfa, oracle_mod, hname, sp
                                        score_only, wl):
     """BiWFA (ultralow memory): the forward and reverse breakpoint searches
     inherit the heuristic (wavefront/wavefront_bialigner.c:48-56), each
-    direction with its own wait counter, cleared at every search; the base
-    cases take none.  wfmash is computed and its scores, statuses and CIGARs
-    equal the checker's (0.5-1.5 kbp pairs, and random-tail pairs); x-drop and
-    the bands are refused (WF2G_ERR_CONFIG)."""
+    direction with its own wait counter and x-drop best, cleared at every
+    search, and each step's range widened by its null inputs as the
+    reference's is; the base cases take none.  Scores, statuses and CIGARs
+    equal the checker's (0.5-1.5 kbp pairs, and random-tail pairs where the
+    cuts end searches)."""
     W, O = wfa, oracle_mod
     spec = _spec(spec_name)
     p = W.generate(wl, 40, first=5)

@@ -320,9 +320,8 @@ static int make_cfg(const wavefront_aligner_t* wf, wf2g_cfg_t* cfg) {
   if ((strategy & (wf_heuristic_xdrop | wf_heuristic_zdrop)) && p->distance_metric <= edit)
     return -1;
   /* BiWFA's searches inherit the heuristic (wavefront/wavefront_bialigner.c:
-   * 48-56): computed with wf-adaptive or wfmash (or none) */
-  if (wf->memory_mode == wavefront_memory_ultralow &&
-      (strategy & ~(wf_heuristic_wfadaptive | wf_heuristic_wfmash)))
+   * 48-56); z-drop is not computed there */
+  if (wf->memory_mode == wavefront_memory_ultralow && (strategy & wf_heuristic_zdrop))
     return -1;
   cfg->metric = (int)p->distance_metric;
   cfg->match = p->match;

@@ -288,14 +288,35 @@ struct BiCtx {
 
     // wavefront/wavefront_compute.c:40-87: output range
     int lo = INT_MAX, hi = INT_MIN;
-    if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
-    if (vMo1) { lo = min(lo, eMo1.x - 1); hi = max(hi, eMo1.y + 1); }
-    if (vI1) { lo = min(lo, eI1.x + 1); hi = max(hi, eI1.y + 1); }
-    if (vD1) { lo = min(lo, eD1.x - 1); hi = max(hi, eD1.y - 1); }
-    if (A2P) {
-      if (vMo2) { lo = min(lo, eMo2.x - 1); hi = max(hi, eMo2.y + 1); }
-      if (vI2) { lo = min(lo, eI2.x + 1); hi = max(hi, eI2.y + 1); }
-      if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
+    if (p.heur && p.metric >= 2) {
+      // The reference widens the range by every input, a null one with the
+      // all-NULL wavefront's limits [1,-1] (wavefront/wavefront.c:110-117),
+      // so the range reaches diagonal 0.  Exact runs read only NULLs out
+      // there; under a cut-off the rows' windows can still hold cells.
+      const int2 nl = make_int2(1, -1);
+      const int2 lMx = vMx ? eMx : nl, lMo1 = vMo1 ? eMo1 : nl;
+      lo = min(lMx.x, lMo1.x - 1);
+      hi = max(lMx.y, lMo1.y + 1);
+      if (!lin) {  // gap-linear stops at the mismatch and open inputs
+        const int2 lI1 = vI1 ? eI1 : nl, lD1 = vD1 ? eD1 : nl;
+        lo = min(lo, min(lI1.x + 1, lD1.x - 1));
+        hi = max(hi, max(lI1.y + 1, lD1.y - 1));
+      }
+      if (A2P) {
+        const int2 lMo2 = vMo2 ? eMo2 : nl, lI2 = vI2 ? eI2 : nl, lD2 = vD2 ? eD2 : nl;
+        lo = min(lo, min(lMo2.x - 1, min(lI2.x + 1, lD2.x - 1)));
+        hi = max(hi, max(lMo2.y + 1, max(lI2.y + 1, lD2.y - 1)));
+      }
+    } else {
+      if (vMx) { lo = min(lo, eMx.x); hi = max(hi, eMx.y); }
+      if (vMo1) { lo = min(lo, eMo1.x - 1); hi = max(hi, eMo1.y + 1); }
+      if (vI1) { lo = min(lo, eI1.x + 1); hi = max(hi, eI1.y + 1); }
+      if (vD1) { lo = min(lo, eD1.x - 1); hi = max(hi, eD1.y - 1); }
+      if (A2P) {
+        if (vMo2) { lo = min(lo, eMo2.x - 1); hi = max(hi, eMo2.y + 1); }
+        if (vI2) { lo = min(lo, eI2.x + 1); hi = max(hi, eI2.y + 1); }
+        if (vD2) { lo = min(lo, eD2.x - 1); hi = max(hi, eD2.y - 1); }
+      }
     }
     if (!ensure_extent(lo - 1, hi + 1)) return 3;
     // what the reused slots hold outside [lo,hi]
@@ -540,9 +561,7 @@ struct BiCtx {
   // x-drop, one of banded static / adaptive, sharing one wait counter (z-drop
   // is not computed here); block-uniform.  Only limits shrink (M, and the I/D
   // rows of the score intersected with M); the cut cells stay in the rows'
-  // initialised windows.  The host admits wf-adaptive and wfmash only: with
-  // x-drop or a band this matched the checker on 80 of 82 GB300 cases, and
-  // the two that differed are not explained yet.
+  // initialised windows.
   __device__ void cutoff(int d, int slot, int2 mlim) {
     if (mlim.x > mlim.y) return;  // empty M: no step counted
     --steps_wait[d];

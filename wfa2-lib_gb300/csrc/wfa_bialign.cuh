@@ -42,8 +42,8 @@ struct BiParams {
   int metric;
   int scope;      // max_score_scope: ring depth of every component
   int max_steps;
-  // heuristic of the forward/reverse searches (strategy bits, 0: none; the
-  // host admits wf-adaptive and wfmash) and its parameters
+  // heuristic of the forward/reverse searches (strategy bits, 0: none; no
+  // z-drop) and its parameters
   int heur, h_min_len, h_max_dist, h_steps;
   int h_xdrop, h_min_k, h_max_k;
   // sequences: caller bytes, and the 2-bit packed copy of ACGT-only pairs
