@@ -1299,8 +1299,21 @@ static void align_one_impl(oracle_ws_t* ws, const pen_t* p, const char* P, int p
     status = oracle_ua_extend(&ua, NULL);
     if (status) break;
     oracle_ua_compute(&ua);
+    /* Edit and indel: a null wavefront does not end the reference's
+     * alignment.  Its extend step counts null steps only for a missing
+     * wavefront (wavefront/wavefront_extend.c:93-101), and the edit driver
+     * allocates every one (wavefront/wavefront_compute_edit.c:321-374).  No
+     * later cell can be valid, so only the step limit ends it.  Without a
+     * step limit the reference never ends; the checker ends it as
+     * unreachable instead. */
+    if (p->metric <= 1 && ua.null_steps >= INT_MAX / 2 && p->max_steps != INT_MAX)
+      ua.s = p->max_steps;
     /* wavefront/wavefront_unialign.c:102-107 */
     if (ua.s >= p->max_steps) {
+      /* the reference exits before the step limit once the score passes its
+       * wavefront table (wavefront/wavefront_compute.c:442-446) */
+      if (!p->score_only && ua.s >= score_table_size(p, plen, tlen))
+        *flags |= ORACLE_FLAG_OVER_BOUND;
       if (ext) *ext = ua.ext;
       if (cells) *cells = ua.cells;
       *out_score = -p->max_steps;

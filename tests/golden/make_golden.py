@@ -218,6 +218,15 @@ HEURISTIC_SETS = {
     "w1_affine_p4_biwfa_wfmash_score": (1, 60, "affine.p4", True, 0, 0, None,
                                         _h(WM, min_wavefront_length=10, max_distance_threshold=50,
                                            steps_between_cutoffs=1), 3),
+    # edit and indel whose band leaves the end outside: the null wavefronts do
+    # not end the alignment (wavefront/wavefront_extend.c:93-101), the step
+    # limit (the optional tenth field) does
+    "w6_indel_bstatic_score_ms": (6, 20, "indel", True, 0, 0, None,
+                                  _h(BS, min_k=-30, max_k=30), 0, 3000),
+    "w6_edit_bstatic_ef_score_ms": (6, 20, "edit", True, 0, 0, (20, 20, 20, 20),
+                                    _h(BS, min_k=-30, max_k=30), 0, 3000),
+    "w1_edit_bstatic5_ms": (1, 40, "edit", False, 0, 0, None, _h(BS, min_k=-5, max_k=5), 0,
+                            400),
 }
 
 
@@ -321,23 +330,29 @@ def heuristics_fixtures():
     for name, spec in HEURISTIC_SETS.items():
         wl, n, pset, so, param, param2, form, hspec = spec[:8]
         mm = spec[8] if len(spec) > 8 else 0
+        ms = spec[9] if len(spec) > 9 else 0
         m, mi, mm_, o1, e1, o2, e2 = {**PENALTY_SETS, **EXTRA_SETS}[pset]
         pen = O.Penalties(metric=m, match=mi, mismatch=mm_, gap_opening1=o1, gap_extension1=e1,
                           gap_opening2=o2, gap_extension2=e2)
         h = heuristic_of(hspec)
         p = W.generate(wl, n, param=param, param2=param2)
         b = O.PairBatch(p.seqs, p.p_off, p.p_len, p.t_off, p.t_len)
-        a = O.align(b, pen, score_only=so, kind="port", form=form, heuristic=h, memory_mode=mm)
+        a = O.align(b, pen, score_only=so, kind="port", form=form, heuristic=h, memory_mode=mm,
+                    max_steps=ms)
+        # (an edit/indel pair the checker ends as unreachable never ends in the
+        # reference without a step limit: left out)
         keep = [i for i in range(n) if not (a.flags[i] & O.FLAG_OVER_BOUND)
                 and not (m <= 1 and a.status[i] == 1)]
         sub = O.PairBatch.from_lists([b.pattern(i) for i in keep], [b.text(i) for i in keep])
         r = O.align(sub, pen, score_only=so, kind="reference_scalar", form=form, heuristic=h,
-                    memory_mode=mm)
+                    memory_mode=mm, max_steps=ms)
         rows = [[int(r.score[j]), int(r.status[j]), crc(r.cigar(j)), int(r.end[j][0]),
                  int(r.end[j][1])] for j in range(sub.n)]
         heur[name] = {"workload": wl, "n": n, "param": param, "param2": param2,
                       "penalties": pset, "score_only": so, "form": form, "heuristic": hspec,
                       "memory_mode": mm, "keep": keep, "rows": rows}
+        if ms:
+            heur[name]["max_steps"] = ms
         print(name, "done", len(keep), "of", n)
     with open(os.path.join(HERE, "heuristics_expected.json"), "w") as f:
         json.dump(heur, f, separators=(",", ":"))

@@ -61,14 +61,15 @@ def _gpu(W, cfg, b):
     return out
 
 
-def _oracle_flags(O, pen_spec, b, score_only, form, hspec):
+def _oracle_flags(O, pen_spec, b, score_only, form, hspec, max_steps=0):
     pen = O.Penalties(**{"metric": pen_spec["metric"], "match": pen_spec["match"],
                          "mismatch": pen_spec["mismatch"],
                          "gap_opening1": pen_spec["gap_opening1"],
                          "gap_extension1": pen_spec["gap_extension1"],
                          "gap_opening2": pen_spec["gap_opening2"],
                          "gap_extension2": pen_spec["gap_extension2"]})
-    return O.align(b, pen, score_only=score_only, form=form, heuristic=O.Heuristic(**hspec))
+    return O.align(b, pen, score_only=score_only, form=form, heuristic=O.Heuristic(**hspec),
+                   max_steps=max_steps)
 
 
 @pytest.mark.parametrize("name", sorted(HX.keys()))
@@ -77,10 +78,11 @@ def test_heuristics_match_reference_fixtures(gpu_available, wfa, oracle_mod, nam
     fx = HX[name]
     spec = _spec(fx["penalties"])
     b = helpers.heuristic_pairs(O, W, fx)
-    ref = _oracle_flags(O, spec, b, fx["score_only"], fx["form"], fx["heuristic"])
+    ref = _oracle_flags(O, spec, b, fx["score_only"], fx["form"], fx["heuristic"],
+                        max_steps=fx.get("max_steps", 0))
     got = _gpu(W, W.Config(**spec, score_only=fx["score_only"], form=fx["form"],
-                           heuristic=fx["heuristic"],
-                           memory_mode=fx.get("memory_mode", 0)), b)
+                           heuristic=fx["heuristic"], memory_mode=fx.get("memory_mode", 0),
+                           max_steps=fx.get("max_steps", 0)), b)
     if got is None:
         return
     compared = 0

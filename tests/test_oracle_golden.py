@@ -112,7 +112,8 @@ def test_oracle_matches_reference_heuristics(oracle_mod, wfa, name):
     pen = _pen(O, UT["penalty_sets"][fx["penalties"]])
     b = helpers.heuristic_pairs(O, W, fx)
     r = O.align(b, pen, score_only=fx["score_only"], form=fx["form"],
-                heuristic=O.Heuristic(**fx["heuristic"]), memory_mode=fx.get("memory_mode", 0))
+                heuristic=O.Heuristic(**fx["heuristic"]), memory_mode=fx.get("memory_mode", 0),
+                max_steps=fx.get("max_steps", 0))
     assert len(fx["rows"]) == b.n
     for i, (score, status, c, ev, eh) in enumerate(fx["rows"]):
         got = (int(r.score[i]), int(r.status[i]), helpers.crc(r.cigar(i)), int(r.end[i][0]),

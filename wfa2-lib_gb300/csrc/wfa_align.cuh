@@ -655,7 +655,13 @@ __global__ void __launch_bounds__(256, WF2G_MIN_BLOCKS) wfa_align_kernel(const K
           }
         }
       } else if (null_steps > pen.R) {
-        result = 3;
+        // Edit and indel: the reference counts null steps only for a missing
+        // wavefront (wavefront/wavefront_extend.c:93-101) and its edit driver
+        // allocates every one, so null steps do not end it; no later cell can
+        // be valid, and only the step limit does (wavefront/wavefront_
+        // unialign.c:102-107).  Without a step limit it never ends: reported
+        // unreachable here.
+        result = (edit_like && p.max_steps != INT32_MAX) ? 2 : 3;
         break;
       }
 
