@@ -249,3 +249,21 @@ def test_maxtrim_and_display_on_host(wfa, tmp_path):
     libc.fclose(fp)
     assert out.read_text() == "WFA(alignment,end2end)(MHigh,inf)"
     L.wavefront_aligner_delete(h)
+
+
+def test_fast_pass_kernel_table(wfa):
+    """The two-diagonal fast pass's kernel table (wfa2-lib_gb300/csrc/wfa_fast2.cu):
+    every (full CIGAR, o+e even, row width, default penalties, cut-off)
+    instance the engine asks for exists, except the score-only cut-off kernel
+    with rows of 1536 diagonals, which is not built (that second pass takes
+    rows of 2048).  The table only hands out kernel addresses: no GPU call."""
+    fn = wfa.lib().wf2g_fast2_kernel_ptr
+    fn.restype = C.c_void_p
+    fn.argtypes = [C.c_int] * 5
+    for width in (1024, 1536, 2048):
+        for cigar in (0, 1):
+            assert fn(cigar, 1, width, 1, 0) and fn(cigar, 1, width, 0, 0), (width, cigar)
+            assert fn(cigar, 0, width, 0, 0), (width, cigar)
+            assert bool(fn(cigar, 1, width, 1, 1)) == (cigar == 1 or width != 1536), (width, cigar)
+            assert not fn(cigar, 1, width, 0, 1), (width, cigar)  # cut-off: default penalties only
+    assert not fn(1, 1, 512, 1, 0) and not fn(0, 1, 4096, 1, 0)
