@@ -1082,7 +1082,11 @@ int oracle_ua_extend(oracle_ua_t* ua, int* max_ak) {
   if (max_ak) *max_ak = 0;
   orow_t* m = row_at(ws, ua->s, C_M);
   if (!m->exists) {
-    if (ua->null_steps > ua->p->scope) return ST_END_UNREACHABLE;
+    /* (edit and indel with a step limit run on past null wavefronts, as
+     * the reference's edit driver does: see align_one_impl) */
+    if (ua->null_steps > ua->p->scope &&
+        !(ua->p->metric <= 1 && ua->p->max_steps != INT_MAX))
+      return ST_END_UNREACHABLE;
     return 0;
   }
   int mak = 0;

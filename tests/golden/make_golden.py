@@ -227,6 +227,11 @@ HEURISTIC_SETS = {
                                     _h(BS, min_k=-30, max_k=30), 0, 3000),
     "w1_edit_bstatic5_ms": (1, 40, "edit", False, 0, 0, None, _h(BS, min_k=-5, max_k=5), 0,
                             400),
+    # ... and in BiWFA's breakpoint searches, which step on to the step limit
+    "w6_edit_biwfa_bstatic_score_ms": (6, 20, "edit", True, 0, 0, None,
+                                       _h(BS, min_k=-30, max_k=30), 3, 3000),
+    "w1_indel_biwfa_bstatic5_ms": (1, 40, "indel", False, 0, 0, None,
+                                   _h(BS, min_k=-5, max_k=5), 3, 400),
 }
 
 

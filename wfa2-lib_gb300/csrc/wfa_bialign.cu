@@ -281,8 +281,10 @@ struct BiCtx {
       }
       __syncthreads();
       mak_out = 0;
-      // wavefront/wavefront_extend.c:183-192
-      return nulls[d] > scope ? 2 : 0;
+      // wavefront/wavefront_extend.c:183-192.  Edit and indel with a step
+      // limit run on: the reference's edit driver allocates every wavefront,
+      // so its null-step count never ends them, only the step limit does.
+      return nulls[d] > scope && !edit_runs_on() ? 2 : 0;
     }
     nulls[d] = 0;
 
@@ -824,6 +826,16 @@ struct BiCtx {
     __syncthreads();
   }
 
+  // Edit and indel with a step limit do not end on null wavefronts.
+  __device__ bool edit_runs_on() const { return p.metric <= 1 && p.max_steps != INT_MAX; }
+
+  // Scores past the segment's bound: no alignment scores that high, so an
+  // edit or indel search that runs on would reach its step limit.
+  __device__ void guard_reached(BiOut& res) {
+    if (edit_runs_on()) res.status = kBiMaxSteps;
+    else finish(res, 3, 0);
+  }
+
   __device__ void finish(BiOut& res, int r, int d) {
     if (r == 1) {
       res.status = kBiEndReached;
@@ -857,7 +869,7 @@ struct BiCtx {
         res.status = kBiMaxSteps;
         return;
       }
-      if (s[0] + s[1] > guard) return finish(res, 3, 0);
+      if (s[0] + s[1] > guard) return guard_reached(res);
     }
     // wavefront/wavefront_bialign.c:960-973
     const Penalties& pen = p.pen;
@@ -883,7 +895,7 @@ struct BiCtx {
         res.status = kBiMaxSteps;
         return;
       }
-      if (s[0] + s[1] > guard) return finish(res, 3, 0);
+      if (s[0] + s[1] > guard) return guard_reached(res);
       last_fwd = true;
     }
     res.status = kBiOk;
